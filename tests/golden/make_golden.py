@@ -1,0 +1,288 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container where the GEOSmie sources are present:
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+It imports the reference's own Python code -- pymiecoated (mie_coated.Mie,
+MultipleMie, mie_coeffs, mie_props) and geosmie/dointegration.fun -- with
+three shims for modules this image lacks: a no-op ``numba`` (the reference
+then runs as plain Python), an in-memory ``netCDF4.Dataset`` that records the
+variables dointegration.fun writes, and an empty ``matplotlib`` (imported by
+carma_utils but not used on this path).  numpy 2 removed ``np.trapz``, which
+dointegration.py:979 calls; it is aliased to ``np.trapezoid``.
+
+Outputs (small .npz files, committed):
+  mie_single.npz   homogeneous Mie(m=..., x=...) and Mie(eps=, mu=, x=):
+                   a_n/b_n, the six efficiencies, S1/S2 at five cosines
+  mie_coated.npz   coated Mie(m=, m2=, x=, y=): efficiencies, S1/S2, a_n/b_n
+  size_range.npz   MultipleMie(...).calculateS12SizeRange(mr, mi)
+  table_*.npz      dointegration.fun on small particle definitions, with the
+                   inputs (JSON text, refractive-index tables, water table)
+                   needed to rerun them without the reference tree.
+"""
+import argparse
+import contextlib
+import io
+import json
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+# --------------------------------------------------------------------------
+# shims
+# --------------------------------------------------------------------------
+def _install_shims():
+    numba = types.ModuleType("numba")
+
+    def jit(*a, **k):
+        if a and callable(a[0]) and len(a) == 1 and not k:
+            return a[0]
+        return lambda f: f
+    numba.jit = jit
+    numba.njit = jit
+    sys.modules["numba"] = numba
+
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    mpl.use = lambda *a, **k: None
+    sys.modules["matplotlib"] = mpl
+    sys.modules["matplotlib.pyplot"] = plt
+
+    nc = types.ModuleType("netCDF4")
+
+    class Var:
+        def __init__(self, shape):
+            self.data = np.zeros(shape)
+
+        def __setitem__(self, k, v):
+            self.data[k] = v
+
+        def __getitem__(self, k):
+            return self.data[k]
+
+    class Dataset:
+        opened = []
+
+        def __init__(self, path, mode="r"):
+            self.path = path
+            self.dims = {}
+            self.variables = {}
+            Dataset.opened.append(self)
+
+        def createDimension(self, name, size):
+            self.dims[name] = size
+
+        def createVariable(self, name, dtype, dims, **kw):
+            if isinstance(dims, str):
+                dims = (dims,)
+            v = Var(tuple(self.dims[d] for d in dims))
+            v.dims = dims
+            self.variables[name] = v
+            return v
+
+        def close(self):
+            pass
+
+    nc.Dataset = Dataset
+    sys.modules["netCDF4"] = nc
+    if not hasattr(np, "trapz"):
+        np.trapz = np.trapezoid
+    return Dataset
+
+
+def _c(lst):
+    return np.array(lst, dtype=np.complex128)
+
+
+def _ragged(arrs):
+    off = np.zeros(len(arrs) + 1, dtype=np.int64)
+    off[1:] = np.cumsum([len(a) for a in arrs])
+    return np.concatenate(arrs) if arrs else np.zeros(0, np.complex128), off
+
+
+U_LIST = [1.0, 0.5, 0.0, -0.6, -1.0]
+
+
+def gen_single(ref_mie):
+    Mie = ref_mie.Mie
+    from pymiecoated import mie_coeffs as mc
+    xs = list(np.logspace(-3, np.log10(650.0), 22)) + [2.5, 4.0, 114.2]
+    ms = [1.33 + 1e-9j, 1.53 + 0.008j, 1.5 + 0.5j, 1.95 + 0.79j, 1.1 + 0.0j, 3.0 + 4.0j]
+    rows_x, rows_eps, rows_mu, eff, s1, s2, ans, bns = [], [], [], [], [], [], [], []
+    cases = [(x, m * m, 1.0 + 0j) for m in ms for x in xs]
+    cases += [(x, 2.2 + 0.8j, 1.6 + 1.4j) for x in [0.05, 0.5, 4.0, 20.0, 80.0]]
+    for x, eps, mu in cases:
+        mie = Mie(eps=eps, mu=mu, x=x)
+        eff.append([mie.qext(), mie.qsca(), mie.qabs(), mie.qb(), mie.asy(), mie.qratio()])
+        ss = [mie.S12(u) for u in U_LIST]
+        s1.append([a for a, _ in ss])
+        s2.append([b for _, b in ss])
+        an, bn, _ = mc.single_mie_coeff(complex(eps), complex(mu), float(x), [], [])
+        ans.append(an)
+        bns.append(bn)
+        rows_x.append(x)
+        rows_eps.append(eps)
+        rows_mu.append(mu)
+    an_all, off = _ragged(ans)
+    bn_all, _ = _ragged(bns)
+    np.savez_compressed(os.path.join(HERE, "mie_single.npz"), x=np.array(rows_x), eps=_c(rows_eps),
+                        mu=_c(rows_mu), eff=np.array(eff), u=np.array(U_LIST), s1=_c(s1), s2=_c(s2),
+                        an=an_all, bn=bn_all, offsets=off)
+    print("mie_single: %d instances, sum nmax %d" % (len(rows_x), off[-1]))
+
+
+def gen_coated(ref_mie):
+    Mie = ref_mie.Mie
+    from pymiecoated import mie_coeffs as mc
+    cases = [(1.5, 5.0, 1.5 + 0.5j, 1.2 + 0.2j)]  # test_mie.py:68
+    for y in [0.05, 0.3, 1.0, 5.0, 20.0, 62.8]:
+        for f in [0.05, 0.2, 0.5]:
+            cases.append((y * f ** (1.0 / 3.0), y, 1.95 + 0.79j, 1.53 + 0.01j))
+    cases += [(3.0, 8.0, 1.33 + 0.0j, 1.6 + 0.1j), (0.4, 0.9, 2.0 + 1.0j, 1.4 + 1e-6j)]
+    xs, ys, m1s, m2s, eff, s1, s2, ans, bns = [], [], [], [], [], [], [], [], []
+    for x, y, m1, m2 in cases:
+        mie = Mie(m=m1, m2=m2, x=x, y=y)
+        eff.append([mie.qext(), mie.qsca(), mie.qabs(), mie.qb(), mie.asy(), mie.qratio()])
+        ss = [mie.S12(u) for u in U_LIST]
+        s1.append([a for a, _ in ss])
+        s2.append([b for _, b in ss])
+        an, bn, _ = mc.coated_mie_coeff(m1 * m1, m2 * m2, x, y)
+        ans.append(an)
+        bns.append(bn)
+        xs.append(x)
+        ys.append(y)
+        m1s.append(m1)
+        m2s.append(m2)
+    an_all, off = _ragged(ans)
+    bn_all, _ = _ragged(bns)
+    np.savez_compressed(os.path.join(HERE, "mie_coated.npz"), x=np.array(xs), y=np.array(ys),
+                        m1=_c(m1s), m2=_c(m2s), eff=np.array(eff), u=np.array(U_LIST),
+                        s1=_c(s1), s2=_c(s2), an=an_all, bn=bn_all, offsets=off)
+    print("mie_coated: %d instances" % len(xs))
+
+
+def gen_size_range(ref_mie):
+    lam = 0.55e-6
+    r = np.logspace(np.log10(0.01e-6), np.log10(10e-6), 80)
+    x = 2 * np.pi * r / lam
+    ang = np.linspace(0.0, 180.0, 37)
+    cost = np.cos(np.radians(ang))
+    mm = ref_mie.MultipleMie(x, None, cost)
+    mm.preCalculate()
+    v = mm.calculateS12SizeRange(1.53, 0.008)
+    s1 = _c([[a for a, _ in row] for row in v["s12"]])
+    s2 = _c([[b for _, b in row] for row in v["s12"]])
+    np.savez_compressed(os.path.join(HERE, "size_range.npz"), x=x, cost=cost, mr=1.53, mi=0.008,
+                        s1=s1, s2=s2, **{k: np.array(v[k]) for k in
+                                         ["qext", "qsca", "qabs", "asy", "qb", "qratio"]})
+    print("size_range: %d sizes x %d angles" % (len(x), len(cost)))
+
+
+TABLE_CASES = {
+    # lognormal, 'simple' growth, a one-mode bin and a two-mode bin
+    "lognorm": {
+        "rhop0": 1700.0,
+        "rh": [0.0, 0.5, 0.9, 0.99],
+        "rhDep": {"type": "simple", "params": {"gf": [1.0, 1.39, 1.77, 2.16]}},
+        "psd": {"type": "lognorm", "params": {
+            "r0": [[0.0695e-6], [0.05e-6, 0.3e-6]],
+            "rmin0": [[0.005e-6], [0.005e-6, 0.005e-6]],
+            "rmax0": [[0.3e-6], [0.5e-6, 0.5e-6]],
+            "sigma": [[2.03], [1.8, 2.2]],
+            "numperdec": [18, 12],
+            "fracs": [[1.0], [0.7, 0.3]]}},
+        "ri": [[0.40, 1.45, -1e-8], [0.55, 1.43, -1e-8], [1.00, 1.42, -2e-6]],
+    },
+    # 'trivial' growth (RH > 0 copies RH = 0), absorbing, rhop0 per bin, maxrh
+    "trivial": {
+        "rhop0": [1800.0],
+        "rh": [0.0, 0.8, 0.95],
+        "maxrh": 0.9,
+        "rhDep": {"type": "trivial", "params": {"gf": [1.0, 1.0, 1.0]}},
+        "psd": {"type": "lognorm", "params": {
+            "r0": [[0.0118e-6]], "rmin0": [[0.001e-6]], "rmax0": [[0.3e-6]],
+            "sigma": [[2.0]], "numperdec": [15], "fracs": [[1.0]]}},
+        "ri": [[0.35, 1.75, -0.46], [0.55, 1.75, -0.44], [1.2, 1.77, -0.45]],
+    },
+    # sea-salt: Gerber growth, Gong PSD, maxrh capping
+    "seasalt": {
+        "rhop0": 2200.0,
+        "rh": [0.0, 0.5, 0.95, 0.98],
+        "maxrh": 0.95,
+        "rhDep": {"type": "ss", "params": {"c1": 0.7674, "c2": 3.079, "c3": 2.573e-11, "c4": -1.424}},
+        "psd": {"type": "ss", "params": {
+            "rMinMaj": [0.1e-6], "rMaxMaj": [0.5e-6], "fracs": [[1.0]], "numperdec": [12]}},
+        "ri": [[0.44, 1.50, -1e-8], [0.87, 1.48, -1e-6]],
+    },
+}
+
+
+def gen_tables(ref_src, Dataset):
+    geosmie_dir = os.path.join(ref_src, "geosmie")
+    import dointegration
+    import particleparams as pp
+    cwd = os.getcwd()
+    os.chdir(geosmie_dir)
+    try:
+        waterm = pp.getWaterM()
+    finally:
+        os.chdir(cwd)
+    for name, case in TABLE_CASES.items():
+        with tempfile.TemporaryDirectory() as td:
+            ri = np.array(case["ri"], dtype=np.float64)
+            rifile = os.path.join(td, "ri-%s.wsv" % name)
+            np.savetxt(rifile, ri, header="lambda[um] m_real m_imaginary")
+            params = {k: v for k, v in case.items() if k != "ri"}
+            params["ri"] = {"format": "wsv", "path": [rifile]}
+            jfile = os.path.join(td, "%s.json" % name)
+            with open(jfile, "w") as fp:
+                json.dump(params, fp)
+            Dataset.opened.clear()
+            os.chdir(geosmie_dir)
+            try:
+                with contextlib.redirect_stdout(io.StringIO()):
+                    dointegration.fun(jfile, "json", td, False)
+            finally:
+                os.chdir(cwd)
+            ds = Dataset.opened[-1]
+            out = {("out_" + k): v.data for k, v in ds.variables.items()}
+            params_rec = dict(params)
+            params_rec["ri"] = {"format": "wsv", "path": ["<inline>"]}
+            mlist = pp.getMSep(rifile, None)
+            np.savez_compressed(os.path.join(HERE, "table_%s.npz" % name),
+                                params_json=json.dumps(params_rec), mlist=np.array([mlist]),
+                                waterm=np.array(waterm), **out)
+            print("table_%s: p11 %s" % (name, out["out_p11"].shape))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default="")
+    a = ap.parse_args()
+    src = os.path.join(a.ref, "src")
+    Dataset = _install_shims()
+    sys.path.insert(0, os.path.join(src, "pymiecoated"))
+    sys.path.insert(0, os.path.join(src, "geosmie"))
+    from pymiecoated import mie_coated
+    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables"]
+    if "single" in sel:
+        gen_single(mie_coated)
+    if "coated" in sel:
+        gen_coated(mie_coated)
+    if "size_range" in sel:
+        gen_size_range(mie_coated)
+    if "tables" in sel:
+        gen_tables(src, Dataset)
+
+
+if __name__ == "__main__":
+    main()
