@@ -1,0 +1,692 @@
+// Table generation: the (bin x wavelength x RH) sweep of
+// geosmie/dointegration.py:786-1031 on the GPU, FP64 ("plain") form.
+//
+// Work decomposition
+//   instance  = (wavelength, RH, component, size)           Mie evaluation
+//   unit      = (wavelength, RH, component)                 shares m
+//   entry     = (bin, wavelength, RH)                       one table row
+// Size grids: GBMIE_GRID_X (one x grid for all wavelengths, the reference's
+// layout) or GBMIE_GRID_RADIUS (x = 2 pi r / lambda).  The "x-grid set" le
+// is 0 for GRID_X and the wavelength for GRID_RADIUS.
+//
+// Device data (context scratch, carved by the plan):
+//   pc     psi_n/chi_n rows of every (le, size), orders 1..nmax, CSR by off
+//   an,bn  coefficients of every instance, unit_base[unit] + off[le, i]
+//   eff4   (qext, qsca, qb, asy) per instance
+//   W      PSD weights [wl][rh][bin][comp][size]; sums [..][4] (num, S r^2 w,
+//          S r^3 w, S r^4 w); reff0 [wl][bin][comp]
+//   pacc   number-weighted Mueller sums [wl][rh][bin][4][ang]
+//          (s11, s12, s33, s34; s22 = s11 and s44 = s33 by construction,
+//          dointegration.py:1044-1050)
+#include "common.cuh"
+#include "mie_device.cuh"
+#include "gsf.cuh"
+
+#define TWO_PI 6.28318530717958647692
+#define PI_D 3.14159265358979323846
+
+struct gbmie_table_plan {
+    gbmie_ctx *ctx;
+    gbmie_table_desc d;
+    int n_le;
+    int64_t n_units, n_inst, n_entries;
+    double *xg;          // [n_le][n_size]
+    int64_t *off;        // [n_le * n_size + 1]
+    int64_t *unit_base;  // [n_units]
+    int64_t pc_total, ab_total;
+    int nmax_max;
+    size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
+    GsfTables gsf;
+    int has_gsf;
+};
+
+// ---------------------------------------------------------------------------
+// block reduction of K doubles (all threads receive the totals)
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K])
+{
+    __shared__ double red[32][K];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) red[wid][k] = v[k];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? red[lane][k] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) red[0][k] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = red[0][k];
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// plan kernels
+// ---------------------------------------------------------------------------
+__global__ void k_tab_make_x(int n_le, int n_size, int grid_kind, const double *__restrict__ grid,
+                             const double *__restrict__ lambda, double *__restrict__ xg, int *flags)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (int64_t)n_le * n_size) return;
+    const int le = (int)(j / n_size), i = (int)(j % n_size);
+    const double g = grid[i];
+    const double x = grid_kind == GBMIE_GRID_X ? g : TWO_PI * g / lambda[le];
+    if (!(x > 0.0) || !isfinite(x)) atomicOr(flags, GBMIE_FLAG_INVALID);
+    xg[j] = x;
+}
+
+// ---------------------------------------------------------------------------
+// run kernels
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_tab_psi_chi(int64_t nrows, const double *__restrict__ xg,
+                                                     const int64_t *__restrict__ off, double2 *__restrict__ pc)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nrows) return;
+    const int64_t o = off[j];
+    psi_chi_row(xg[j], (int)(off[j + 1] - o), pc + o);
+}
+
+struct TabView {
+    int n_lambda, n_rh, n_size, n_bin, n_comp, n_ang, grid_kind, psd_kind, rh0;
+    const double *lambda, *grid, *dgrid, *psd_param, *gf_psd, *frac, *rhop, *rhop0, *gf, *rlow, *rup;
+    const double *theta;
+    const double2 *m;
+    const double *xg;
+    const int64_t *off, *unit_base;
+    double2 *pc, *an, *bn;
+    double *eff4, *W, *sums, *reff0, *pacc, *sraw, *nlraw;
+    const double2 *pq;
+    __device__ __forceinline__ int le(int lam) const { return grid_kind == GBMIE_GRID_X ? 0 : lam; }
+    __device__ __forceinline__ double radius(int lam, int i) const {
+        return grid_kind == GBMIE_GRID_RADIUS ? grid[i] : xg[i] * lambda[lam] / TWO_PI;
+    }
+};
+
+// PSD weights of (lam, rh, bin, comp): lognormal dN/dx x dgrid or r^-4 x
+// dgrid, normalised (dointegration.py:546-583, 626-662), or the caller's
+// weights; plus the radius moments and the dry effective radius.
+__global__ void __launch_bounds__(256) k_tab_weights(TabView v, const double *__restrict__ wgiven)
+{
+    const int blk = blockIdx.x;   // ((lam * n_rh + rh) * n_bin + bin) * n_comp + comp
+    const int comp = blk % v.n_comp;
+    const int bin = (blk / v.n_comp) % v.n_bin;
+    const int rh = (blk / (v.n_comp * v.n_bin)) % v.n_rh;
+    const int lam = blk / (v.n_comp * v.n_bin * v.n_rh);
+    const int n = v.n_size;
+    double *W = v.W + (size_t)blk * n;
+    const double *xs = v.xg + (size_t)v.le(lam) * n;
+    const double *pp = v.psd_param + ((size_t)bin * v.n_comp + comp) * 4;
+    const double lamv = v.lambda[lam];
+    const double xconv = TWO_PI / lamv;
+    double tot[1] = {0.0};
+    if (v.psd_kind == GBMIE_PSD_WEIGHTS) {
+        const double *src = wgiven + (size_t)blk * n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) W[i] = src[i];
+        tot[0] = 1.0;
+    } else if (v.psd_kind == GBMIE_PSD_LOGNORM) {
+        const double gfp = v.gf_psd[rh];
+        const double xmode = pp[0] * gfp * xconv, xmin = pp[1] * xconv, xmax = pp[2] * gfp * xconv;
+        const double lns = log(pp[3]);
+        const double c0 = 1.0 / (sqrt(TWO_PI) * lns), c1 = 1.0 / (2.0 * lns * lns);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double x = xs[i];
+            double w = 0.0;
+            if (x < xmax && x > xmin) {
+                const double l = log(x / xmode);
+                w = c0 / x * exp(-(l * l) * c1) * v.dgrid[i];
+            }
+            W[i] = w;
+            tot[0] += w;
+        }
+        block_sum<1>(tot);
+    } else {   // GBMIE_PSD_POWER4
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double r = v.radius(lam, i);
+            double w = 0.0;
+            if (!(r < pp[0]) && !(r > pp[1])) w = 1.0 / (r * r * r * r) * v.dgrid[i];
+            W[i] = w;
+            tot[0] += w;
+        }
+        block_sum<1>(tot);
+    }
+    const double inv = (v.psd_kind == GBMIE_PSD_WEIGHTS || tot[0] == 0.0) ? 1.0 : 1.0 / tot[0];
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double w = W[i] * inv;
+        if (v.psd_kind != GBMIE_PSD_WEIGHTS) W[i] = w;
+        const double r = v.radius(lam, i);
+        const double r2 = r * r * w;
+        s[0] += w;
+        s[1] += r2;
+        s[2] += r2 * r;
+        s[3] += r2 * r * r;
+    }
+    block_sum<4>(s);
+    if (threadIdx.x == 0) {
+        double *o = v.sums + (size_t)blk * 4;
+        o[0] = s[0];
+        o[1] = s[1];
+        o[2] = s[2];
+        o[3] = s[3];
+        if (rh == v.rh0) v.reff0[((size_t)lam * v.n_bin + bin) * v.n_comp + comp] = s[3] / s[2];
+    }
+}
+
+// Coefficients + per-instance efficiencies, one thread per instance.
+struct EmitTab {
+    double2 *an, *bn;
+    __device__ __forceinline__ void operator()(int k, cplx a, cplx b) const {
+        an[k - 1] = d2(a);
+        bn[k - 1] = d2(b);
+    }
+};
+
+__global__ void __launch_bounds__(128) k_tab_coeffs(TabView v, int64_t n_inst, int *flags)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_inst) return;
+    const int i = (int)(t % v.n_size);
+    const int64_t unit = t / v.n_size;
+    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+    const int le = v.le(lam);
+    const int64_t row = (int64_t)le * v.n_size + i;
+    const int64_t o = v.off[row];
+    const int nmax = (int)(v.off[row + 1] - o);
+    const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
+    const double x = v.xg[row];
+    const cplx m = cx(v.m[unit]);
+    if (!isfinite(m.re) || !isfinite(m.im)) atomicOr(flags, GBMIE_FLAG_INVALID);
+    EmitTab emit{v.an + c, v.bn + c};
+    EffSums es;
+    homog_instance(x, m * m, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
+    double e[6];
+    es.finish(x, e);
+    double *o4 = v.eff4 + t * 4;
+    o4[0] = e[0];
+    o4[1] = e[1];
+    o4[2] = e[3];
+    o4[3] = e[4];
+}
+
+// Fused S+/S- sums, Mueller elements and number-weighted size integration
+// (rawMie + calculateScatVals + the phase part of integratePSD,
+// dointegration.py:1044-1050, 1160-1166).  Block = (unit, chunk of sizes);
+// threads over angles; the chunk's coefficients (contiguous in memory)
+// streamed through shared memory as (a+b, a-b).
+#define TAB_CAP 2048
+template <int NB>
+__global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int nchunk)
+{
+    __shared__ double2 cd[TAB_CAP][2];
+    const int64_t unit = blockIdx.x / nchunk;
+    const int ch = blockIdx.x % nchunk;
+    const int comp = (int)(unit % v.n_comp);
+    const int64_t lr = unit / v.n_comp;   // lam * n_rh + rh
+    const int lam = (int)(lr / v.n_rh);
+    const int le = v.le(lam);
+    const int i0 = ch * chunk, i1 = min(v.n_size, i0 + chunk);
+    if (i0 >= i1) return;
+    const int64_t *off = v.off + (int64_t)le * v.n_size;   // off[i] for this x grid
+    const int64_t cbase = v.unit_base[unit] - off[0];
+    const double2 *A = v.an + cbase, *B = v.bn + cbase;
+    const int64_t wstride = v.n_size;
+    const double *Wb = v.W + (size_t)lr * v.n_bin * v.n_comp * wstride + (size_t)comp * wstride;
+    const int nang = v.n_ang;
+    for (int a0 = 0; a0 < nang; a0 += blockDim.x) {
+        const int a = a0 + threadIdx.x;
+        const bool act = a < nang;
+        double acc[NB][4];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) acc[b][0] = acc[b][1] = acc[b][2] = acc[b][3] = 0.0;
+        double sp_r = 0, sp_i = 0, sm_r = 0, sm_i = 0;
+        int j = i0;                // current size
+        int64_t pos = off[i0];     // next unconsumed coefficient (CSR position)
+        const int64_t pend = off[i1];
+        while (pos < pend) {
+            const int64_t cnt = min((int64_t)TAB_CAP, pend - pos);
+            __syncthreads();
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+                const double2 av = A[pos + k], bv = B[pos + k];
+                cd[k][0] = make_double2(av.x + bv.x, av.y + bv.y);
+                cd[k][1] = make_double2(av.x - bv.x, av.y - bv.y);
+            }
+            __syncthreads();
+            int64_t p = pos;
+            const int64_t pe = pos + cnt;
+            while (p < pe) {
+                const int64_t jb = off[j], je = off[j + 1];
+                const int64_t stop = min(je, pe);
+                if (act) {
+                    const double2 *col = v.pq + (int64_t)(p - jb) * nang + a;
+                    for (int64_t q = p; q < stop; ++q) {
+                        const double2 t = *col;
+                        col += nang;
+                        const double2 c = cd[q - pos][0], d = cd[q - pos][1];
+                        sp_r = fma(c.x, t.x, sp_r);
+                        sp_i = fma(c.y, t.x, sp_i);
+                        sm_r = fma(d.x, t.y, sm_r);
+                        sm_i = fma(d.y, t.y, sm_i);
+                    }
+                }
+                p = stop;
+                if (stop == je) {   // size j complete
+                    if (act) {
+                        const double A2 = sp_r * sp_r + sp_i * sp_i, B2 = sm_r * sm_r + sm_i * sm_i;
+                        const double s11 = 0.25 * (A2 + B2);
+                        const double s12 = -0.5 * (sp_r * sm_r + sp_i * sm_i);
+                        const double s33 = 0.25 * (A2 - B2);
+                        const double s34 = -0.5 * (sm_r * sp_i - sm_i * sp_r);
+#pragma unroll
+                        for (int b = 0; b < NB; ++b) {
+                            if (b < v.n_bin) {
+                                const double w = Wb[(size_t)b * v.n_comp * wstride + j];
+                                acc[b][0] = fma(w, s11, acc[b][0]);
+                                acc[b][1] = fma(w, s12, acc[b][1]);
+                                acc[b][2] = fma(w, s33, acc[b][2]);
+                                acc[b][3] = fma(w, s34, acc[b][3]);
+                            }
+                        }
+                    }
+                    sp_r = sp_i = sm_r = sm_i = 0.0;
+                    ++j;
+                }
+            }
+            pos = pe;
+        }
+        if (act) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                if (b < v.n_bin) {
+                    const double f = v.frac[(size_t)b * v.n_comp + comp];
+                    double *dst = v.pacc + (((size_t)lr * v.n_bin + b) * 4) * nang + a;
+                    atomicAdd(dst, f * acc[b][0]);
+                    atomicAdd(dst + nang, f * acc[b][1]);
+                    atomicAdd(dst + 2 * nang, f * acc[b][2]);
+                    atomicAdd(dst + 3 * nang, f * acc[b][3]);
+                }
+            }
+        }
+    }
+}
+
+// Scalar integration of integratePSD ('dumix', dointegration.py:1064-1209),
+// one block per (lam, rh, bin).  sraw: qext qsca qabs qb g csca cext bsca
+// bext bbck; nlraw: mass volume area rEff rMass (before division by mass0).
+__global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
+{
+    const int blk = blockIdx.x;   // (lam * n_rh + rh) * n_bin + bin
+    const int bin = blk % v.n_bin;
+    const int64_t lr = blk / v.n_bin;
+    const int rh = (int)(lr % v.n_rh), lam = (int)(lr / v.n_rh);
+    const double rhop = v.rhop[(size_t)bin * v.n_rh + rh];
+    const double rhop0 = v.rhop0[bin];
+    double R[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) R[k] = 0.0;   // frac-weighted accumulated results
+    for (int comp = 0; comp < v.n_comp; ++comp) {
+        const int64_t unit = lr * v.n_comp + comp;
+        const double *W = v.W + (((size_t)lr * v.n_bin + bin) * v.n_comp + comp) * v.n_size;
+        const double *E = v.eff4 + (size_t)unit * v.n_size * 4;
+        double s[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) s[k] = 0.0;
+        for (int i = threadIdx.x; i < v.n_size; i += blockDim.x) {
+            const double w = W[i];
+            const double r = v.radius(lam, i);
+            const double A = PI_D * r * r;
+            const double qext = E[4 * i], qsca = E[4 * i + 1], qb = E[4 * i + 2], g = E[4 * i + 3];
+            const double wa = w * A, was = wa * qsca;
+            s[0] += wa;                     // sum w A
+            s[1] += qext * wa;
+            s[2] += qsca * wa;
+            s[3] += (qext - qsca) * wa;
+            s[4] += qb * wa;
+            s[5] += g * was;                // weights aliased to A qsca from 'g' on
+            s[6] += qsca * A * was;         // csca_i = qsca_i pi r^2
+            s[7] += qext * A * was;         // cext_i = qext_i pi r^2
+            s[8] += was;
+        }
+        block_sum<9>(s);
+        if (threadIdx.x == 0) {
+            const double *m4 = v.sums + (((size_t)lr * v.n_bin + bin) * v.n_comp + comp) * 4;
+            const double num = m4[0], s2 = m4[1], s3 = m4[2], s4 = m4[3];
+            const double reff0 = v.reff0[((size_t)lam * v.n_bin + bin) * v.n_comp + comp];
+            const double area = PI_D * s2 / num;
+            const double volume = 4.0 / 3.0 * PI_D * s3 / num;
+            const double mass = volume * rhop;
+            const double reff = s3 / s2;
+            const double reffm = s4 / s3;
+            const double rmass = 4.0 / 3.0 * PI_D * rhop * reffm * reffm * reffm;
+            const double rmass0 = 4.0 / 3.0 * PI_D * rhop0 * reff0 * reff0 * reff0;
+            const double qext = s[1] / s[0], qsca = s[2] / s[0], qabs = s[3] / s[0];
+            const double qb = s[4] / s[2] * qsca;   // p11back qsca / (4 pi)
+            const double g = s[5] / s[8], csca = s[6] / s[8], cext = s[7] / s[8];
+            const double conv = 1.0 / rhop / reff * rmass / rmass0;
+            const double f = v.frac[(size_t)bin * v.n_comp + comp];
+            const double vals[15] = {qext, qsca, qabs, qb, g, csca, cext, 0.75 * qsca * conv, 0.75 * qext * conv,
+                                     0.75 * qb * conv / (4.0 * PI_D), mass, volume, area, reff, rmass};
+#pragma unroll
+            for (int k = 0; k < 15; ++k) R[k] += f * vals[k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double *so = v.sraw + (size_t)blk * 10;
+        for (int k = 0; k < 10; ++k) so[k] = R[k];
+        double *no = v.nlraw + (size_t)blk * 5;
+        for (int k = 0; k < 5; ++k) no[k] = R[10 + k];
+    }
+}
+
+// Phase normalisation and the per-entry outputs (dointegration.py:950-1001).
+__global__ void __launch_bounds__(256) k_tab_finalize(TabView v, gbmie_table_out out)
+{
+    const int blk = blockIdx.x;   // (lam * n_rh + rh) * n_bin + bin
+    const int bin = blk % v.n_bin;
+    const int64_t lr = blk / v.n_bin;
+    const int rh = (int)(lr % v.n_rh), lam = (int)(lr / v.n_rh);
+    const int nang = v.n_ang;
+    const double *P = v.pacc + (size_t)blk * 4 * nang;
+    // trapz(p11 sin(theta), theta)
+    double tr[1] = {0.0};
+    for (int a = threadIdx.x; a < nang - 1; a += blockDim.x) {
+        const double t0 = v.theta[a], t1 = v.theta[a + 1];
+        tr[0] += (t1 - t0) * (P[a] * sin(t0) + P[a + 1] * sin(t1)) * 0.5;
+    }
+    block_sum<1>(tr);
+    const size_t e = ((size_t)bin * v.n_lambda + lam) * v.n_rh + rh;   // output entry
+    double *ph = out.phase + e * 6 * nang;
+    for (int a = threadIdx.x; a < nang; a += blockDim.x) {
+        const double p11 = P[a], p12 = P[nang + a], p33 = P[2 * nang + a], p34 = P[3 * nang + a];
+        const double p11n = 2.0 * p11 / tr[0];
+        const double p12n = p12 * p11n / p11, p22n = p11 * p11n / p11;
+        const double p33n = p33 * p11n / p11, p34n = p34 * p11n / p11;
+        ph[a] = p11n;
+        ph[nang + a] = p12n;
+        ph[2 * nang + a] = p22n;
+        ph[3 * nang + a] = p33n;
+        ph[4 * nang + a] = p34n;
+        ph[5 * nang + a] = p33n;
+        if (a == nang - 1 && out.pback) {
+            double *pb = out.pback + e * 6;   // p11 p12 p33 p34 p22 p44
+            pb[0] = p11n;
+            pb[1] = p12n;
+            pb[2] = p33n;
+            pb[3] = p34n;
+            pb[4] = p22n;
+            pb[5] = p33n;
+        }
+    }
+    if (threadIdx.x == 0) {
+        const double *s = v.sraw + (size_t)blk * 10;
+        const double2 m0 = v.m[(size_t)lr * v.n_comp];
+        if (out.scalar) {
+            double *o = out.scalar + e * GBMIE_NSCALAR;
+            o[GBMIE_S_QEXT] = s[0];
+            o[GBMIE_S_QSCA] = s[1];
+            o[GBMIE_S_QABS] = s[2];
+            o[GBMIE_S_QB] = s[3];
+            o[GBMIE_S_G] = s[4];
+            o[GBMIE_S_CSCA] = s[5];
+            o[GBMIE_S_CEXT] = s[6];
+            o[GBMIE_S_SSA] = s[1] / s[0];
+            o[GBMIE_S_BSCA] = s[7];
+            o[GBMIE_S_BEXT] = s[8];
+            o[GBMIE_S_BBCK] = s[9];
+            o[GBMIE_S_REFREAL] = m0.x;
+            o[GBMIE_S_REFIMAG] = -fabs(m0.y);
+            o[GBMIE_S_LIDAR_RATIO] = s[0] / s[3] * 4.0 * PI_D;
+        }
+        if (out.nl) {
+            const double *nl = v.nlraw + (size_t)blk * 5;
+            const double *nl0 = v.nlraw + (((size_t)lam * v.n_rh + 0) * v.n_bin + bin) * 5;
+            const double mass0 = nl0[1] * v.rhop0[bin];
+            double *o = out.nl + e * GBMIE_NNL;
+            o[GBMIE_N_MASS] = nl[0];
+            o[GBMIE_N_VOLUME] = nl[1] / mass0;
+            o[GBMIE_N_AREA] = nl[2] / mass0;
+            o[GBMIE_N_REFF] = nl[3];
+            o[GBMIE_N_RMASS] = nl[4];
+            o[GBMIE_N_RHOP] = v.rhop[(size_t)bin * v.n_rh + rh];
+            o[GBMIE_N_GF] = v.gf[rh];
+            o[GBMIE_N_RLOW] = v.rlow[bin];
+            o[GBMIE_N_RUP] = v.rup[bin];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static TabView make_view(const gbmie_table_plan *p, char *scr)
+{
+    const gbmie_table_desc &d = p->d;
+    TabView v;
+    v.n_lambda = d.n_lambda;
+    v.n_rh = d.n_rh;
+    v.n_size = d.n_size;
+    v.n_bin = d.n_bin;
+    v.n_comp = d.n_comp;
+    v.n_ang = d.n_ang;
+    v.grid_kind = d.grid_kind;
+    v.psd_kind = d.psd_kind;
+    v.rh0 = d.rh0_index;
+    v.lambda = d.lambda;
+    v.grid = d.grid;
+    v.dgrid = d.dgrid;
+    v.psd_param = d.psd_param;
+    v.gf_psd = d.gf_psd;
+    v.frac = d.frac;
+    v.rhop = d.rhop;
+    v.rhop0 = d.rhop0;
+    v.gf = d.gf;
+    v.rlow = d.rlow;
+    v.rup = d.rup;
+    v.theta = d.theta;
+    v.m = (const double2 *)d.m;
+    v.xg = p->xg;
+    v.off = p->off;
+    v.unit_base = p->unit_base;
+    v.pc = (double2 *)(scr + p->o_pc);
+    v.an = (double2 *)(scr + p->o_an);
+    v.bn = (double2 *)(scr + p->o_bn);
+    v.eff4 = (double *)(scr + p->o_eff);
+    v.W = (double *)(scr + p->o_w);
+    v.sums = (double *)(scr + p->o_sums);
+    v.reff0 = (double *)(scr + p->o_reff0);
+    v.pacc = (double *)(scr + p->o_pacc);
+    v.pq = (const double2 *)(scr + p->o_pq);
+    v.sraw = (double *)(scr + p->o_sraw);
+    v.nlraw = (double *)(scr + p->o_nlraw);
+    return v;
+}
+
+static void plan_free(gbmie_table_plan *p)
+{
+    if (!p) return;
+    if (p->xg) cudaFree(p->xg);
+    if (p->off) cudaFree(p->off);
+    if (p->unit_base) cudaFree(p->unit_base);
+    gsf_release(&p->gsf);
+    free(p);
+}
+
+extern "C" int gbmie_table_plan_destroy(gbmie_table_plan *plan)
+{
+    if (plan) {
+        cudaSetDevice(plan->ctx->device);
+        cudaStreamSynchronize(plan->ctx->stream);
+    }
+    plan_free(plan);
+    return GBMIE_OK;
+}
+
+extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *desc, gbmie_table_plan **out,
+                                       int64_t *scratch_bytes)
+{
+    if (!ctx) return GBMIE_ERR_INVALID;
+    if (!desc || !out) return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: NULL argument");
+    *out = nullptr;
+    const gbmie_table_desc &d = *desc;
+    if (d.n_lambda < 1 || d.n_rh < 1 || d.n_size < 2 || d.n_bin < 1 || d.n_comp < 1 || d.n_ang < 2 ||
+        d.n_bin > 8 || d.n_gsf < 0 || (d.n_gsf > 0 && d.n_gsf < 3) || d.rh0_index < 0 || d.rh0_index >= d.n_rh)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad sizes (n_size >= 2, n_ang >= 2, "
+                                                "1 <= n_bin <= 8, n_gsf = 0 or >= 3)");
+    if (d.grid_kind != GBMIE_GRID_X && d.grid_kind != GBMIE_GRID_RADIUS)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad grid_kind");
+    if (d.psd_kind < GBMIE_PSD_LOGNORM || d.psd_kind > GBMIE_PSD_WEIGHTS)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad psd_kind");
+    if (d.precision != GBMIE_PLAIN_FP64 && d.precision != GBMIE_MIXED)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad precision");
+    if (d.precision == GBMIE_MIXED)
+        return ctx_fail(ctx, GBMIE_ERR_UNSUPPORTED, "gbmie_table_plan_create: mixed precision not built");
+    if (!d.lambda || !d.grid || !d.dgrid || !d.m || !d.frac || !d.rhop || !d.rhop0 || !d.gf || !d.rlow || !d.rup ||
+        !d.cos_theta || !d.theta || (d.psd_kind != GBMIE_PSD_WEIGHTS && (!d.psd_param || !d.gf_psd)) ||
+        (d.psd_kind == GBMIE_PSD_WEIGHTS && !d.weights))
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: missing array");
+    cudaSetDevice(ctx->device);
+    gbmie_table_plan *p = (gbmie_table_plan *)calloc(1, sizeof(gbmie_table_plan));
+    if (!p) return GBMIE_ERR_NOMEM;
+    p->ctx = ctx;
+    p->d = d;
+    p->n_le = d.grid_kind == GBMIE_GRID_X ? 1 : d.n_lambda;
+    p->n_units = (int64_t)d.n_lambda * d.n_rh * d.n_comp;
+    p->n_inst = p->n_units * d.n_size;
+    p->n_entries = (int64_t)d.n_lambda * d.n_rh * d.n_bin;
+    const int64_t nrows = (int64_t)p->n_le * d.n_size;
+    int st = ctx_cuda(ctx, cudaMalloc(&p->xg, sizeof(double) * nrows), "plan x grid");
+    if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMalloc(&p->off, sizeof(int64_t) * (nrows + 1)), "plan offsets");
+    if (st == GBMIE_OK)
+        st = ctx_cuda(ctx, cudaMalloc(&p->unit_base, sizeof(int64_t) * p->n_units), "plan unit base");
+    if (st == GBMIE_OK) {
+        k_tab_make_x<<<(unsigned)ceil_div64(nrows, 256), 256, 0, ctx->stream>>>(p->n_le, d.n_size, d.grid_kind,
+                                                                               d.grid, d.lambda, p->xg,
+                                                                               ctx->d_flags);
+        st = ctx_check_launch(ctx, "k_tab_make_x");
+    }
+    int64_t total = 0;
+    if (st == GBMIE_OK) st = launch_layout(ctx, nrows, p->xg, 0, p->off, &total);
+    int64_t *hoff = nullptr;
+    if (st == GBMIE_OK) {
+        hoff = (int64_t *)malloc(sizeof(int64_t) * (nrows + 1));
+        if (!hoff) st = GBMIE_ERR_NOMEM;
+    }
+    if (st == GBMIE_OK)
+        st = ctx_cuda(ctx, cudaMemcpy(hoff, p->off, sizeof(int64_t) * (nrows + 1), cudaMemcpyDeviceToHost),
+                      "plan offsets copy");
+    if (st == GBMIE_OK) {
+        p->pc_total = total;
+        int nm = 2;
+        for (int64_t j = 0; j < nrows; ++j) {
+            const int g = (int)(hoff[j + 1] - hoff[j]);
+            if (g > nm) nm = g;
+        }
+        p->nmax_max = nm;
+        int64_t *ub = (int64_t *)malloc(sizeof(int64_t) * p->n_units);
+        if (!ub) st = GBMIE_ERR_NOMEM;
+        int64_t acc = 0;
+        for (int64_t u = 0; ub && u < p->n_units; ++u) {
+            const int lam = (int)(u / ((int64_t)d.n_rh * d.n_comp));
+            const int le = d.grid_kind == GBMIE_GRID_X ? 0 : lam;
+            ub[u] = acc;
+            acc += hoff[(int64_t)(le + 1) * d.n_size] - hoff[(int64_t)le * d.n_size];
+        }
+        p->ab_total = acc;
+        if (ub) {
+            st = ctx_cuda(ctx, cudaMemcpy(p->unit_base, ub, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice),
+                          "plan unit base copy");
+            free(ub);
+        }
+    }
+    free(hoff);
+    if (st == GBMIE_OK) {
+        size_t o = 0;
+        auto carve = [&](size_t bytes) {
+            const size_t at = o;
+            o = align_up(o + bytes, 256);
+            return at;
+        };
+        const size_t nW = (size_t)d.n_lambda * d.n_rh * d.n_bin * d.n_comp;
+        p->o_pc = carve(sizeof(double2) * (size_t)p->pc_total);
+        p->o_an = carve(sizeof(double2) * (size_t)p->ab_total);
+        p->o_bn = carve(sizeof(double2) * (size_t)p->ab_total);
+        p->o_eff = carve(sizeof(double) * 4 * (size_t)p->n_inst);
+        p->o_w = carve(sizeof(double) * nW * d.n_size);
+        p->o_sums = carve(sizeof(double) * nW * 4);
+        p->o_reff0 = carve(sizeof(double) * (size_t)d.n_lambda * d.n_bin * d.n_comp);
+        p->o_pacc = carve(sizeof(double) * (size_t)p->n_entries * 4 * d.n_ang);
+        p->o_pq = carve(sizeof(double2) * (size_t)p->nmax_max * d.n_ang);
+        p->o_sraw = carve(sizeof(double) * (size_t)p->n_entries * 10);
+        p->o_nlraw = carve(sizeof(double) * (size_t)p->n_entries * 5);
+        p->bytes = o;
+        void *scr = nullptr;
+        st = ctx_scratch(ctx, p->bytes, &scr);
+    }
+    if (st == GBMIE_OK && d.n_gsf > 0) {
+        st = gsf_prepare(ctx, d.n_gsf, d.n_ang, d.theta, &p->gsf);
+        p->has_gsf = 1;
+    }
+    if (st == GBMIE_OK) st = gbmie_ctx_synchronize(ctx);
+    if (st != GBMIE_OK) {
+        plan_free(p);
+        return st;
+    }
+    if (scratch_bytes) *scratch_bytes = (int64_t)p->bytes;
+    *out = p;
+    return GBMIE_OK;
+}
+
+extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_table_out *out)
+{
+    if (!ctx || !p || !out || p->ctx != ctx) return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_run: bad plan");
+    if (!out->phase || (p->has_gsf && !out->pmom))
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_run: phase (and pmom with n_gsf) required");
+    cudaSetDevice(ctx->device);
+    void *s = nullptr;
+    GBMIE_TRY(ctx_scratch(ctx, p->bytes, &s));
+    char *scr = (char *)s;
+    TabView v = make_view(p, scr);
+    const gbmie_table_desc &d = p->d;
+    cudaStream_t st = ctx->stream;
+    const int64_t nrows = (int64_t)p->n_le * d.n_size;
+    k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_psi_chi"));
+    const int64_t nW = (int64_t)d.n_lambda * d.n_rh * d.n_bin * d.n_comp;
+    k_tab_weights<<<(unsigned)nW, 256, 0, st>>>(v, d.weights);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_weights"));
+    k_tab_coeffs<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs"));
+    GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
+    GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
+                       "pacc clear"));
+    const int chunk = 256;
+    const int nchunk = (d.n_size + chunk - 1) / chunk;
+    const int threads = d.n_ang >= 256 ? 256 : ((d.n_ang + 31) / 32) * 32;
+    const unsigned grid = (unsigned)(p->n_units * nchunk);
+    if (d.n_bin <= 1) k_tab_s12_plain<1><<<grid, threads, 0, st>>>(v, chunk, nchunk);
+    else if (d.n_bin <= 2) k_tab_s12_plain<2><<<grid, threads, 0, st>>>(v, chunk, nchunk);
+    else if (d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk);
+    else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_s12_plain"));
+    k_tab_scalars<<<(unsigned)p->n_entries, 256, 0, st>>>(v);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_scalars"));
+    k_tab_finalize<<<(unsigned)p->n_entries, 256, 0, st>>>(v, *out);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
+    if (p->has_gsf) {
+        GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
+        GBMIE_TRY(launch_gsf_expand(ctx, &p->gsf, (int)p->n_entries, out->phase, (int64_t)6 * d.n_ang, d.n_ang, map,
+                                    out->pmom, (int64_t)6 * d.n_gsf, d.n_gsf, nullptr));
+    }
+    return GBMIE_OK;
+}

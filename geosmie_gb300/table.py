@@ -1,0 +1,403 @@
+"""Optics-table generation: the runoptics / dointegration.fun drop-in.
+
+``fun(partID0, datatype, oppfx, oppclassic)`` and ``run_table(params, mlist,
+waterm)`` follow geosmie/dointegration.py:672-1036: per size bin the
+reference's size-parameter grid (initializeXarr :425-463), per wavelength the
+interpolated refractive index (:700-710, :813-816), per RH the growth factor
+and volume-mixed index (getHumidRefractiveIndex :493-536), PSD weights
+(calculatePSD :539-664), Mie + Mueller + size integration (rawMie,
+integratePSD :1064-1254) and the phase normalisation (:950-1001).
+
+The host does the bookkeeping on small arrays (grids, indices, growth
+factors); every per-size and per-angle number is computed by libgbmie.so
+through ``gbmie_table_plan_create`` / ``gbmie_table_run``.  The NetCDF
+writer of the reference (createNCDF :205-422) is not part of this module:
+results come back as arrays with the reference file's variable names and its
+non-legacy dimension order (bin, wavelength, rh, ...).
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+import torch
+
+from . import _native
+from ._native import GRID_RADIUS, GRID_X, PSD_LOGNORM, PSD_POWER4, PSD_WEIGHTS  # noqa: F401
+
+SCATKEYS = ["p11", "p12", "p22", "p33", "p34", "p44"]
+SCALARKEYS = ["qext", "qsca", "qabs", "qb", "g", "csca", "cext"]
+EXTRAKEYS = ["ssa", "bsca", "bext", "bbck", "refreal", "refimag", "lidar_ratio"]
+NLSCALARKEYS = ["mass", "volume", "area", "rEff", "rMass", "rhop", "growth_factor", "rLow", "rUp"]
+# order of the scalar block returned by the C ABI (GBMIE_S_*) and of the
+# wavelength-independent block (GBMIE_N_*)
+SCALAR_ORDER = ["qext", "qsca", "qabs", "qb", "g", "csca", "cext", "ssa", "bsca", "bext", "bbck",
+                "refreal", "refimag", "lidar_ratio"]
+NL_ORDER = ["mass", "volume", "area", "rEff", "rMass", "rhop", "growth_factor", "rLow", "rUp"]
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in
+                ["n_lambda", "n_rh", "n_size", "n_bin", "n_comp", "n_ang", "grid_kind", "psd_kind",
+                 "precision", "n_gsf"]] + \
+               [(n, ctypes.c_void_p) for n in ["lambda_", "grid", "dgrid", "m", "psd_param", "gf_psd"]] + \
+               [("rh0_index", ctypes.c_int32), ("pad0", ctypes.c_int32)] + \
+               [(n, ctypes.c_void_p) for n in ["frac", "weights", "rhop", "rhop0", "gf", "rlow", "rup",
+                                                "cos_theta", "theta"]]
+
+
+class _Out(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ["phase", "pback", "scalar", "nl", "pmom"]]
+
+
+def angmie():
+    """The reference's 371 output angles (dointegration.py:739-742), degrees."""
+    return np.concatenate([np.linspace(0.0, 1.0, 100, endpoint=False),
+                           np.linspace(1.0, 10.0, 100, endpoint=False),
+                           np.linspace(10.0, 180.0, 171, endpoint=True)])
+
+
+class TablePlan(object):
+    """One planned table on the GPU (a C ``gbmie_table_plan``).
+
+    ``spec`` holds host arrays (numpy) with the fields of gbmie_table_desc:
+    lambda [nl] m, grid [ns], dgrid [ns], grid_kind, m [nl, nrh, ncomp]
+    complex, psd_kind, psd_param [nbin, ncomp, 4], gf_psd [nrh], rh0_index,
+    frac [nbin, ncomp], weights [nl, nrh, nbin, ncomp, ns] (psd_kind
+    PSD_WEIGHTS), rhop [nbin, nrh], rhop0 [nbin], gf [nrh], rlow [nbin],
+    rup [nbin], ang (degrees) [nang].  Inputs are copied to the device once;
+    ``run()`` launches the whole pipeline on the current stream (no host
+    synchronisation, capturable in a CUDA graph).
+    """
+
+    def __init__(self, spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=0, device=0):
+        self.ctx = _native.context(device)
+        dv = self.ctx.device
+        ang = np.asarray(spec["ang"], np.float64)
+        theta = np.radians(ang)
+        lam = np.asarray(spec["lambda"], np.float64)
+        m = np.asarray(spec["m"], np.complex128)
+        nl, nrh, ncomp = m.shape
+        frac = np.asarray(spec["frac"], np.float64)
+        nbin = frac.shape[0]
+        ns = len(spec["grid"])
+        f64 = torch.float64
+
+        def d(a, dt=f64):
+            return torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dv)
+
+        self.t = {
+            "lambda": d(lam), "grid": d(spec["grid"]), "dgrid": d(spec["dgrid"]),
+            "m": d(m, torch.complex128), "frac": d(frac), "rhop": d(spec["rhop"]),
+            "rhop0": d(spec["rhop0"]), "gf": d(spec["gf"]), "rlow": d(spec["rlow"]), "rup": d(spec["rup"]),
+            "cos_theta": d(np.cos(theta)), "theta": d(theta),
+        }
+        psd_kind = int(spec["psd_kind"])
+        if psd_kind == PSD_WEIGHTS:
+            self.t["weights"] = d(spec["weights"])
+        else:
+            self.t["psd_param"] = d(spec["psd_param"])
+            self.t["gf_psd"] = d(spec["gf_psd"])
+        desc = _Desc()
+        desc.n_lambda, desc.n_rh, desc.n_size, desc.n_bin, desc.n_comp = nl, nrh, ns, nbin, ncomp
+        desc.n_ang = ang.size
+        desc.grid_kind = int(spec["grid_kind"])
+        desc.psd_kind = psd_kind
+        desc.precision = int(precision)
+        desc.n_gsf = int(n_gsf)
+        desc.rh0_index = int(spec.get("rh0_index", 0))
+
+        def p(k):
+            t = self.t.get(k)
+            return None if t is None else t.data_ptr()
+        desc.lambda_ = p("lambda")
+        for k in ["grid", "dgrid", "m", "psd_param", "gf_psd", "frac", "weights", "rhop", "rhop0", "gf",
+                  "rlow", "rup", "cos_theta", "theta"]:
+            setattr(desc, k, p(k))
+        self.desc = desc
+        self.shape = (nbin, nl, nrh)
+        self.nang = ang.size
+        self.ang = ang
+        self.n_gsf = int(n_gsf)
+        h = ctypes.c_void_p()
+        nbytes = ctypes.c_int64()
+        self.ctx.call("gbmie_table_plan_create", ctypes.byref(desc), ctypes.byref(h), ctypes.byref(nbytes))
+        self.h = h
+        self.scratch_bytes = nbytes.value
+        ne = nbin * nl * nrh
+        self.out_t = {
+            "phase": torch.empty((nbin, nl, nrh, 6, ang.size), dtype=f64, device=dv),
+            "pback": torch.empty((nbin, nl, nrh, 6), dtype=f64, device=dv),
+            "scalar": torch.empty((nbin, nl, nrh, _native.NSCALAR), dtype=f64, device=dv),
+            "nl": torch.empty((nbin, nl, nrh, _native.NNL), dtype=f64, device=dv),
+        }
+        if n_gsf:
+            self.out_t["pmom"] = torch.empty((nbin, nl, nrh, 6, n_gsf), dtype=f64, device=dv)
+        out = _Out()
+        for k, v in self.out_t.items():
+            setattr(out, k, v.data_ptr())
+        self.out = out
+        self.n_entries = ne
+        self.n_instances = nl * nrh * ncomp * ns
+
+    def run(self):
+        """Launch the table pipeline on torch's current stream."""
+        self.ctx.call("gbmie_table_run", self.h, ctypes.byref(self.out))
+
+    def sync(self):
+        self.ctx.sync()
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.ctx.lib.gbmie_table_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def results(self):
+        """Host dict: scatkeys [nbin, nl, nrh, nang], scalar keys [nbin, nl,
+        nrh], pback [nbin, nl, nrh, 6], wavelength-independent keys [nbin, nl,
+        nrh] (per wavelength), pmom [nbin, nl, nrh, 6, n_gsf] (p order P11
+        P12 P33 P34 P22 P44, i.e. alpha1 beta1 alpha3 beta2 alpha2 alpha4)."""
+        self.sync()
+        ph = self.out_t["phase"].cpu().numpy()
+        sc = self.out_t["scalar"].cpu().numpy()
+        nlv = self.out_t["nl"].cpu().numpy()
+        res = {k: ph[..., i, :] for i, k in enumerate(SCATKEYS)}
+        res.update({k: sc[..., i] for i, k in enumerate(SCALAR_ORDER)})
+        res.update({"nl_" + k: nlv[..., i] for i, k in enumerate(NL_ORDER)})
+        res["pback"] = self.out_t["pback"].cpu().numpy()
+        if "pmom" in self.out_t:
+            res["pmom"] = self.out_t["pmom"].cpu().numpy()
+        return res
+
+
+# ---------------------------------------------------------------------------
+# reference-style host bookkeeping (small arrays only)
+# ---------------------------------------------------------------------------
+def _get_dr(arr):
+    """Centred differences (dointegration.py:93-101)."""
+    arr = np.asarray(arr, np.float64)
+    d = np.empty_like(arr)
+    d[0] = arr[1] - arr[0]
+    d[1:-1] = ((arr[1:-1] - arr[:-2]) + (arr[2:] - arr[1:-1])) / 2.0
+    d[-1] = arr[-1] - arr[-2]
+    return d
+
+
+def _carma_grid(minx, maxx, nbinperdecade):
+    """Volume-ratio size grid and widths (dointegration.py:103-153)."""
+    rat = maxx / minx
+    nbin = np.log10(maxx / minx) * nbinperdecade
+    rmrat = (rat ** 3) ** (1.0 / nbin)
+    rmin = minx * ((1.0 + rmrat) / 2.0) ** (1.0 / 3.0)
+    cpi = 4.0 / 3.0 * np.pi
+    rvolmin = cpi * rmin ** 3.0
+    vrfact = ((3.0 / 2.0 / np.pi / (rmrat + 1)) ** (1.0 / 3.0)) * (rmrat ** (1.0 / 3.0) - 1.0)
+    i = np.arange(int(nbin))
+    rvol = rvolmin * rmrat ** i
+    return (rvol / cpi) ** (1.0 / 3.0), vrfact * rvol ** (1.0 / 3.0)
+
+
+def _x_grid(params, b, minlam, maxlam):
+    """initializeXarr (dointegration.py:425-463)."""
+    pp = params["psd"]["params"]
+    t = params["psd"]["type"]
+    if t == "lognorm":
+        return _carma_grid(pp["rmin0"][b][0] * 2 * np.pi / maxlam, pp["rmax0"][b][-1] * 2 * np.pi / minlam * 3.0,
+                           pp["numperdec"][b])
+    if t == "ss":
+        return _carma_grid(pp["rMinMaj"][b] * 2 * np.pi / maxlam, pp["rMaxMaj"][b] * 2 * np.pi / minlam * 10,
+                           pp["numperdec"][b])
+    if t == "du":
+        minx = pp["rMinMaj"][b][0] * 2 * np.pi / maxlam
+        maxx = pp["rMaxMaj"][b][-1] * 2 * np.pi / minlam
+        return (np.linspace(np.log10(minx), np.log10(maxx), 1000)) ** 10.0, None
+    raise ValueError("unknown psd type %s" % t)
+
+
+def _growth(rhdep, siz0, rh, allrh):
+    """humidityGrowth (particleparams.py:85-108) for 'simple', 'trivial', 'ss'."""
+    rhi = list(allrh).index(rh)
+    t = rhdep["type"]
+    p = rhdep["params"]
+    if t in ("simple", "trivial"):
+        return siz0 * p["gf"][rhi]
+    if t == "ss":
+        if rh == 0.0:
+            return siz0
+        siz = siz0 * 100
+        return (p["c1"] * siz ** p["c2"] / (p["c3"] * siz ** p["c4"] - np.log10(rh)) + siz ** 3.0) ** (1.0 / 3.0) / 100.0
+    raise NotImplementedError("growth law '%s' (CARMA 'su') is not implemented" % t)
+
+
+def _ss_weights(params, b, rh_list, x, lams):
+    """Gong sea-salt PSD weights (dointegration.py:585-624) [nl, nrh, ns]."""
+    pp = params["psd"]["params"]
+    rminmaj, rmaxmaj = pp["rMinMaj"][b], pp["rMaxMaj"][b]
+    out = np.zeros((lams.size, len(rh_list), x.size))
+    for li, lam in enumerate(lams):
+        rarr = x / (2 * np.pi / lam)
+        dr = _get_dr(rarr)
+        for ri, onerh in enumerate(rh_list):
+            rminuse = _growth(params["rhDep"], rminmaj, onerh, rh_list)
+            rmaxuse = _growth(params["rhDep"], rmaxmaj, onerh, rh_list)
+            rrat = rminmaj / rminuse
+            r80rat = 1.65 * rrat
+            r80 = rarr * r80rat * 1e6
+            afac = 4.7 * (1.0 + 30.0 * r80) ** (-0.017 * r80 ** (-1.44))
+            bfac = (0.433 - np.log10(r80)) / 0.433
+            dndr = 1.373 * r80 ** (-afac) * (1.0 + 0.057 * r80 ** 3.45) * 10.0 ** (1.607 * np.exp(-bfac ** 2.0)) * r80rat
+            dndr[rarr < rminuse] = 0.0
+            dndr[rarr > rmaxuse] = 0.0
+            dndr = dndr / np.sum(dndr)
+            w = dndr * dr
+            out[li, ri] = w / np.sum(w)
+    return out
+
+
+def bin_spec(params, b, mlist, waterm, ang, lambdas=None):
+    """The TablePlan spec of size bin b of a reference particle definition."""
+    lam = np.asarray(mlist[0][0], np.float64) if lambdas is None else np.asarray(lambdas, np.float64)
+    rh = list(params["rh"])
+    if "maxrh" in params:
+        rh = list(np.minimum(np.array(rh, dtype=np.float64), params["maxrh"]))
+    rtype = params["rhDep"]["type"]
+    ptype = params["psd"]["type"]
+    pp = params["psd"]["params"]
+    trivial = rtype == "trivial"
+    rh_run = rh[:1] if trivial else rh
+    x, dx = _x_grid(params, b, lam[0], lam[-1])
+    # refractive indices: particle (imaginary sign flipped, :813-816) and water
+    n0 = np.array([[complex(np.interp(l_, t[0], t[1]), -np.interp(l_, t[0], t[2])) for t in mlist] for l_ in lam])
+    if trivial:
+        nw = np.ones(lam.size, np.complex128)
+    else:
+        nw = np.array([complex(np.interp(l_, waterm[0], waterm[1]), np.interp(l_, waterm[0], waterm[2]))
+                       for l_ in lam])
+    nrh = len(rh_run)
+    gf = np.zeros(nrh)
+    rrat = np.zeros(nrh)
+    for ri in range(nrh):
+        if rtype in ("simple", "trivial"):
+            gf[ri] = params["rhDep"]["params"]["gf"][ri]
+            rrat[ri] = 1.0 / gf[ri]
+        elif rtype == "ss":
+            rminmaj = pp["rMinMaj"][b] if "rMinMaj" in pp else pp["rmin0"][b][0]
+            rminuse = _growth(params["rhDep"], rminmaj, rh[ri], rh)
+            rrat[ri] = rminmaj / rminuse
+            gf[ri] = 1.0 / rrat[ri]
+        else:
+            raise NotImplementedError("growth law '%s' (CARMA 'su') is not implemented" % rtype)
+    # volume mixing (dointegration.py:505); components follow the PSD (one RI
+    # table is shared by every component, as the reference replicates it)
+    fr = list(pp["fracs"][b])
+    ncomp = len(fr)
+    mix = nw[:, None, None] + (n0[:, None, :] - nw[:, None, None]) * (rrat[None, :, None] ** 3.0)
+    if mix.shape[2] == 1 and ncomp > 1:
+        mix = np.repeat(mix, ncomp, axis=2)
+    rhop0v = params["rhop0"][b] if isinstance(params["rhop0"], list) else params["rhop0"]
+    spec = {
+        "lambda": lam, "grid": x, "grid_kind": GRID_X, "m": mix, "frac": np.array([fr]),
+        "rhop": (rrat ** 3.0 * rhop0v + (1.0 - rrat ** 3.0) * 1000.0)[None, :], "rhop0": np.array([rhop0v]),
+        "gf": gf, "ang": np.asarray(ang, np.float64), "rh0_index": rh.index(0.0) if 0.0 in rh else 0,
+    }
+    if ptype == "lognorm":
+        spec["psd_kind"] = PSD_LOGNORM
+        spec["dgrid"] = dx
+        spec["psd_param"] = np.array([[[pp["r0"][b][k], pp["rmin0"][b][k], pp["rmax0"][b][k], pp["sigma"][b][k]]
+                                       for k in range(ncomp)]])
+        # growth of r0/rmax0 looks the RH up by value (particleparams.py:86)
+        spec["gf_psd"] = np.array([params["rhDep"]["params"]["gf"][rh.index(v)] for v in rh_run])
+        spec["rlow"] = np.array([pp["rmin0"][b][0]])
+        spec["rup"] = np.array([pp["rmax0"][b][0]])
+    elif ptype == "du":
+        spec["psd_kind"] = PSD_POWER4
+        spec["dgrid"] = _get_dr(x)
+        spec["psd_param"] = np.array([[[pp["rMinMaj"][b][k], pp["rMaxMaj"][b][k], 0.0, 0.0]
+                                       for k in range(ncomp)]])
+        spec["gf_psd"] = np.ones(nrh)
+        spec["rlow"] = np.array([pp["rMinMaj"][b][-1]])
+        spec["rup"] = np.array([pp["rMaxMaj"][b][-1]])
+    elif ptype == "ss":
+        spec["psd_kind"] = PSD_WEIGHTS
+        spec["dgrid"] = _get_dr(x)
+        spec["weights"] = _ss_weights(params, b, rh_run if not trivial else rh[:1], x, lam)[:, :, None, None, :]
+        spec["rlow"] = np.array([pp["rMinMaj"][b]])
+        spec["rup"] = np.array([pp["rMaxMaj"][b]])
+    else:
+        raise ValueError("unknown psd type %s" % ptype)
+    spec["trivial_nrh"] = len(rh) if trivial else 0
+    return spec
+
+
+def run_table(params, mlist, waterm, ang=None, lambdas=None, precision=_native.GBMIE_PLAIN_FP64, n_gsf=0,
+              device=0):
+    """The (bin x wavelength x RH) table of a reference particle definition.
+
+    Returns {key: array} with the reference file's variables and
+    non-legacy dimensions: scatkeys (bin, wavelength, rh, ang), scalar keys
+    (bin, wavelength, rh), pback (bin, wavelength, rh, p), and the
+    wavelength-independent keys (bin, rh) holding the last wavelength's
+    values as the reference file does; with n_gsf > 0 also 'pmom'
+    (bin, wavelength, rh, p, m) as written by rungsf (pygeos mode).
+    """
+    ang = angmie() if ang is None else np.asarray(ang, np.float64)
+    pp = params["psd"]["params"]
+    nbin = len(pp["r0"]) if params["psd"]["type"] == "lognorm" else len(pp["rMinMaj"])
+    parts = []
+    for b in range(nbin):
+        spec = bin_spec(params, b, mlist, waterm, ang, lambdas)
+        plan = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=device)
+        plan.run()
+        res = plan.results()
+        plan.close()
+        nrh_full = spec["trivial_nrh"]
+        if nrh_full:   # 'trivial': every RH copies the dry values (copyDryValues)
+            res = {k: np.repeat(v, nrh_full, axis=2) for k, v in res.items()}
+        parts.append(res)
+    out = {k: np.concatenate([p_[k] for p_ in parts], axis=0) for k in parts[0]}
+    for k in NLSCALARKEYS:
+        out[k] = out.pop("nl_" + k)[:, -1, :]
+    return out
+
+
+def load_particle(path, data_dir=None):
+    """particleparams.getPPJSON (particleparams.py:18-56): the JSON dict, the
+    refractive-index tables (wavelength in metres) and the water table."""
+    with open(path) as fp:
+        params = json.load(fp)
+    base = data_dir or os.getcwd()
+    ri = params["ri"]
+
+    def rel(p):
+        return p if os.path.isabs(p) else os.path.join(base, p)
+    if ri["format"] == "gads":
+        mlist = [np.loadtxt(rel(p), skiprows=17, max_rows=61, comments=None, unpack=True, usecols=[1, 8, 9])
+                 for p in ri["path"]]
+    elif ri["format"] in ("csv", "wsv"):
+        mlist = [np.loadtxt(rel(p), unpack=True, delimiter="," if ri["format"] == "csv" else None)
+                 for p in ri["path"]]
+    else:
+        raise ValueError("refractive index format %s not supported" % ri["format"])
+    for t in mlist:
+        t[0] *= 1e-6
+    waterm = np.loadtxt(rel("data/refrac.water.txt"), skiprows=13, unpack=True, usecols=[0, 1, 2])
+    waterm[0] *= 1e-6
+    return params, mlist, waterm
+
+
+def fun(partID0, datatype="json", oppfx=".", oppclassic=False, data_dir=None, n_gsf=0,
+        precision=_native.GBMIE_PLAIN_FP64):
+    """dointegration.fun (:672): returns the table dict instead of writing
+    optics_<id>.nomom.nc4 (the NetCDF writer is outside this module)."""
+    if datatype != "json":
+        raise ValueError("bad datatype: %s" % datatype)
+    params, mlist, waterm = load_particle(partID0, data_dir)
+    if params.get("mode", "mie") != "mie":
+        raise NotImplementedError("kernel (GRASP) mode is not a Mie table")
+    return run_table(params, mlist, waterm, n_gsf=n_gsf, precision=precision)

@@ -1,0 +1,219 @@
+/*
+ * gbmie.h -- C ABI of the GB300 (sm_103a) Mie hot path of GEOSmie.
+ *
+ * The reference (GEOS-ESM/GEOSmie) is a Python package; its hot path is the
+ * pymiecoated Mie kernel (pymiecoated/mie_coeffs.py, mie_props.py,
+ * mie_coated.py), the size/humidity integration of the runoptics table
+ * builder (geosmie/dointegration.py) and the GSF expansion program
+ * (gsf/spher_expan.f, reached through os.system in gsf/convertncdf.py:188).
+ * It has no FFI of its own, so each entry point below states the reference
+ * function whose work it replaces; the Python layer in geosmie_gb300/ binds
+ * these with ctypes behind the reference's own Python signatures.
+ *
+ * Conventions
+ *  - Every call returns an int status (GBMIE_OK == 0).  The message of the
+ *    last failure on a context is available from gbmie_last_error().
+ *  - Array arguments are DEVICE pointers owned by the caller unless a
+ *    comment says "host".  Complex numbers are two doubles (re, im), the
+ *    memory layout of numpy complex128 and CUDA double2.
+ *  - Calls are asynchronous on the context's stream (gbmie_ctx_set_stream)
+ *    except where a host result is returned (gbmie_layout, gbmie_table_plan).
+ *  - A context is used by one host thread at a time.
+ *  - Refractive indices follow pymiecoated: Im(m) > 0 is absorbing,
+ *    eps = m^2, mu = 1 unless given.
+ */
+#ifndef GBMIE_H
+#define GBMIE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GBMIE_OK 0
+#define GBMIE_ERR_INVALID 1     /* bad argument: x < 0, y < x, NaN/Inf, |u| > 1,
+                                   coated with mu != 1, bad sizes or pointers */
+#define GBMIE_ERR_NMAX 2        /* an instance needs more partial waves than
+                                   GBMIE_MAX_NMAX */
+#define GBMIE_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define GBMIE_ERR_TIMEOUT 4     /* a device-side wait hit its iteration limit */
+#define GBMIE_ERR_NOMEM 5       /* device allocation failed */
+#define GBMIE_ERR_UNSUPPORTED 6 /* option not implemented */
+
+#define GBMIE_MAX_NMAX 100000   /* x up to about 9.9e4 */
+
+/* precision of the contractions (S1/S2 angular sums, size integration, GSF) */
+#define GBMIE_PLAIN_FP64 0      /* everything in FP64 */
+#define GBMIE_MIXED 1           /* FP64 recurrences, tensor-core split-FP16
+                                   contractions with FP32 accumulation */
+
+typedef struct gbmie_ctx gbmie_ctx;
+typedef struct { double re, im; } gbmie_complex;
+
+/* ---- context ----------------------------------------------------------- */
+int gbmie_ctx_create(int device, gbmie_ctx **ctx);
+int gbmie_ctx_destroy(gbmie_ctx *ctx);
+/* stream: a cudaStream_t (NULL = legacy default stream). */
+int gbmie_ctx_set_stream(gbmie_ctx *ctx, void *stream);
+int gbmie_ctx_synchronize(gbmie_ctx *ctx);
+const char *gbmie_status_string(int status);
+const char *gbmie_last_error(const gbmie_ctx *ctx);
+/* Kernel launches issued by this context so far (host counter). */
+int64_t gbmie_launch_count(const gbmie_ctx *ctx);
+
+/* Number of partial waves round(2 + x + 4 x^(1/3)) for one size parameter,
+ * computed by the same device function the kernels use (host result).
+ * Replaces the nmax expression of pymiecoated/mie_coeffs.py:99,148,203. */
+int gbmie_nmax(gbmie_ctx *ctx, double x, int32_t *nmax /* host */);
+
+/* CSR layout of ragged per-instance coefficient arrays: offsets[0] = 0,
+ * offsets[i+1] = offsets[i] + nmax(size[i]).  size = x (homogeneous) or
+ * y (coated).  *total (host) receives offsets[n].  Synchronous. */
+int gbmie_layout(gbmie_ctx *ctx, int64_t n, const double *size,
+                 int64_t *offsets, int64_t *total /* host */);
+
+/* Mie coefficients a_n, b_n (n = 1..nmax) and the six efficiencies
+ * (qext, qsca, qabs, qb, asy, qratio) of n instances.
+ * Replaces pymiecoated/mie_coeffs.py:36-73 (mie_coeffs dispatch),
+ * :83-180 (homogeneous), :183-251 (coated) and mie_props.py:28-70.
+ *   x[n]                 core (or only) size parameter
+ *   y[n] or NULL         shell size parameter (coated if y != x and
+ *                        eps2 != eps, as the reference dispatches)
+ *   eps[n]               permittivity (core)
+ *   mu[n] or NULL        permeability (homogeneous only; NULL = 1)
+ *   eps2[n] or NULL      shell permittivity (required with y)
+ *   offsets[n+1]         from gbmie_layout on max(x, y); may be NULL when
+ *                        an and bn are NULL
+ *   an, bn or NULL       [offsets[n]] complex
+ *   eff or NULL          [n][6]
+ * Uses scratch device memory owned by the context. */
+int gbmie_coeffs(gbmie_ctx *ctx, int64_t n, const double *x, const double *y,
+                 const gbmie_complex *eps, const gbmie_complex *mu,
+                 const gbmie_complex *eps2, const int64_t *offsets,
+                 gbmie_complex *an, gbmie_complex *bn, double *eff);
+
+/* Scaled angular functions pi~_n(u) and tau~_n(u) (times (2n+1)/(n(n+1))),
+ * n = 1..nmax, at nang cosines: pi_out, tau_out [nang][nmax].
+ * Replaces pymiecoated/mie_props.py:166-231 and mie_coated.py:160-179. */
+int gbmie_pitau(gbmie_ctx *ctx, int32_t nang, const double *cos_theta,
+                int32_t nmax, double *pi_out, double *tau_out);
+
+/* Amplitude functions S1, S2 [n][nang] of n instances from their
+ * coefficients (CSR by offsets).  Replaces mie_props.py:108-149 and
+ * mie_coated.py:31-39 (runS12Loop).  |cos_theta| <= 1 is required. */
+int gbmie_s12(gbmie_ctx *ctx, int64_t n, const int64_t *offsets,
+              const gbmie_complex *an, const gbmie_complex *bn, int32_t nang,
+              const double *cos_theta, gbmie_complex *s1, gbmie_complex *s2);
+
+/* One MultipleMie(xArr, None, costarr).calculateS12SizeRange(mr, mi) call:
+ * eps = (mr + i mi)^2, mu = 1; S1, S2 [n][nang] and eff [n][6] for every x.
+ * Replaces pymiecoated/mie_coated.py:61-89.  Uses context scratch. */
+int gbmie_size_range(gbmie_ctx *ctx, int64_t n, const double *x, double mr,
+                     double mi, int32_t nang, const double *cos_theta,
+                     gbmie_complex *s1, gbmie_complex *s2, double *eff);
+
+/* ---- table generation (runoptics / dointegration.fun) ------------------ */
+#define GBMIE_GRID_X 0          /* grid = size parameters, shared by all
+                                   wavelengths (dointegration.py:791) */
+#define GBMIE_GRID_RADIUS 1     /* grid = radii (m); x = 2 pi r / lambda */
+
+#define GBMIE_PSD_LOGNORM 0     /* particleparams.py:113-127 x dgrid,
+                                   dointegration.py:546-583 */
+#define GBMIE_PSD_POWER4 1      /* r^-4 in [rmin, rmax] x dgrid,
+                                   dointegration.py:626-662 */
+#define GBMIE_PSD_WEIGHTS 2     /* caller-supplied normalised weights */
+
+/* scalar outputs per (bin, lambda, rh) */
+enum {
+    GBMIE_S_QEXT = 0, GBMIE_S_QSCA, GBMIE_S_QABS, GBMIE_S_QB, GBMIE_S_G,
+    GBMIE_S_CSCA, GBMIE_S_CEXT, GBMIE_S_SSA, GBMIE_S_BSCA, GBMIE_S_BEXT,
+    GBMIE_S_BBCK, GBMIE_S_REFREAL, GBMIE_S_REFIMAG, GBMIE_S_LIDAR_RATIO,
+    GBMIE_NSCALAR
+};
+/* wavelength-independent outputs per (bin, lambda, rh); the reference file
+ * keeps the values of the last wavelength */
+enum {
+    GBMIE_N_MASS = 0, GBMIE_N_VOLUME, GBMIE_N_AREA, GBMIE_N_REFF,
+    GBMIE_N_RMASS, GBMIE_N_RHOP, GBMIE_N_GF, GBMIE_N_RLOW, GBMIE_N_RUP,
+    GBMIE_NNL
+};
+
+typedef struct {
+    int32_t n_lambda, n_rh, n_size, n_bin, n_comp, n_ang;
+    int32_t grid_kind;          /* GBMIE_GRID_* */
+    int32_t psd_kind;           /* GBMIE_PSD_* */
+    int32_t precision;          /* GBMIE_PLAIN_FP64 or GBMIE_MIXED */
+    int32_t n_gsf;              /* Gauss nodes = moments of the GSF expansion
+                                   (reference 129); 0 = no expansion */
+    const double *lambda;       /* [n_lambda] m */
+    const double *grid;         /* [n_size] ascending, see grid_kind */
+    const double *dgrid;        /* [n_size] PSD widths (drarr), same unit */
+    const gbmie_complex *m;     /* [n_lambda][n_rh][n_comp], Im > 0 absorbing */
+    const double *psd_param;    /* [n_bin][n_comp][4]: lognormal r0, rmin0,
+                                   rmax0, sigma; power4 rmin, rmax, -, - (m) */
+    const double *gf_psd;       /* [n_rh] growth applied to r0 and rmax0
+                                   (particleparams.py:85-91) */
+    int32_t rh0_index;          /* rh index whose growth defines the dry
+                                   effective radius reff0 (dointegration.py:841) */
+    int32_t pad0;
+    const double *frac;         /* [n_bin][n_comp] */
+    const double *weights;      /* GBMIE_PSD_WEIGHTS: [n_lambda][n_rh][n_bin]
+                                   [n_comp][n_size]; weights of rh0_index give
+                                   reff0 */
+    const double *rhop;         /* [n_bin][n_rh] wet density */
+    const double *rhop0;        /* [n_bin] dry density */
+    const double *gf;           /* [n_rh] growth factor recorded in the table */
+    const double *rlow;         /* [n_bin] */
+    const double *rup;          /* [n_bin] */
+    const double *cos_theta;    /* [n_ang] */
+    const double *theta;        /* [n_ang] radians, ascending */
+} gbmie_table_desc;
+
+typedef struct {
+    double *phase;   /* [n_bin][n_lambda][n_rh][6][n_ang]: p11 p12 p22 p33 p34 p44 */
+    double *pback;   /* [n_bin][n_lambda][n_rh][6]: p11 p12 p33 p34 p22 p44 at the
+                        last angle (dointegration.py:990-991) */
+    double *scalar;  /* [n_bin][n_lambda][n_rh][GBMIE_NSCALAR] */
+    double *nl;      /* [n_bin][n_lambda][n_rh][GBMIE_NNL] */
+    double *pmom;    /* [n_bin][n_lambda][n_rh][6][n_gsf] alpha1..alpha4, beta1,
+                        beta2 normalised to alpha1(0) = 1, or NULL */
+} gbmie_table_out;
+
+typedef struct gbmie_table_plan gbmie_table_plan;
+
+/* Plan a table: validates the descriptor, computes the per-wavelength
+ * coefficient layout on the device and sizes the scratch memory
+ * (synchronous).  The descriptor's pointers must stay valid until the plan
+ * is destroyed.  *scratch_bytes (host) receives the scratch size. */
+int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *desc,
+                            gbmie_table_plan **plan, int64_t *scratch_bytes);
+int gbmie_table_plan_destroy(gbmie_table_plan *plan);
+/* Run a planned table: replaces the (bin x lambda x RH) loop of
+ * geosmie/dointegration.py:786-1031 (rawMie, calculateScatVals,
+ * calculatePSD, integratePSD, the phase normalisation) and, when n_gsf > 0,
+ * the pygeos pass of gsf/convertncdf.py:319-401 + gsf/spher_expan.f.
+ * Asynchronous; uses context scratch sized by the plan. */
+int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_out *out);
+
+/* ---- GSF expansion ------------------------------------------------------ */
+/* Expansion coefficients of ntab scattering matrices given on one angle grid:
+ * ang_deg [nang] ascending degrees; F [ntab][6][nang] in the order F11 F22
+ * F33 F44 F12 F34; coef [ntab][6][nnodes] alpha1 alpha2 alpha3 alpha4 beta1
+ * beta2 (l = 0..nnodes-1) normalised so alpha1(0) = 1; cnorm [ntab] or NULL
+ * receives 1/alpha1(0).  Replaces gsf/spher_expan.f:93-107,120-180,269-407,
+ * 520-623 (one program run per matrix in the reference). */
+int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const double *ang_deg,
+              const double *F, int32_t nnodes, double *coef, double *cnorm,
+              int32_t precision);
+
+/* ---- measurement helper ------------------------------------------------- */
+/* Sustained FP64 FMA throughput of this device (GFLOP/s, host), measured by
+ * a dependent-chain-free DFMA loop over the whole GPU. */
+int gbmie_measure_fp64_peak(gbmie_ctx *ctx, double *gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBMIE_H */

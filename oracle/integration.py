@@ -379,3 +379,83 @@ def run_table(params, mlist, waterm, ang=None, batch=True, lambdas=None):
                 for k in NLSCALARKEYS:
                     out[k][b, rhi] = fin[k]
     return out
+
+
+def run_spec(spec, n_gsf=0):
+    """CPU evaluation of a table spec (the arrays of geosmie_gb300's
+    TablePlan / gbmie_table_desc) with the restated reference formulas:
+    raw_mie, lognormal / r^-4 / given PSD weights, integrate_psd,
+    finalize_unit, the RH=0 mass normalisation, and (n_gsf > 0) the GSF
+    expansion of oracle/spher_expan.c on the normalised phase matrix.
+
+    Returns arrays shaped like the GPU results: scatkeys [nbin, nl, nrh,
+    nang], scalar keys [nbin, nl, nrh], pback [nbin, nl, nrh, 6], 'nl_<key>'
+    [nbin, nl, nrh], pmom [nbin, nl, nrh, 6, n_gsf] in the pygeos p order.
+    """
+    from . import gsf as ogsf
+    lam = np.asarray(spec["lambda"], np.float64)
+    grid = np.asarray(spec["grid"], np.float64)
+    dgrid = np.asarray(spec["dgrid"], np.float64)
+    m = np.asarray(spec["m"], np.complex128)
+    frac = np.asarray(spec["frac"], np.float64)
+    ang = np.asarray(spec["ang"], np.float64)
+    cost = np.cos(np.radians(ang))
+    nl, nrh, ncomp = m.shape
+    nbin = frac.shape[0]
+    kind = int(spec["psd_kind"])
+    radius_grid = int(spec["grid_kind"]) == 1
+    rh0 = int(spec.get("rh0_index", 0))
+    out = {k: np.zeros((nbin, nl, nrh, ang.size)) for k in SCATKEYS}
+    for k in SCALARKEYS + EXTRAKEYS:
+        out[k] = np.zeros((nbin, nl, nrh))
+    for k in NLSCALARKEYS:
+        out["nl_" + k] = np.zeros((nbin, nl, nrh))
+    out["pback"] = np.zeros((nbin, nl, nrh, 6))
+
+    def weights(li, ri, b, c, x):
+        if kind == 2:
+            return np.asarray(spec["weights"])[li, ri, b, c]
+        pp = np.asarray(spec["psd_param"])[b, c]
+        if kind == 0:
+            gfp = np.asarray(spec["gf_psd"])[ri]
+            w = lognorm_psd(pp[0] * gfp, pp[3], x, lam[li], pp[2] * gfp, pp[1]) * dgrid
+        else:
+            r = x * lam[li] / (2 * np.pi)
+            w = r ** (-4.0) * dgrid
+            w[r < pp[0]] = 0.0
+            w[r > pp[1]] = 0.0
+        return w / np.sum(w)
+
+    for li in range(nl):
+        x = 2 * np.pi * grid / lam[li] if radius_grid else grid
+        rr = x * lam[li] / (2 * np.pi)
+        reff0 = [[np.sum(rr ** 4 * weights(li, rh0, b, c, x)) / np.sum(rr ** 3 * weights(li, rh0, b, c, x))
+                  for c in range(ncomp)] for b in range(nbin)]
+        mass0 = [None] * nbin
+        for ri in range(nrh):
+            raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag) for c in range(ncomp)]
+            for b in range(nbin):
+                psd = [weights(li, ri, b, c, x) for c in range(ncomp)]
+                rhop = float(np.asarray(spec["rhop"])[b, ri])
+                rhop0 = float(np.asarray(spec["rhop0"])[b])
+                ret = integrate_psd(x, raws, psd, frac[b], lam[li], reff0[b], rhop0, rhop)
+                fin = finalize_unit(ret, ang, float(np.asarray(spec["gf"])[ri]), rhop, [m[li, ri, 0].real],
+                                    [m[li, ri, 0].imag], float(np.asarray(spec["rlow"])[b]),
+                                    float(np.asarray(spec["rup"])[b]))
+                if ri == 0:
+                    mass0[b] = fin["volume"] * rhop0
+                fin["area"] = fin["area"] / mass0[b]
+                fin["volume"] = fin["volume"] / mass0[b]
+                for k in SCATKEYS:
+                    out[k][b, li, ri] = fin[k]
+                out["pback"][b, li, ri] = fin["pback"]
+                for k in SCALARKEYS + EXTRAKEYS:
+                    out[k][b, li, ri] = fin[k]
+                for k in NLSCALARKEYS:
+                    out["nl_" + k][b, li, ri] = fin[k]
+    if n_gsf:
+        F = np.stack([out[k] for k in ["p11", "p22", "p33", "p44", "p12", "p34"]], axis=3)
+        coef, _ = ogsf.expand(ang, F.reshape(-1, 6, ang.size), n_gsf)
+        coef = coef.reshape(nbin, nl, nrh, 6, n_gsf)
+        out["pmom"] = coef[:, :, :, [0, 4, 2, 5, 1, 3], :]
+    return out

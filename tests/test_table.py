@@ -1,0 +1,113 @@
+"""Table generation (dointegration.fun drop-in) and GSF expansion on the GPU.
+
+Parity: the reference's own tables (tests/golden/table_*.npz, produced by
+dointegration.fun) and, for layouts the reference does not produce (radius
+grids shared by several bins, the GSF moments), the oracle's restatement.
+Tolerances: phase elements 1e-9 relative to P11 at the same angle; qext,
+qsca, g 1e-10 relative; the other scalars 1e-9 relative; GSF moments 1e-9
+absolute (they are normalised to alpha1(0) = 1; the reference writes them
+rounded to 1e-10).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+SCAT = ["p11", "p12", "p22", "p33", "p34", "p44"]
+TIGHT = ["qext", "qsca", "g"]
+LOOSE = ["qb", "csca", "cext", "ssa", "bsca", "bext", "bbck", "refreal", "refimag", "lidar_ratio"]
+NL = ["mass", "volume", "area", "rEff", "rMass", "rhop", "growth_factor", "rLow", "rUp"]
+
+
+def _check_table(got, ref, prefix=""):
+    p11 = np.abs(ref[prefix + "p11"])
+    for k in SCAT:
+        err = np.max(np.abs(got[k] - ref[prefix + k]) / p11)
+        assert err < 1e-9, (k, err)
+    pb = ref[prefix + "pback"]
+    assert np.max(np.abs(got["pback"] - pb) / np.abs(pb[..., :1])) < 1e-9
+    for k, tol in [(k, 1e-10) for k in TIGHT] + [(k, 1e-9) for k in LOOSE]:
+        r = ref[prefix + k]
+        err = np.max(np.abs(got[k] - r) / np.maximum(np.abs(r), 1e-300))
+        assert err < tol, (k, err)
+    # qabs = qext - qsca cancels for weakly absorbing particles: 1e-10 of qext
+    err = np.max(np.abs(got["qabs"] - ref[prefix + "qabs"]) / np.abs(ref[prefix + "qext"]))
+    assert err < 1e-10, ("qabs", err)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt"])
+def test_reference_tables_gpu(name):
+    from geosmie_gb300 import table
+    g = load_golden("table_%s.npz" % name)
+    params = json.loads(str(g["params_json"]))
+    got = table.run_table(params, list(g["mlist"]), g["waterm"])
+    _check_table(got, g, "out_")
+    for k in NL:
+        r = g["out_" + k]
+        assert np.max(np.abs(got[k] - r) / np.maximum(np.abs(r), 1e-300)) < 1e-9, k
+
+
+def synthetic_spec(nl=3, nrh=4, ns=300, nbin=3, nang=181, seed=20261203):
+    """Small radius-grid table: several lognormal bins sharing one grid,
+    kappa growth (the layout of the sulfate-like benchmark table)."""
+    rng = np.random.default_rng(seed)
+    lam = np.logspace(np.log10(0.2e-6), np.log10(4e-6), nl)
+    rh = np.linspace(0.0, 0.95, nrh)
+    gf = (1 + 0.6 * rh / (1 - rh)) ** (1.0 / 3.0)
+    r = np.logspace(np.log10(0.005e-6), np.log10(5e-6), ns)
+    ndry, nw = 1.43 + 1e-8j, 1.333 + 1e-9j
+    m = np.empty((nl, nrh, 1), np.complex128)
+    for i in range(nl):
+        m[i, :, 0] = nw + (ndry - nw) / gf ** 3 * (1 + 0.01 * rng.random())
+    rg = 0.0695e-6 * np.array([0.5, 1.0, 2.0, 4.0, 0.25])[:nbin]
+    return {
+        "lambda": lam, "grid": r, "dgrid": np.gradient(r), "grid_kind": 1, "m": m,
+        "psd_kind": 0, "psd_param": np.array([[[g_, 0.0, 1e30, 2.03]] for g_ in rg]), "gf_psd": gf,
+        "rh0_index": 0, "frac": np.ones((nbin, 1)), "rhop": (gf[None, :] ** -3 * 1700 + (1 - gf ** -3) * 1000) *
+        np.ones((nbin, 1)), "rhop0": np.full(nbin, 1700.0), "gf": gf, "rlow": np.full(nbin, 0.005e-6),
+        "rup": np.full(nbin, 5e-6), "ang": np.linspace(0.0, 180.0, nang),
+    }
+
+
+@pytest.mark.gpu
+def test_radius_grid_multibin_with_gsf_gpu():
+    from geosmie_gb300.table import TablePlan
+    from oracle import integration
+    spec = synthetic_spec()
+    plan = TablePlan(spec, n_gsf=32)
+    plan.run()
+    got = plan.results()
+    ref = integration.run_spec(spec, n_gsf=32)
+    _check_table(got, ref)
+    for k in NL:
+        assert np.max(np.abs(got["nl_" + k] - ref["nl_" + k]) / np.abs(ref["nl_" + k])) < 1e-9, k
+    assert np.max(np.abs(got["pmom"] - ref["pmom"])) < 1e-9
+    # idempotence: a second run of the same plan gives the same table
+    plan.run()
+    again = plan.results()
+    assert np.max(np.abs(again["p11"] - got["p11"]) / got["p11"]) < 1e-13
+
+
+@pytest.mark.gpu
+def test_gsf_api_gpu():
+    from geosmie_gb300 import gsf
+    from oracle import gsf as ogsf
+    ang = np.linspace(0.0, 180.0, 361)
+    mu = np.cos(np.radians(ang))
+    F = np.zeros((3, 6, ang.size))
+    for t, g in enumerate([0.3, 0.6, 0.85]):
+        p = (1 - g * g) / (1 + g * g - 2 * g * mu) ** 1.5
+        F[t, 0] = p
+        F[t, 1] = 0.9 * p
+        F[t, 2] = 0.8 * p * mu
+        F[t, 3] = 0.7 * p * mu
+        F[t, 4] = -0.2 * p * (1 - mu * mu)
+        F[t, 5] = 0.1 * p * (1 - mu * mu)
+    for ng in [64, 129]:
+        got, cn = gsf.expand(ang, F, ng)
+        ref, rcn = ogsf.expand(ang, F, ng)
+        assert np.max(np.abs(got - ref)) < 1e-10, ng
+        assert np.max(np.abs(cn - rcn) / rcn) < 1e-12
