@@ -1,0 +1,309 @@
+#!/usr/bin/env python3
+"""Benchmark: Mie instance-evaluations per second of a whole optics table.
+
+One step = one full sulfate-like table on the GPU: 36 RH x 60 wavelengths x
+5 lognormal bins on one shared grid of 2000 wet radii (4.32e6 Mie instances),
+181 scattering angles, size/RH integration and 64 GSF moments -- the
+(bin x wavelength x RH) sweep of dointegration.fun followed by the pygeos
+pass of rungsf.  Inputs are synthetic and seeded (geosmie_gb300/workloads.py).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  --impl reference times the CPU restatement of the
+reference's own per-size algorithm (oracle/, scipy Bessel functions, per-angle
+sums) on the host cores over a fixed stratified sample of the same table.
+Multi-GPU: replicas (each rank builds the whole table; the path needs no
+exchange), value = all ranks' instances / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mie instance-evals/s + table gen time, mixed vs FP64 plain on 1 GB300 at ≤1e-6 rel"
+UNIT = "instance-evals/s"
+# CPU sample: wavelength and RH indices of the stratified sample of units
+SAMPLE_LAMBDA = [0, 12, 24, 36, 48, 59]
+SAMPLE_RH = [0, 35]
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _oracle_unit(args):
+    """One (wavelength, RH) unit of the table on the CPU with the oracle:
+    per-size coefficients, per-angle S1/S2 sums (pymiecoated's algorithm),
+    Mueller elements, integration of all bins, normalisation, GSF."""
+    spec, li, ri, n_gsf = args
+    from oracle import gsf as ogsf
+    from oracle import integration as oi
+    lam = float(spec["lambda"][li])
+    x = 2 * np.pi * np.asarray(spec["grid"]) / lam
+    m = complex(spec["m"][li, ri, 0])
+    ang = np.asarray(spec["ang"])
+    raw = oi.raw_mie(x, np.cos(np.radians(ang)), lam, m.real, m.imag, batch=False)
+    gf = float(spec["gf_psd"][ri])
+    out = []
+    for b in range(np.asarray(spec["frac"]).shape[0]):
+        pp = spec["psd_param"][b][0]
+        w = oi.lognorm_psd(pp[0] * gf, pp[3], x, lam, pp[2] * gf, pp[1]) * spec["dgrid"]
+        w = w / w.sum()
+        w0 = oi.lognorm_psd(pp[0], pp[3], x, lam, pp[2], pp[1]) * spec["dgrid"]
+        rr = x * lam / (2 * np.pi)
+        reff0 = np.sum(rr ** 4 * w0) / np.sum(rr ** 3 * w0)
+        ret = oi.integrate_psd(x, [raw], [w], [1.0], lam, [reff0], float(spec["rhop0"][b]),
+                               float(spec["rhop"][b, ri]))
+        fin = oi.finalize_unit(ret, ang, gf, float(spec["rhop"][b, ri]), [m.real], [m.imag], 0.0, 0.0)
+        out.append(np.stack([fin[k] for k in ["p11", "p22", "p33", "p44", "p12", "p34"]]))
+    ogsf.expand(ang, np.array(out), n_gsf)
+    return x.size
+
+
+def cpu_sample(spec, n_gsf, processes=1):
+    units = [(spec, li, ri, n_gsf) for li in SAMPLE_LAMBDA for ri in SAMPLE_RH]
+    t0 = time.perf_counter()
+    if processes > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(processes) as pool:
+            n = sum(pool.map(_oracle_unit, units))
+    else:
+        n = sum(_oracle_unit(u) for u in units)
+    return n, time.perf_counter() - t0, len(units)
+
+
+def run_reference(args):
+    """--impl reference: the CPU path timed on the host cores (rank 0 only)."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from geosmie_gb300 import workloads
+    from oracle import gsf as ogsf
+    ogsf.build()
+    spec, desc = workloads.sulfate_table()
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(spec, 64, processes=cores)
+    times = []
+    n = 0
+    for _ in range(args.steps):
+        n, dt, nu = cpu_sample(spec, 64, processes=cores)
+        times.append(dt)
+    tot = sum(times)
+    value = n * args.steps / tot
+    sample = ("%d of 2160 (wavelength, RH) units of the table (wavelength indices %s x RH indices %s), "
+              "2000 radii each, all 5 bins, 181 angles, 64 GSF moments" % (len(SAMPLE_LAMBDA) * len(SAMPLE_RH),
+                                                                          SAMPLE_LAMBDA, SAMPLE_RH))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                         "note": "CPU restatement of pymiecoated + dointegration (scipy jv/yv, per-angle "
+                                 "sums; the reference's numba is not installed) and of spher_expan.f in C, "
+                                 "multiprocessing pool over units"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "projected_table_s": 4.32e6 / value,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+class Clocks(object):
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="reduced table (quick check, not a bench line)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local
+    from geosmie_gb300 import _native, workloads
+    from geosmie_gb300.table import TablePlan
+    ctx = _native.context(dev)
+    if args.small:
+        spec, desc = workloads.sulfate_table(n_rh=6, n_lambda=10, n_radii=500)
+    else:
+        spec, desc = workloads.sulfate_table()
+    counts = workloads.work_counts(spec)
+    n_gsf = 64
+    peak = _native._D()
+    ctx.call("gbmie_measure_fp64_peak", _native.ctypes.byref(peak))
+    fp64_peak = peak.value
+
+    plan = TablePlan(spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=n_gsf, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:%d" % dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        plan.run()
+    plan.sync()
+    # ---- timed region: K tables, L2 flushed (256 MB write) before each ----
+    clocks = Clocks(dev)
+    ctx.set_timing(True)
+    launches0 = ctx.launches()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+        plan.run()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    launches = ctx.launches() - launches0
+    ktimes = ctx.kernel_times()
+    ctx.set_timing(False)
+    if ws > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda:%d" % dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    ms_step = ms / args.steps
+    value = ws * counts["instances"] * args.steps / (ms * 1e-3)
+
+    # ---- end to end through the public API: host inputs in, host table out ----
+    e2e_times = []
+    h2d = d2h = 0
+    for it in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        p2 = TablePlan(spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=n_gsf, device=dev)
+        p2.run()
+        res = p2.results()
+        t1 = time.perf_counter()
+        p2.close()
+        e2e_times.append(t1 - t0)
+        h2d = sum(v.numel() * v.element_size() for v in p2.t.values())
+        d2h = sum(v.numel() * v.element_size() for v in p2.out_t.values())
+    e2e_value = ws * counts["instances"] * len(e2e_times) / sum(e2e_times)
+
+    # ---- roofline of the dominant kernel (FP64 pipe) ----
+    top = max(ktimes.items(), key=lambda kv: kv[1][1]) if ktimes else (None, (0, 0.0))
+    nang, nbin = counts["nang"], counts["nbin"]
+    flops = {
+        # S+/S- sums (4 DFMA per order and angle), Mueller elements (14 flop),
+        # number-weighted accumulation (4 FMA per bin)
+        "k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * counts["instances"]) * nang,
+        # D_n steps (12 flop), a_n/b_n and efficiency sums (89 flop per order)
+        "k_tab_coeffs": 12.0 * counts["sum_nmx"] + 89.0 * counts["sum_nmax"],
+    }
+    roof = None
+    kernels = {}
+    for name, (nl_, tms) in ktimes.items():
+        kernels[name] = {"launches": nl_, "ms_per_launch": tms / max(nl_, 1), "share": tms / max(1e-9, sum(
+            v[1] for v in ktimes.values()))}
+        if name in flops:
+            kernels[name]["gflops"] = flops[name] / (tms / nl_ * 1e-3) / 1e9
+    if top[0] in flops:
+        nl_, tms = top[1]
+        ach = flops[top[0]] / (tms / nl_ * 1e-3) / 1e9
+        roof = {"bound": "fp64", "kernel": top[0], "achieved": ach, "peak": fp64_peak, "unit": "GFLOP/s",
+                "frac": ach / fp64_peak, "traffic": None,
+                "peak_source": "DFMA throughput measured in this run (gbmie_measure_fp64_peak); "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "algorithmic_flop_per_launch": flops[top[0]]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline and not args.small:
+        n, dt, nu = cpu_sample(spec, n_gsf, processes=1)
+        cpu = {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "%d (wavelength, RH) units x 2000 radii, all bins, 181 angles, 64 GSF moments; "
+                         "CPU restatement of the reference algorithm (numba absent)" % nu,
+               "seconds": dt}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; no dataset)",
+        "config": {"workload": desc, "instances": counts["instances"], "sum_nmax": counts["sum_nmax"],
+                   "gsf_moments": n_gsf, "precision": "plain FP64", "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "l2": "flushed before every table (256 MB write inside the timed region)"},
+        "table_gen_ms": {"plain_fp64": ms_step},
+        "roofline": roof,
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "note": "TablePlan from host arrays (H2D, device layout) + run + results() (D2H) per step"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "fp64_peak_gflops": fp64_peak,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

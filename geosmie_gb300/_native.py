@@ -40,6 +40,8 @@ SIGNATURES = {
     "gbmie_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "gbmie_last_error": (ctypes.c_char_p, [_P]),
     "gbmie_launch_count": (_I64, [_P]),
+    "gbmie_ctx_set_timing": (ctypes.c_int, [_P, ctypes.c_int]),
+    "gbmie_ctx_kernel_times": (ctypes.c_int, [_P, _I32, _P, _P, _P, ctypes.POINTER(_I32)]),
     "gbmie_nmax": (ctypes.c_int, [_P, _D, ctypes.POINTER(_I32)]),
     "gbmie_layout": (ctypes.c_int, [_P, _I64, _P, _P, ctypes.POINTER(_I64)]),
     "gbmie_coeffs": (ctypes.c_int, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
@@ -133,6 +135,21 @@ class Context:
 
     def launches(self):
         return int(self.lib.gbmie_launch_count(self.h))
+
+    def set_timing(self, enable):
+        self.check(self.lib.gbmie_ctx_set_timing(self.h, int(enable)), "gbmie_ctx_set_timing")
+
+    def kernel_times(self):
+        """{kernel name: (launches, total device ms)} since timing was enabled."""
+        cap = 64
+        names = (ctypes.c_char_p * cap)()
+        launches = (ctypes.c_int64 * cap)()
+        ms = (ctypes.c_double * cap)()
+        n = _I32()
+        self.bind_stream()
+        self.check(self.lib.gbmie_ctx_kernel_times(self.h, cap, names, launches, ms, ctypes.byref(n)),
+                   "gbmie_ctx_kernel_times")
+        return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(n.value)}
 
 
 _ctx = {}

@@ -84,9 +84,19 @@ __host__ __device__ __forceinline__ int psi_start(double x, int nmax) {
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
+#define GBMIE_TIMER_CAP 8192
+struct gbmie_timer_rec {
+    const char *name;
+    cudaEvent_t start, stop;
+};
+
 struct gbmie_ctx {
     int device;
     cudaStream_t stream;
+    int timing;               // per-kernel event timing enabled
+    int timer_open;           // a start event is recorded and awaits its kernel
+    int ntimer;
+    gbmie_timer_rec *timers;  // GBMIE_TIMER_CAP records (events created lazily)
     void *scratch;            // grown on demand
     size_t scratch_bytes;
     int *d_flags;             // device error flags
@@ -102,6 +112,9 @@ int ctx_cuda(gbmie_ctx *ctx, cudaError_t e, const char *what);
 // it must reallocate).  Returns GBMIE_OK or an error status.
 int ctx_scratch(gbmie_ctx *ctx, size_t bytes, void **ptr);
 int ctx_check_launch(gbmie_ctx *ctx, const char *what);
+// Call right before a kernel launch: records the start event when timing is
+// enabled (ctx_check_launch records the matching stop event).
+void ctx_pre_launch(gbmie_ctx *ctx);
 
 #define GBMIE_TRY(expr)                         \
     do {                                        \

@@ -116,6 +116,7 @@ int launch_coeffs_uniform(gbmie_ctx *ctx, int64_t n, const double *x, double2 ep
                           double2 *an, double2 *bn, double *eff)
 {
     if (n == 0) return GBMIE_OK;
+    ctx_pre_launch(ctx);
     k_coeffs_uniform<<<(unsigned)ceil_div64(n, 128), 128, 0, ctx->stream>>>(n, x, eps, off, an, bn, eff,
                                                                              ctx->d_flags);
     return ctx_check_launch(ctx, "k_coeffs_uniform");
@@ -142,6 +143,7 @@ extern "C" int gbmie_coeffs(gbmie_ctx *ctx, int64_t n, const double *x, const do
         GBMIE_TRY(ctx_scratch(ctx, (size_t)(5 * total + 1) * sizeof(double2), &p));
         dscr = (double2 *)p;
     }
+    ctx_pre_launch(ctx);
     k_coeffs_api<<<(unsigned)ceil_div64(n, 128), 128, 0, ctx->stream>>>(
         n, x, y, (const double2 *)eps, (const double2 *)mu, (const double2 *)eps2, offsets, (double2 *)an,
         (double2 *)bn, eff, dscr, ctx->d_flags);

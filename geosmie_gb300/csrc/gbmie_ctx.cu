@@ -23,9 +23,28 @@ int ctx_cuda(gbmie_ctx *ctx, cudaError_t e, const char *what)
     return ctx_fail(ctx, st, "%s: %s", what, cudaGetErrorString(e));
 }
 
+void ctx_pre_launch(gbmie_ctx *ctx)
+{
+    if (!ctx->timing || ctx->ntimer >= GBMIE_TIMER_CAP) return;
+    gbmie_timer_rec &r = ctx->timers[ctx->ntimer];
+    if (!r.start) {
+        cudaEventCreate(&r.start);
+        cudaEventCreate(&r.stop);
+    }
+    cudaEventRecord(r.start, ctx->stream);
+    ctx->timer_open = 1;
+}
+
 int ctx_check_launch(gbmie_ctx *ctx, const char *what)
 {
     ctx->launches++;
+    if (ctx->timer_open) {
+        gbmie_timer_rec &r = ctx->timers[ctx->ntimer];
+        cudaEventRecord(r.stop, ctx->stream);
+        r.name = what;
+        ctx->ntimer++;
+        ctx->timer_open = 0;
+    }
     return ctx_cuda(ctx, cudaGetLastError(), what);
 }
 
@@ -100,10 +119,58 @@ int gbmie_ctx_destroy(gbmie_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     else cudaDeviceSynchronize();
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->timers) {
+        for (int i = 0; i < GBMIE_TIMER_CAP; ++i)
+            if (ctx->timers[i].start) {
+                cudaEventDestroy(ctx->timers[i].start);
+                cudaEventDestroy(ctx->timers[i].stop);
+            }
+        free(ctx->timers);
+    }
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     free(ctx);
+    return GBMIE_OK;
+}
+
+int gbmie_ctx_set_timing(gbmie_ctx *ctx, int enable)
+{
+    if (!ctx) return GBMIE_ERR_INVALID;
+    if (enable && !ctx->timers) {
+        ctx->timers = (gbmie_timer_rec *)calloc(GBMIE_TIMER_CAP, sizeof(gbmie_timer_rec));
+        if (!ctx->timers) return GBMIE_ERR_NOMEM;
+    }
+    ctx->timing = enable ? 1 : 0;
+    ctx->ntimer = 0;
+    ctx->timer_open = 0;
+    return GBMIE_OK;
+}
+
+int gbmie_ctx_kernel_times(gbmie_ctx *ctx, int32_t cap, const char **names, int64_t *launches, double *total_ms,
+                           int32_t *n)
+{
+    if (!ctx || !n || cap < 0 || (cap > 0 && (!names || !launches || !total_ms))) return GBMIE_ERR_INVALID;
+    *n = 0;
+    if (!ctx->timers) return GBMIE_OK;
+    GBMIE_TRY(ctx_cuda(ctx, cudaStreamSynchronize(ctx->stream), "timing sync"));
+    int nk = 0;
+    for (int i = 0; i < ctx->ntimer; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->timers[i].start, ctx->timers[i].stop);
+        int k = 0;
+        while (k < nk && strcmp(names[k], ctx->timers[i].name) != 0) ++k;
+        if (k == nk) {
+            if (nk >= cap) continue;
+            names[k] = ctx->timers[i].name;
+            launches[k] = 0;
+            total_ms[k] = 0.0;
+            ++nk;
+        }
+        launches[k] += 1;
+        total_ms[k] += ms;
+    }
+    *n = nk;
     return GBMIE_OK;
 }
 
@@ -239,10 +306,13 @@ static int layout_impl(gbmie_ctx *ctx, int64_t n, const double *size, int64_t ad
 {
     const int64_t per = SCAN_THREADS * SCAN_ITEMS;
     const int64_t nb = ceil_div64(n, per);
+    ctx_pre_launch(ctx);
     k_layout_blocks<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(n, size, add, off, aux, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_layout_blocks"));
+    ctx_pre_launch(ctx);
     k_layout_bsum<<<1, SCAN_THREADS, 0, ctx->stream>>>(nb, aux, total_dev);
     GBMIE_TRY(ctx_check_launch(ctx, "k_layout_bsum"));
+    ctx_pre_launch(ctx);
     k_layout_add<<<(unsigned)ceil_div64(n, 256), 256, 0, ctx->stream>>>(n, aux, off);
     return ctx_check_launch(ctx, "k_layout_add");
 }
@@ -293,6 +363,7 @@ extern "C" int gbmie_nmax(gbmie_ctx *ctx, double x, int32_t *nmax)
     cudaSetDevice(ctx->device);
     int *d = NULL;
     GBMIE_TRY(ctx_cuda(ctx, cudaMallocAsync((void **)&d, sizeof(int), ctx->stream), "nmax alloc"));
+    ctx_pre_launch(ctx);
     k_nmax_one<<<1, 1, 0, ctx->stream>>>(x, d);
     int st = ctx_check_launch(ctx, "k_nmax_one");
     if (st == GBMIE_OK)

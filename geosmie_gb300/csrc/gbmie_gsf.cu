@@ -204,10 +204,13 @@ int gsf_prepare(gbmie_ctx *ctx, int ng, int nang, const double *theta, GsfTables
     t->frac = (double *)p; p += sizeof(double) * ng;
     t->base = (int *)p;
     const int tb = 128, nb = (ng + tb - 1) / tb;
+    ctx_pre_launch(ctx);
     k_gsf_nodes<<<nb, tb, 0, ctx->stream>>>(ng, t->z, t->w);
     GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_nodes"));
+    ctx_pre_launch(ctx);
     k_gsf_gener<<<nb, tb, 0, ctx->stream>>>(ng, t->L, t->z, t->P);
     GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_gener"));
+    ctx_pre_launch(ctx);
     k_gsf_interp<<<nb, tb, 0, ctx->stream>>>(ng, nang, t->z, theta, t->base, t->frac);
     return ctx_check_launch(ctx, "k_gsf_interp");
 }
@@ -226,6 +229,7 @@ int launch_gsf_expand(gbmie_ctx *ctx, const GsfTables *t, int ntab, const double
     int threads = ((t->L + 31) / 32) * 32;
     if (threads > 256) threads = 256;
     const int grid = ntab < 152 * 16 ? ntab : 152 * 16;
+    ctx_pre_launch(ctx);
     k_gsf_expand<<<grid, threads, 0, ctx->stream>>>(ntab, t->nang, t->ng, t->L, F, entry_stride, row_stride, map,
                                                     t->w, t->P, t->base, t->frac, coef, out_stride, out_row_stride,
                                                     cnorm);
@@ -254,6 +258,7 @@ extern "C" int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const doubl
     void *p = nullptr;
     GBMIE_TRY(ctx_scratch(ctx, sizeof(double) * nang, &p));
     double *theta = (double *)p;
+    ctx_pre_launch(ctx);
     k_deg2rad<<<(nang + 127) / 128, 128, 0, ctx->stream>>>(nang, ang_deg, theta, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_deg2rad"));
     GsfTables t{};

@@ -54,6 +54,7 @@ __global__ void k_pitau(int nang, const double *__restrict__ cost, int nmax, dou
 
 int launch_pq_table(gbmie_ctx *ctx, int nang, const double *cost, int nmax, double2 *pq)
 {
+    ctx_pre_launch(ctx);
     k_pitau<0><<<(nang + 127) / 128, 128, 0, ctx->stream>>>(nang, cost, nmax, pq, nullptr, nullptr, ctx->d_flags);
     return ctx_check_launch(ctx, "k_pitau");
 }
@@ -66,6 +67,7 @@ extern "C" int gbmie_pitau(gbmie_ctx *ctx, int32_t nang, const double *cos_theta
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_pitau: bad arguments");
     if (nang == 0) return GBMIE_OK;
     cudaSetDevice(ctx->device);
+    ctx_pre_launch(ctx);
     k_pitau<1><<<(nang + 127) / 128, 128, 0, ctx->stream>>>(nang, cos_theta, nmax, nullptr, pi_out, tau_out,
                                                             ctx->d_flags);
     return ctx_check_launch(ctx, "k_pitau");
@@ -124,6 +126,7 @@ int launch_s12_api(gbmie_ctx *ctx, int64_t n, const int64_t *off, const double2 
 {
     if (n == 0 || nang == 0) return GBMIE_OK;
     const unsigned grid = (unsigned)(n < 152 * 64 ? n : 152 * 64);
+    ctx_pre_launch(ctx);
     k_s12_api<<<grid, S12_THREADS, 0, ctx->stream>>>(n, off, an, bn, nang, pq, s1, s2);
     return ctx_check_launch(ctx, "k_s12_api");
 }
@@ -155,6 +158,7 @@ extern "C" int gbmie_s12(gbmie_ctx *ctx, int64_t n, const int64_t *offsets, cons
     unsigned long long *dmax = nullptr;
     GBMIE_TRY(ctx_cuda(ctx, cudaMallocAsync((void **)&dmax, sizeof(unsigned long long), ctx->stream), "s12"));
     cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), ctx->stream);
+    ctx_pre_launch(ctx);
     k_max_gap<<<152, 256, 0, ctx->stream>>>(n, offsets, dmax);
     int st = ctx_check_launch(ctx, "k_max_gap");
     if (st == GBMIE_OK)
@@ -196,6 +200,7 @@ extern "C" int gbmie_size_range(gbmie_ctx *ctx, int64_t n, const double *x, doub
         st = ctx_cuda(ctx, cudaMallocAsync((void **)&dm, 8, ctx->stream), "size_range max");
         if (st == GBMIE_OK) {
             cudaMemsetAsync(dm, 0, 8, ctx->stream);
+            ctx_pre_launch(ctx);
             k_max_gap<<<152, 256, 0, ctx->stream>>>(n, off, dm);
             st = ctx_check_launch(ctx, "k_max_gap");
             if (st == GBMIE_OK)

@@ -570,6 +570,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     if (st == GBMIE_OK)
         st = ctx_cuda(ctx, cudaMalloc(&p->unit_base, sizeof(int64_t) * p->n_units), "plan unit base");
     if (st == GBMIE_OK) {
+        ctx_pre_launch(ctx);
         k_tab_make_x<<<(unsigned)ceil_div64(nrows, 256), 256, 0, ctx->stream>>>(p->n_le, d.n_size, d.grid_kind,
                                                                                d.grid, d.lambda, p->xg,
                                                                                ctx->d_flags);
@@ -660,11 +661,14 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     const gbmie_table_desc &d = p->d;
     cudaStream_t st = ctx->stream;
     const int64_t nrows = (int64_t)p->n_le * d.n_size;
+    ctx_pre_launch(ctx);
     k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_psi_chi"));
     const int64_t nW = (int64_t)d.n_lambda * d.n_rh * d.n_bin * d.n_comp;
+    ctx_pre_launch(ctx);
     k_tab_weights<<<(unsigned)nW, 256, 0, st>>>(v, d.weights);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_weights"));
+    ctx_pre_launch(ctx);
     k_tab_coeffs<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs"));
     GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
@@ -674,13 +678,16 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     const int nchunk = (d.n_size + chunk - 1) / chunk;
     const int threads = d.n_ang >= 256 ? 256 : ((d.n_ang + 31) / 32) * 32;
     const unsigned grid = (unsigned)(p->n_units * nchunk);
+    ctx_pre_launch(ctx);
     if (d.n_bin <= 1) k_tab_s12_plain<1><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     else if (d.n_bin <= 2) k_tab_s12_plain<2><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     else if (d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_s12_plain"));
+    ctx_pre_launch(ctx);
     k_tab_scalars<<<(unsigned)p->n_entries, 256, 0, st>>>(v);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_scalars"));
+    ctx_pre_launch(ctx);
     k_tab_finalize<<<(unsigned)p->n_entries, 256, 0, st>>>(v, *out);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
     if (p->has_gsf) {

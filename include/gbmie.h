@@ -62,6 +62,15 @@ const char *gbmie_status_string(int status);
 const char *gbmie_last_error(const gbmie_ctx *ctx);
 /* Kernel launches issued by this context so far (host counter). */
 int64_t gbmie_launch_count(const gbmie_ctx *ctx);
+/* Per-kernel device timing: when enabled, every kernel the context launches
+ * is bracketed by CUDA events on its stream.  gbmie_ctx_kernel_times
+ * synchronises and reports, for up to `cap` distinct kernels, the name (a
+ * static string owned by the library), the launch count and the summed
+ * device time in ms; *n receives the number of kernels.  Enabling clears
+ * earlier records.  No counterpart in the reference (measurement only). */
+int gbmie_ctx_set_timing(gbmie_ctx *ctx, int enable);
+int gbmie_ctx_kernel_times(gbmie_ctx *ctx, int32_t cap, const char **names, int64_t *launches,
+                           double *total_ms, int32_t *n);
 
 /* Number of partial waves round(2 + x + 4 x^(1/3)) for one size parameter,
  * computed by the same device function the kernels use (host result).
