@@ -81,6 +81,7 @@ const char *gbmie_status_string(int status)
     case GBMIE_ERR_TIMEOUT: return "device wait timed out";
     case GBMIE_ERR_NOMEM: return "out of device memory";
     case GBMIE_ERR_UNSUPPORTED: return "unsupported option";
+    case GBMIE_ERR_CAPACITY: return "request exceeds the fixed device array of gbmie_s12_noalloc";
     default: return "unknown status";
     }
 }

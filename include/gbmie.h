@@ -41,6 +41,8 @@ extern "C" {
 #define GBMIE_ERR_TIMEOUT 4     /* a device-side wait hit its iteration limit */
 #define GBMIE_ERR_NOMEM 5       /* device allocation failed */
 #define GBMIE_ERR_UNSUPPORTED 6 /* option not implemented */
+#define GBMIE_ERR_CAPACITY 7    /* request larger than gbmie_s12_noalloc's fixed
+                                   device array */
 
 #define GBMIE_MAX_NMAX 100000   /* x up to about 9.9e4 */
 
@@ -115,6 +117,24 @@ int gbmie_pitau(gbmie_ctx *ctx, int32_t nang, const double *cos_theta,
 int gbmie_s12(gbmie_ctx *ctx, int64_t n, const int64_t *offsets,
               const gbmie_complex *an, const gbmie_complex *bn, int32_t nang,
               const double *cos_theta, gbmie_complex *s1, gbmie_complex *s2);
+
+/* gbmie_s12 for callers that cannot allocate device memory (code running in
+ * another framework's memory pool, or recorded into someone else's CUDA
+ * graph, or that must not grow the device footprint after start-up).  No
+ * counterpart in the reference.  Allocates nothing: no context, no scratch;
+ * the angular table lives in a fixed 4 MiB device array inside the library
+ * (held by every GPU that loads it until exit), so nmax_max * nang must not
+ * exceed 262144 (e.g. nmax 700 with 371 angles), else GBMIE_ERR_CAPACITY.
+ * nmax_max (host) bounds every instance's offsets[i+1] - offsets[i]; an
+ * instance above it returns GBMIE_ERR_NMAX (that instance is skipped).
+ * Runs on `stream` (a cudaStream_t, NULL = legacy default) with the current
+ * device and returns after the stream finishes.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make it before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int gbmie_s12_noalloc(void *stream, int64_t n, const int64_t *offsets, const gbmie_complex *an,
+                      const gbmie_complex *bn, int32_t nmax_max, int32_t nang, const double *cos_theta,
+                      gbmie_complex *s1, gbmie_complex *s2);
 
 /* One MultipleMie(xArr, None, costarr).calculateS12SizeRange(mr, mi) call:
  * eps = (mr + i mi)^2, mu = 1; S1, S2 [n][nang] and eff [n][6] for every x.
