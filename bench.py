@@ -196,40 +196,59 @@ def main():
     ctx.call("gbmie_measure_fp64_peak", _native.ctypes.byref(peak))
     fp64_peak = peak.value
 
-    plan = TablePlan(spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=n_gsf, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:%d" % dev)
     stream = torch.cuda.current_stream(dev)
-    for _ in range(args.warmup):
-        plan.run()
-    plan.sync()
-    # ---- timed region: K tables, L2 flushed (256 MB write) before each ----
-    clocks = Clocks(dev)
-    ctx.set_timing(True)
-    launches0 = ctx.launches()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize(dev)
-    clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        flush.zero_()
-        plan.run()
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1)
-    clk = clocks.stop()
-    launches = ctx.launches() - launches0
-    ktimes = ctx.kernel_times()
-    ctx.set_timing(False)
-    if ws > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda:%d" % dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
+
+    def timed(precision, with_clocks=False):
+        """Warm-up, then K tables between barriers + syncs, L2 flushed before
+        each (256 MB write, inside the timed region).  Returns (ms, launches,
+        kernel times, clocks, plan)."""
+        plan = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=dev)
+        for _ in range(args.warmup):
+            plan.run()
+        plan.sync()
+        clocks = Clocks(dev)
+        ctx.set_timing(True)
+        launches0 = ctx.launches()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        if with_clocks:
+            clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            flush.zero_()
+            plan.run()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        clk = clocks.stop() if with_clocks else None
+        launches = ctx.launches() - launches0
+        kt = ctx.kernel_times()
+        ctx.set_timing(False)
+        if ws > 1:
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda:%d" % dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+            torch.distributed.barrier()
+        return ms, launches, kt, clk, plan
+
+    ms_plain, _, kt_plain, _, plan_plain = timed(_native.GBMIE_PLAIN_FP64)
+    ms, launches, ktimes, clk, plan_mixed = timed(_native.GBMIE_MIXED, with_clocks=True)
     ms_step = ms / args.steps
     value = ws * counts["instances"] * args.steps / (ms * 1e-3)
+    # accuracy of the mixed table against the FP64 table (same run)
+    ra, rb = plan_plain.results(), plan_mixed.results()
+    p11 = np.abs(ra["p11"])
+    acc = {"phase_max_abs_err_over_p11": float(max(np.max(np.abs(rb[k] - ra[k]) / p11)
+                                                  for k in ["p11", "p12", "p22", "p33", "p34", "p44"])),
+           "pmom_max_abs_err_over_max_alpha1": float(np.max(np.abs(rb["pmom"] - ra["pmom"]) / np.max(
+               np.abs(ra["pmom"][..., 0, :]), axis=-1)[..., None, None])),
+           "scalars_max_rel_err": float(max(np.max(np.abs(rb[k] - ra[k]) / np.maximum(np.abs(ra[k]), 1e-300))
+                                            for k in ["qext", "qsca", "g", "qb", "ssa", "bext", "bsca"]))}
+    del plan_plain
 
     # ---- end to end through the public API: host inputs in, host table out ----
     e2e_times = []
@@ -237,7 +256,7 @@ def main():
     for it in range(args.steps):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        p2 = TablePlan(spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=n_gsf, device=dev)
+        p2 = TablePlan(spec, precision=_native.GBMIE_MIXED, n_gsf=n_gsf, device=dev)
         p2.run()
         res = p2.results()
         t1 = time.perf_counter()
@@ -250,20 +269,30 @@ def main():
     # ---- roofline of the dominant kernel (FP64 pipe) ----
     top = max(ktimes.items(), key=lambda kv: kv[1][1]) if ktimes else (None, (0, 0.0))
     nang, nbin = counts["nang"], counts["nbin"]
+    coef_flop = 12.0 * counts["sum_nmx"] + 89.0 * counts["sum_nmax"]
     flops = {
         # S+/S- sums (4 DFMA per order and angle), Mueller elements (14 flop),
         # number-weighted accumulation (4 FMA per bin)
         "k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * counts["instances"]) * nang,
         # D_n steps (12 flop), a_n/b_n and efficiency sums (89 flop per order)
-        "k_tab_coeffs": 12.0 * counts["sum_nmx"] + 89.0 * counts["sum_nmax"],
+        "k_tab_coeffs": coef_flop,
+        "k_tab_coeffs_mixed": coef_flop,
     }
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        peaks = {"bf16_tflops": 1900.0, "hbm_gbs": 6800.0, "fallback": True}
+
+    def kernel_table(kt):
+        out = {}
+        tot = max(1e-9, sum(v[1] for v in kt.values()))
+        for name, (nl_, tms) in kt.items():
+            out[name] = {"launches": nl_, "ms_per_launch": tms / max(nl_, 1), "share": tms / tot}
+            if name in flops:
+                out[name]["fp64_gflops"] = flops[name] / (tms / nl_ * 1e-3) / 1e9
+        return out
+    kernels = kernel_table(ktimes)
     roof = None
-    kernels = {}
-    for name, (nl_, tms) in ktimes.items():
-        kernels[name] = {"launches": nl_, "ms_per_launch": tms / max(nl_, 1), "share": tms / max(1e-9, sum(
-            v[1] for v in ktimes.values()))}
-        if name in flops:
-            kernels[name]["gflops"] = flops[name] / (tms / nl_ * 1e-3) / 1e9
     if top[0] in flops:
         nl_, tms = top[1]
         ach = flops[top[0]] / (tms / nl_ * 1e-3) / 1e9
@@ -272,6 +301,25 @@ def main():
                 "peak_source": "DFMA throughput measured in this run (gbmie_measure_fp64_peak); "
                                "MEASURED_PEAKS.json has no FP64 figure",
                 "algorithmic_flop_per_launch": flops[top[0]]}
+    # tensor-core contraction: executed MMA flop (3 split products x 2 GEMMs,
+    # padded K and N) and algorithmic flop (8 per order and angle, S+/S- form)
+    if "k_tab_s12_tc" in ktimes:
+        nl_, tms = ktimes["k_tab_s12_tc"]
+        sec = tms / nl_ * 1e-3
+        alg = 8.0 * counts["sum_nmax"] * nang
+        # 6 MMAs (M 128 x N 192 x K 16) per 16 orders of a tile, per 192-angle block
+        exe = counts["sum_ktile"] / 16.0 * 6 * 2 * 128 * 192 * 16 * (-(-nang // 192))
+        kernels["k_tab_s12_tc"]["algorithmic_tflops"] = alg / sec / 1e12
+        kernels["k_tab_s12_tc"]["executed_mma_tflops"] = exe / sec / 1e12
+        kernels["k_tab_s12_tc"]["tensor_peak_tflops"] = peaks.get("bf16_tflops")
+        if top[0] == "k_tab_s12_tc":
+            roof = {"bound": "tensor", "kernel": "k_tab_s12_tc", "achieved": exe / sec / 1e12,
+                    "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                    "frac": exe / sec / 1e12 / peaks.get("bf16_tflops"), "traffic": None,
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
+                    "algorithmic_flop_per_launch": alg, "executed_mma_flop_per_launch": exe,
+                    "note": "executed = 3 split products x 2 GEMMs on padded tiles; algorithmic = 8 flop "
+                            "per (order, angle) of the S+/S- sums"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.small:
@@ -284,11 +332,16 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; no dataset)",
+        "vs_baseline": None, "dtype": "f64 recurrences + f16x2-split tensor contractions (f32 accumulate)", "data": "synthetic (seeded; no dataset)",
         "config": {"workload": desc, "instances": counts["instances"], "sum_nmax": counts["sum_nmax"],
-                   "gsf_moments": n_gsf, "precision": "plain FP64", "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "gsf_moments": n_gsf, "precision": "mixed: FP64 recurrences, tcgen05 split-FP16 contractions "
+                   "with FP32 accumulation", "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "l2": "flushed before every table (256 MB write inside the timed region)"},
-        "table_gen_ms": {"plain_fp64": ms_step},
+        "table_gen_ms": {"mixed": ms_step, "plain_fp64": ms_plain / args.steps},
+        "mixed_vs_plain_speedup": ms_plain / ms,
+        "plain_fp64": {"value": ws * counts["instances"] * args.steps / (ms_plain * 1e-3), "unit": UNIT,
+                       "kernels": kernel_table(kt_plain)},
+        "accuracy_mixed_vs_fp64": acc,
         "roofline": roof,
         "kernels": kernels,
         "cpu_baseline": cpu,

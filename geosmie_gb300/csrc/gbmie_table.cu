@@ -22,53 +22,7 @@
 #include "mie_device.cuh"
 #include "gsf.cuh"
 
-#define TWO_PI 6.28318530717958647692
-#define PI_D 3.14159265358979323846
-
-struct gbmie_table_plan {
-    gbmie_ctx *ctx;
-    gbmie_table_desc d;
-    int n_le;
-    int64_t n_units, n_inst, n_entries;
-    double *xg;          // [n_le][n_size]
-    int64_t *off;        // [n_le * n_size + 1]
-    int64_t *unit_base;  // [n_units]
-    int64_t pc_total, ab_total;
-    int nmax_max;
-    size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
-    GsfTables gsf;
-    int has_gsf;
-};
-
-// ---------------------------------------------------------------------------
-// block reduction of K doubles (all threads receive the totals)
-// ---------------------------------------------------------------------------
-template <int K>
-__device__ __forceinline__ void block_sum(double (&v)[K])
-{
-    __shared__ double red[32][K];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < K; ++k) red[wid][k] = v[k];
-    __syncthreads();
-    if (wid == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            double t = lane < nw ? red[lane][k] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (lane == 0) red[0][k] = t;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = red[0][k];
-    __syncthreads();
-}
+#include "table_internal.cuh"
 
 // ---------------------------------------------------------------------------
 // plan kernels
@@ -97,34 +51,18 @@ __global__ void __launch_bounds__(128) k_tab_psi_chi(int64_t nrows, const double
     psi_chi_row(xg[j], (int)(off[j + 1] - o), pc + o);
 }
 
-struct TabView {
-    int n_lambda, n_rh, n_size, n_bin, n_comp, n_ang, grid_kind, psd_kind, rh0;
-    const double *lambda, *grid, *dgrid, *psd_param, *gf_psd, *frac, *rhop, *rhop0, *gf, *rlow, *rup;
-    const double *theta;
-    const double2 *m;
-    const double *xg;
-    const int64_t *off, *unit_base;
-    double2 *pc, *an, *bn;
-    double *eff4, *W, *sums, *reff0, *pacc, *sraw, *nlraw;
-    const double2 *pq;
-    __device__ __forceinline__ int le(int lam) const { return grid_kind == GBMIE_GRID_X ? 0 : lam; }
-    __device__ __forceinline__ double radius(int lam, int i) const {
-        return grid_kind == GBMIE_GRID_RADIUS ? grid[i] : xg[i] * lambda[lam] / TWO_PI;
-    }
-};
-
 // PSD weights of (lam, rh, bin, comp): lognormal dN/dx x dgrid or r^-4 x
 // dgrid, normalised (dointegration.py:546-583, 626-662), or the caller's
 // weights; plus the radius moments and the dry effective radius.
 __global__ void __launch_bounds__(256) k_tab_weights(TabView v, const double *__restrict__ wgiven)
 {
-    const int blk = blockIdx.x;   // ((lam * n_rh + rh) * n_bin + bin) * n_comp + comp
+    const int blk = blockIdx.x;   // ((lam * n_rh + rh) * n_bin + bin) * n_comp + comp, lam = 0 if shared
     const int comp = blk % v.n_comp;
     const int bin = (blk / v.n_comp) % v.n_bin;
     const int rh = (blk / (v.n_comp * v.n_bin)) % v.n_rh;
     const int lam = blk / (v.n_comp * v.n_bin * v.n_rh);
     const int n = v.n_size;
-    double *W = v.W + (size_t)blk * n;
+    double *W = v.W + (size_t)blk * n;   // caller-supplied weights: never wavelength-shared
     const double *xs = v.xg + (size_t)v.le(lam) * n;
     const double *pp = v.psd_param + ((size_t)bin * v.n_comp + comp) * 4;
     const double lamv = v.lambda[lam];
@@ -241,7 +179,7 @@ __global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int
     const int64_t cbase = v.unit_base[unit] - off[0];
     const double2 *A = v.an + cbase, *B = v.bn + cbase;
     const int64_t wstride = v.n_size;
-    const double *Wb = v.W + (size_t)lr * v.n_bin * v.n_comp * wstride + (size_t)comp * wstride;
+    const double *Wb = v.W + v.wlam(lam) + ((size_t)(lr % v.n_rh) * v.n_bin * v.n_comp + comp) * wstride;
     const int nang = v.n_ang;
     for (int a0 = 0; a0 < nang; a0 += blockDim.x) {
         const int a = a0 + threadIdx.x;
@@ -336,7 +274,7 @@ __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
     for (int k = 0; k < 15; ++k) R[k] = 0.0;   // frac-weighted accumulated results
     for (int comp = 0; comp < v.n_comp; ++comp) {
         const int64_t unit = lr * v.n_comp + comp;
-        const double *W = v.W + (((size_t)lr * v.n_bin + bin) * v.n_comp + comp) * v.n_size;
+        const double *W = v.W + v.wlam(lam) + (((size_t)rh * v.n_bin + bin) * v.n_comp + comp) * v.n_size;
         const double *E = v.eff4 + (size_t)unit * v.n_size * 4;
         double s[9];
 #pragma unroll
@@ -359,9 +297,9 @@ __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
         }
         block_sum<9>(s);
         if (threadIdx.x == 0) {
-            const double *m4 = v.sums + (((size_t)lr * v.n_bin + bin) * v.n_comp + comp) * 4;
+            const double *m4 = v.sums + ((((size_t)v.wl(lam) * v.n_rh + rh) * v.n_bin + bin) * v.n_comp + comp) * 4;
             const double num = m4[0], s2 = m4[1], s3 = m4[2], s4 = m4[3];
-            const double reff0 = v.reff0[((size_t)lam * v.n_bin + bin) * v.n_comp + comp];
+            const double reff0 = v.reff0[((size_t)v.wl(lam) * v.n_bin + bin) * v.n_comp + comp];
             const double area = PI_D * s2 / num;
             const double volume = 4.0 / 3.0 * PI_D * s3 / num;
             const double mass = volume * rhop;
@@ -482,6 +420,7 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.grid_kind = d.grid_kind;
     v.psd_kind = d.psd_kind;
     v.rh0 = d.rh0_index;
+    v.lam_shared = (d.grid_kind == GBMIE_GRID_RADIUS && d.psd_kind != GBMIE_PSD_WEIGHTS) ? 1 : 0;
     v.lambda = d.lambda;
     v.grid = d.grid;
     v.dgrid = d.dgrid;
@@ -518,6 +457,7 @@ static void plan_free(gbmie_table_plan *p)
     if (p->xg) cudaFree(p->xg);
     if (p->off) cudaFree(p->off);
     if (p->unit_base) cudaFree(p->unit_base);
+    if (p->unit_order) cudaFree(p->unit_order);
     gsf_release(&p->gsf);
     free(p);
 }
@@ -549,8 +489,6 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad psd_kind");
     if (d.precision != GBMIE_PLAIN_FP64 && d.precision != GBMIE_MIXED)
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad precision");
-    if (d.precision == GBMIE_MIXED)
-        return ctx_fail(ctx, GBMIE_ERR_UNSUPPORTED, "gbmie_table_plan_create: mixed precision not built");
     if (!d.lambda || !d.grid || !d.dgrid || !d.m || !d.frac || !d.rhop || !d.rhop0 || !d.gf || !d.rlow || !d.rup ||
         !d.cos_theta || !d.theta || (d.psd_kind != GBMIE_PSD_WEIGHTS && (!d.psd_param || !d.gf_psd)) ||
         (d.psd_kind == GBMIE_PSD_WEIGHTS && !d.weights))
@@ -604,6 +542,42 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
             acc += hoff[(int64_t)(le + 1) * d.n_size] - hoff[(int64_t)le * d.n_size];
         }
         p->ab_total = acc;
+        // mixed path: units in decreasing order of work (sum of nmax of their size row)
+        p->n_pad_total = (d.n_ang + 191) / 192 * 192;
+        p->k_pad = (p->nmax_max + 31) / 32 * 32;
+        if (ub && d.precision == GBMIE_MIXED && st == GBMIE_OK) {
+            int64_t *cost = (int64_t *)malloc(sizeof(int64_t) * p->n_units);
+            int *ord = (int *)malloc(sizeof(int) * p->n_units);
+            if (!cost || !ord) st = GBMIE_ERR_NOMEM;
+            for (int64_t u = 0; st == GBMIE_OK && u < p->n_units; ++u) {
+                const int lam = (int)(u / ((int64_t)d.n_rh * d.n_comp));
+                const int le = d.grid_kind == GBMIE_GRID_X ? 0 : lam;
+                cost[u] = hoff[(int64_t)(le + 1) * d.n_size] - hoff[(int64_t)le * d.n_size];
+                ord[u] = (int)u;
+            }
+            if (st == GBMIE_OK) {
+                // insertion-free sort: counting by cost rank is not needed; qsort on (cost desc, id)
+                struct K { int64_t c; int u; };
+                K *keys = (K *)malloc(sizeof(K) * p->n_units);
+                if (!keys) st = GBMIE_ERR_NOMEM;
+                for (int64_t u = 0; keys && u < p->n_units; ++u) keys[u] = K{cost[u], (int)u};
+                if (keys) {
+                    qsort(keys, (size_t)p->n_units, sizeof(K), [](const void *a, const void *b) -> int {
+                        const K *x = (const K *)a, *y = (const K *)b;
+                        if (x->c != y->c) return x->c > y->c ? -1 : 1;
+                        return x->u - y->u;
+                    });
+                    for (int64_t u = 0; u < p->n_units; ++u) ord[u] = keys[u].u;
+                    free(keys);
+                }
+            }
+            if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMalloc(&p->unit_order, sizeof(int) * p->n_units), "unit order");
+            if (st == GBMIE_OK)
+                st = ctx_cuda(ctx, cudaMemcpy(p->unit_order, ord, sizeof(int) * p->n_units, cudaMemcpyHostToDevice),
+                              "unit order copy");
+            free(cost);
+            free(ord);
+        }
         if (ub) {
             st = ctx_cuda(ctx, cudaMemcpy(p->unit_base, ub, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice),
                           "plan unit base copy");
@@ -619,15 +593,21 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
             return at;
         };
         const size_t nW = (size_t)d.n_lambda * d.n_rh * d.n_bin * d.n_comp;
+        const bool mixed = d.precision == GBMIE_MIXED;
         p->o_pc = carve(sizeof(double2) * (size_t)p->pc_total);
-        p->o_an = carve(sizeof(double2) * (size_t)p->ab_total);
-        p->o_bn = carve(sizeof(double2) * (size_t)p->ab_total);
+        p->o_an = carve(mixed ? 16 : sizeof(double2) * (size_t)p->ab_total);
+        p->o_bn = carve(mixed ? 16 : sizeof(double2) * (size_t)p->ab_total);
         p->o_eff = carve(sizeof(double) * 4 * (size_t)p->n_inst);
         p->o_w = carve(sizeof(double) * nW * d.n_size);
         p->o_sums = carve(sizeof(double) * nW * 4);
         p->o_reff0 = carve(sizeof(double) * (size_t)d.n_lambda * d.n_bin * d.n_comp);
         p->o_pacc = carve(sizeof(double) * (size_t)p->n_entries * 4 * d.n_ang);
-        p->o_pq = carve(sizeof(double2) * (size_t)p->nmax_max * d.n_ang);
+        p->o_pq = carve(mixed ? 16 : sizeof(double2) * (size_t)p->nmax_max * d.n_ang);
+        p->o_cf = carve(mixed ? sizeof(float4) * (size_t)p->ab_total : 16);
+        p->o_eexp = carve(mixed ? sizeof(int) * (size_t)p->n_inst : 16);
+        p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
+        p->o_bt = carve(mixed ? 4 * 2 * (size_t)p->n_pad_total * p->k_pad : 16);
+        p->o_counter = carve(16);
         p->o_sraw = carve(sizeof(double) * (size_t)p->n_entries * 10);
         p->o_nlraw = carve(sizeof(double) * (size_t)p->n_entries * 5);
         p->bytes = o;
@@ -648,6 +628,27 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     return GBMIE_OK;
 }
 
+// integratePSD scalars, normalisation and GSF moments (both precisions)
+static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, const gbmie_table_out *out)
+{
+    const gbmie_table_desc &d = p->d;
+    cudaStream_t st = ctx->stream;
+    ctx_pre_launch(ctx);
+    k_tab_scalars<<<(unsigned)p->n_entries, 256, 0, st>>>(v);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_scalars"));
+    ctx_pre_launch(ctx);
+    k_tab_finalize<<<(unsigned)p->n_entries, 256, 0, st>>>(v, *out);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
+    if (p->has_gsf) {
+        GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
+        GBMIE_TRY(launch_gsf_expand(ctx, &p->gsf, (int)p->n_entries, out->phase, (int64_t)6 * d.n_ang, d.n_ang, map,
+                                    out->pmom, (int64_t)6 * d.n_gsf, d.n_gsf, nullptr));
+    }
+    return GBMIE_OK;
+}
+
+int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr);
+
 extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_table_out *out)
 {
     if (!ctx || !p || !out || p->ctx != ctx) return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_run: bad plan");
@@ -664,11 +665,17 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     ctx_pre_launch(ctx);
     k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_psi_chi"));
-    const int64_t nW = (int64_t)d.n_lambda * d.n_rh * d.n_bin * d.n_comp;
+    const int64_t nW = (int64_t)(v.lam_shared ? 1 : d.n_lambda) * d.n_rh * d.n_bin * d.n_comp;
     ctx_pre_launch(ctx);
     k_tab_weights<<<(unsigned)nW, 256, 0, st>>>(v, d.weights);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_weights"));
     ctx_pre_launch(ctx);
+    if (d.precision == GBMIE_MIXED) {
+        GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
+                           "pacc clear"));
+        GBMIE_TRY(launch_table_mixed(ctx, p, v, scr));
+        return launch_table_tail(ctx, p, v, out);
+    }
     k_tab_coeffs<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs"));
     GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
@@ -684,16 +691,5 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     else if (d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_s12_plain"));
-    ctx_pre_launch(ctx);
-    k_tab_scalars<<<(unsigned)p->n_entries, 256, 0, st>>>(v);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_scalars"));
-    ctx_pre_launch(ctx);
-    k_tab_finalize<<<(unsigned)p->n_entries, 256, 0, st>>>(v, *out);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
-    if (p->has_gsf) {
-        GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
-        GBMIE_TRY(launch_gsf_expand(ctx, &p->gsf, (int)p->n_entries, out->phase, (int64_t)6 * d.n_ang, d.n_ang, map,
-                                    out->pmom, (int64_t)6 * d.n_gsf, d.n_gsf, nullptr));
-    }
-    return GBMIE_OK;
+    return launch_table_tail(ctx, p, v, out);
 }

@@ -1,0 +1,86 @@
+// Internal structures of the table pipeline shared by gbmie_table.cu (plain
+// FP64 kernels, plan/run) and gbmie_table_tc.cu (tensor-core kernels).
+#pragma once
+#include "common.cuh"
+#include "gsf.cuh"
+
+#define TWO_PI 6.28318530717958647692
+#define PI_D 3.14159265358979323846
+
+struct gbmie_table_plan {
+    gbmie_ctx *ctx;
+    gbmie_table_desc d;
+    int n_le;
+    int64_t n_units, n_inst, n_entries;
+    double *xg;          // [n_le][n_size]
+    int64_t *off;        // [n_le * n_size + 1]
+    int64_t *unit_base;  // [n_units]
+    int64_t pc_total, ab_total;
+    int nmax_max;
+    size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
+    // mixed precision (tensor-core) path
+    size_t o_cf, o_eexp, o_eunit, o_bt, o_counter;
+    int n_pad_total;     // angles padded to whole 192-column blocks
+    int k_pad;           // orders padded to 32
+    int *unit_order;     // [n_units] units by decreasing work (plan-owned)
+    GsfTables gsf;
+    int has_gsf;
+};
+
+// ---------------------------------------------------------------------------
+// block reduction of K doubles (all threads receive the totals)
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K])
+{
+    __shared__ double red[32][K];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) red[wid][k] = v[k];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? red[lane][k] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) red[0][k] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = red[0][k];
+    __syncthreads();
+}
+
+struct TabView {
+    int n_lambda, n_rh, n_size, n_bin, n_comp, n_ang, grid_kind, psd_kind, rh0;
+    const double *lambda, *grid, *dgrid, *psd_param, *gf_psd, *frac, *rhop, *rhop0, *gf, *rlow, *rup;
+    const double *theta;
+    const double2 *m;
+    const double *xg;
+    const int64_t *off, *unit_base;
+    double2 *pc, *an, *bn;
+    double *eff4, *W, *sums, *reff0, *pacc, *sraw, *nlraw;
+    const double2 *pq;
+    // PSD weights, their radius moments and reff0 do not depend on the
+    // wavelength when the grid is a radius grid and the PSD is analytic
+    // (x = 2 pi r / lambda: the lognormal argument ln(x / x_mode) and the
+    // r^-4 law are wavelength-free and the 1/x factor cancels in the
+    // normalisation); they are then stored once (lam_shared = 1).
+    int lam_shared;
+    __device__ __forceinline__ int le(int lam) const { return grid_kind == GBMIE_GRID_X ? 0 : lam; }
+    __device__ __forceinline__ int wl(int lam) const { return lam_shared ? 0 : lam; }
+    // offset of wavelength lam's block of W ([rh][bin][comp][size])
+    __device__ __forceinline__ size_t wlam(int lam) const {
+        return (size_t)wl(lam) * n_rh * n_bin * n_comp * n_size;
+    }
+    __device__ __forceinline__ double radius(int lam, int i) const {
+        return grid_kind == GBMIE_GRID_RADIUS ? grid[i] : xg[i] * lambda[lam] / TWO_PI;
+    }
+};
+

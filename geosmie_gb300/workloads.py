@@ -129,6 +129,13 @@ def work_counts(spec):
                 nmx = np.rint(np.maximum(nmi, z) + 16.0)
                 sum_nmax += int(nmi.sum())
                 sum_nmx += int(nmx.sum())
+    # tensor-core tiles: 64 sizes, K padded to 32 orders, per unit
+    sum_ktile = 0
+    for li in range(nl):
+        nmi = nm[le[li]]
+        last = nmi[np.minimum(np.arange(63, grid.size + 63, 64), grid.size - 1)]
+        sum_ktile += int(np.sum((last + 31) // 32 * 32)) * nrh * ncomp
     return {"instances": int(nl * nrh * ncomp * grid.size), "sum_nmax": sum_nmax, "sum_nmx": sum_nmx,
+            "sum_ktile": sum_ktile,
             "rows": int(x.shape[0] * grid.size), "nbin": int(np.asarray(spec["frac"]).shape[0]),
             "nang": int(np.asarray(spec["ang"]).size)}

@@ -111,3 +111,49 @@ def test_gsf_api_gpu():
         ref, rcn = ogsf.expand(ang, F, ng)
         assert np.max(np.abs(got - ref)) < 1e-10, ng
         assert np.max(np.abs(cn - rcn) / rcn) < 1e-12
+
+
+def _mixed_vs_plain(spec, n_gsf):
+    from geosmie_gb300.table import TablePlan
+    plain = TablePlan(spec, precision=0, n_gsf=n_gsf)
+    plain.run()
+    a = plain.results()
+    mixed = TablePlan(spec, precision=1, n_gsf=n_gsf)
+    mixed.run()
+    b = mixed.results()
+    return a, b
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_gsf", [0, 64])
+def test_mixed_precision_within_1e6_gpu(n_gsf):
+    """Tensor-core (split FP16, FP32 accumulation) table vs the FP64 table:
+    phase elements within 1e-6 of P11 at the same angle, the FP64 scalars
+    identical, GSF moments within 1e-6 of the entry's largest alpha1."""
+    spec = synthetic_spec(nl=3, nrh=3, ns=400, nbin=5, nang=181)
+    a, b = _mixed_vs_plain(spec, n_gsf)
+    p11 = np.abs(a["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, k
+    assert np.max(np.abs(b["pback"] - a["pback"]) / np.abs(a["pback"][..., :1])) < 1e-6
+    for k in TIGHT + LOOSE + ["qabs"]:
+        assert np.array_equal(a[k], b[k]), k
+    if n_gsf:
+        scale = np.max(np.abs(a["pmom"][..., 0, :]), axis=-1)[..., None, None]
+        assert np.max(np.abs(b["pmom"] - a["pmom"]) / scale) < 1e-6
+
+
+@pytest.mark.gpu
+def test_mixed_reference_layout_and_many_angles_gpu():
+    """The reference's own layout (one x grid per bin, 371 angles in two
+    column blocks, two-mode bin) through the mixed path, against the
+    reference's table."""
+    from geosmie_gb300 import table
+    g = load_golden("table_lognorm.npz")
+    params = json.loads(str(g["params_json"]))
+    got = table.run_table(params, list(g["mlist"]), g["waterm"], precision=1)
+    p11 = np.abs(g["out_p11"])
+    for k in SCAT:
+        assert np.max(np.abs(got[k] - g["out_" + k]) / p11) < 1e-6, k
+    for k in TIGHT:
+        assert np.max(np.abs(got[k] - g["out_" + k]) / np.abs(g["out_" + k])) < 1e-10, k
