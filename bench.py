@@ -171,6 +171,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced table (quick check, not a bench line)")
+    ap.add_argument("--lambdas", type=int, default=60, help="wavelengths of the table (profiling subsets)")
+    ap.add_argument("--rh", type=int, default=36, help="RH values of the table (profiling subsets)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -189,7 +191,7 @@ def main():
     if args.small:
         spec, desc = workloads.sulfate_table(n_rh=6, n_lambda=10, n_radii=500)
     else:
-        spec, desc = workloads.sulfate_table()
+        spec, desc = workloads.sulfate_table(n_rh=args.rh, n_lambda=args.lambdas)
     counts = workloads.work_counts(spec)
     n_gsf = 64
     peak = _native._D()

@@ -100,9 +100,11 @@ __global__ void __launch_bounds__(256) k_tab_weights(TabView v, const double *__
     }
     const double inv = (v.psd_kind == GBMIE_PSD_WEIGHTS || tot[0] == 0.0) ? 1.0 : 1.0 / tot[0];
     double s[4] = {0.0, 0.0, 0.0, 0.0};
+    float *Wf = v.Wf ? v.Wf + (size_t)blk * n : nullptr;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const double w = W[i] * inv;
         if (v.psd_kind != GBMIE_PSD_WEIGHTS) W[i] = w;
+        if (Wf) Wf[i] = (float)w;
         const double r = v.radius(lam, i);
         const double r2 = r * r * w;
         s[0] += w;
@@ -448,6 +450,7 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.pq = (const double2 *)(scr + p->o_pq);
     v.sraw = (double *)(scr + p->o_sraw);
     v.nlraw = (double *)(scr + p->o_nlraw);
+    v.Wf = p->d.precision == GBMIE_MIXED ? (float *)(scr + p->o_wf) : nullptr;
     return v;
 }
 
@@ -608,6 +611,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
         p->o_bt = carve(mixed ? 4 * 2 * (size_t)p->n_pad_total * p->k_pad : 16);
         p->o_counter = carve(16);
+        p->o_wf = carve(mixed ? sizeof(float) * nW * d.n_size : 16);
         p->o_sraw = carve(sizeof(double) * (size_t)p->n_entries * 10);
         p->o_nlraw = carve(sizeof(double) * (size_t)p->n_entries * 5);
         p->bytes = o;

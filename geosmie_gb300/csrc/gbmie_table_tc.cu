@@ -35,14 +35,60 @@
 // ---------------------------------------------------------------------------
 // FP64 coefficients -> FP32 (c, d) + exponent
 // ---------------------------------------------------------------------------
+// Emits FP32 (c, d) and accumulates the efficiency sums from them: with
+// c = a + b and d = a - b,
+//   Re a + Re b = Re c,   |a|^2 + |b|^2 = (|c|^2 + |d|^2) / 2,
+//   Re(a_n a*_{n+1} + b_n b*_{n+1}) = (Re(c_n c*_{n+1}) + Re(d_n d*_{n+1})) / 2,
+//   Re(a_n b*_n) = (|c|^2 - |d|^2) / 4.
+// qext, qsca and the asymmetry sum are accumulated in FP32 with Kahan
+// compensation (the accumulated rounding then stays at the FP32 unit
+// roundoff whatever nmax is, and the terms do not cancel in the PSD-weighted
+// bulk values); the
+// back-scattering sum sum (2n+1)(-1)^n (a_n - b_n) cancels strongly for
+// large particles and stays FP64 from the FP64 d_n.
+__device__ __forceinline__ void kahan(float &sum, float &comp, float v)
+{
+    const float y = v - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
 struct EmitMixed {
     float4 *cf;
-    double amax;
+    float amax;
+    float ext, sca, asy;
+    float ext_c, sca_c, asy_c;   // Kahan compensations
+    double qbr, qbi;
+    float4 prev;         // (c, d) of order n+1 (zero above nmax)
+    float inv_n1;        // 1/(n+1)
     __device__ __forceinline__ void operator()(int k, cplx a, cplx b) {
-        const cplx c = a + b, d = a - b;
-        cf[k - 1] = make_float4((float)c.re, (float)c.im, (float)d.re, (float)d.im);
-        amax = fmax(amax, fmax(fmax(fabs(c.re), fabs(c.im)), fmax(fabs(d.re), fabs(d.im))));
+        const double dr = a.re - b.re, di = a.im - b.im;
+        const float4 q = make_float4((float)(a.re + b.re), (float)(a.im + b.im), (float)dr, (float)di);
+        cf[k - 1] = q;
+        amax = fmaxf(amax, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
+        const float fk = (float)k;
+        const float cn = 2.f * fk + 1.f;
+        const float inv_n = 1.f / fk;
+        const float c2 = q.x * q.x + q.y * q.y, d2v = q.z * q.z + q.w * q.w;
+        kahan(ext, ext_c, cn * q.x);
+        kahan(sca, sca_c, cn * 0.5f * (c2 + d2v));
+        kahan(asy, asy_c, ((fk + 1.f) - inv_n1) * 0.5f * (q.x * prev.x + q.y * prev.y + q.z * prev.z + q.w * prev.w) +
+                              (inv_n + inv_n1) * 0.25f * (c2 - d2v));
+        const double sg = (k & 1) ? -(2.0 * k + 1.0) : (2.0 * k + 1.0);
+        qbr = fma(sg, dr, qbr);
+        qbi = fma(sg, di, qbi);
+        prev = q;
+        inv_n1 = inv_n;
     }
+};
+
+// The homogeneous recurrences without the FP64 efficiency sums (they are
+// accumulated by EmitMixed): same D_n, psi/chi and a_n/b_n arithmetic as
+// homog_instance.
+struct NoSums {
+    __device__ __forceinline__ void init() {}
+    __device__ __forceinline__ void add_rcp(int, cplx, cplx, double, double) {}
 };
 
 __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
@@ -62,17 +108,25 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_i
     const double x = v.xg[row];
     const cplx m = cx(v.m[unit]);
     if (!isfinite(m.re) || !isfinite(m.im)) atomicOr(flags, GBMIE_FLAG_INVALID);
-    EmitMixed emit{cf + c, 0.0};
-    EffSums es;
-    homog_instance(x, m * m, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
-    double e[6];
-    es.finish(x, e);
+    EmitMixed emit;
+    emit.cf = cf + c;
+    emit.amax = 0.f;
+    emit.ext = emit.sca = emit.asy = 0.f;
+    emit.ext_c = emit.sca_c = emit.asy_c = 0.f;
+    emit.qbr = emit.qbi = 0.0;
+    emit.prev = make_float4(0.f, 0.f, 0.f, 0.f);
+    emit.inv_n1 = 1.f / (float)(nmax + 1);
+    NoSums ns;
+    homog_instance(x, m * m, cx(1.0, 0.0), v.pc + o, nmax, emit, ns);
+    const double y2 = x * x;
+    const double qext = 2.0 * (double)emit.ext / y2;
+    const double qsca = 2.0 * (double)emit.sca / y2;
     double *o4 = v.eff4 + t * 4;
-    o4[0] = e[0];
-    o4[1] = e[1];
-    o4[2] = e[3];
-    o4[3] = e[4];
-    const int ex = emit.amax > 0.0 ? ilogb(emit.amax) : -1000;
+    o4[0] = qext;
+    o4[1] = qsca;
+    o4[2] = (emit.qbr * emit.qbr + emit.qbi * emit.qbi) / y2;
+    o4[3] = 4.0 / y2 * (double)emit.asy / qsca;
+    const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
 }
@@ -149,15 +203,33 @@ struct TcArgs {
 #define TC_B_BYTES (TC_KC * TC_NBLK * 2)               // one B matrix chunk: 12 KB
 #define TC_STAGE_PITCH (TC_INST + 1)                   // padded row: conflict-free reads
 #define TC_STAGE_FLOATS (4 * 64 * TC_STAGE_PITCH)      // Mueller staging [k][col][size]: 65 KB
-#define TC_SMEM_BYTES (4 * TC_A_BYTES + 4 * TC_B_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
+#define TC_SMEM_BYTES (4 * TC_A_BYTES + 8 * TC_B_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
+
+// One K chunk (TC_KC orders from k0) of angle block blk of the four B
+// matrices into shared memory, [m][kg][ng][8][16 B]; plain 16-byte loads.
+__device__ __forceinline__ void copy_b_chunk(const TcArgs &g, uint8_t *dstbase, int k0, int blk, int tid)
+{
+    const int nkg = TC_KC / 8, nng = TC_NBLK / 8, ngt = g.n_pad / 8;
+    const size_t mat = (size_t)g.n_pad * g.k_pad;
+    for (int idx = tid; idx < 4 * nkg * nng * 8; idx += TC_THREADS) {
+        const int rr = idx & 7;
+        const int ng = (idx >> 3) % nng;
+        const int kg = ((idx >> 3) / nng) % nkg;
+        const int m = (idx >> 3) / (nng * nkg);
+        const size_t src = m * mat + (((size_t)(k0 / 8 + kg) * ngt + blk * nng + ng) * 64 + rr * 8);
+        const uint32_t dst = m * TC_B_BYTES + (kg * nng + ng) * 128 + rr * 16;
+        *(uint4 *)(dstbase + dst) = *(const uint4 *)(g.bt + src);
+    }
+}
 
 template <int NB>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sA = smem;                                     // 4 x TC_A_BYTES
-    uint8_t *sB = sA + 4 * TC_A_BYTES;                      // 4 x TC_B_BYTES
-    float *stage = (float *)(sB + 4 * TC_B_BYTES);          // [4][64][65]
+    uint8_t *sB0 = sA + 4 * TC_A_BYTES;                     // chunk 0 of the angle block, resident
+    uint8_t *sB1 = sB0 + 4 * TC_B_BYTES;                    // later chunks
+    float *stage = (float *)(sB1 + 4 * TC_B_BYTES);         // [4][64][65]
     float *sw = stage + TC_STAGE_FLOATS;                    // [NB][64]
     uint64_t *bar = (uint64_t *)(sw + 8 * TC_INST);
     uint32_t *s_tmem = (uint32_t *)(bar + 1);
@@ -166,6 +238,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
 
     const TabView &v = g.v;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int s_blk_loaded = -1;   // angle block whose chunk 0 sits in sB0 (same value in every thread)
     if (warp == 0) tmem_alloc(s_tmem, 512);
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -198,14 +271,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         const int *ex = g.eexp + unit * v.n_size;
         const int E = g.eunit[unit];
         const int rhi = (int)(lr % v.n_rh);
-        const double *Wb = v.W + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
+        const float *Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
 
         for (int blk = 0; blk < nblocks; ++blk) {
-            double uacc[TC_ROUNDS][NB];
+            // per-unit sums as unevaluated FP32 pairs (hi + lo, two-sum)
+            float uh[TC_ROUNDS][NB], ul[TC_ROUNDS][NB];
 #pragma unroll
             for (int r = 0; r < TC_ROUNDS; ++r)
 #pragma unroll
-                for (int b = 0; b < NB; ++b) uacc[r][b] = 0.0;
+                for (int b = 0; b < NB; ++b) uh[r][b] = ul[r][b] = 0.f;
+            if (blk != s_blk_loaded) {   // uniform: chunk 0 of this angle block into sB0
+                copy_b_chunk(g, sB0, 0, blk, tid);
+                s_blk_loaded = blk;
+            }
 
             for (int t0 = 0; t0 < v.n_size; t0 += TC_INST) {
                 const int ntile = min(TC_INST, v.n_size - t0);
@@ -215,10 +293,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 for (int idx = tid; idx < NB * TC_INST; idx += TC_THREADS) {
                     const int b = idx / TC_INST, i = idx % TC_INST;
                     float w = 0.f;
-                    if (i < ntile && b < v.n_bin) {
-                        const double wd = Wb[(size_t)b * v.n_comp * v.n_size + t0 + i];
-                        w = (float)ldexp(wd, 2 * (ex[t0 + i] - E));
-                    }
+                    if (i < ntile && b < v.n_bin)
+                        w = ldexpf(Wb[(size_t)b * v.n_comp * v.n_size + t0 + i], max(-300, 2 * (ex[t0 + i] - E)));
                     sw[b * TC_INST + i] = w;
                 }
                 // A-row data of this thread: size i = tid / 4, orders 8 (tid % 4) .. + 8 of each chunk
@@ -256,21 +332,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         *(uint4 *)(sA + 3 * TC_A_BYTES + o0) = *(uint4 *)cl[2];
                         *(uint4 *)(sA + 3 * TC_A_BYTES + o1) = *(uint4 *)cl[3];
                     }
-                    // ---- B: chunk of the angle block from the precomputed tables
-                    {
-                        const int nkg = TC_KC / 8, nng = TC_NBLK / 8, ngt = g.n_pad / 8;
-                        const size_t mat = (size_t)g.n_pad * g.k_pad;
-                        for (int idx = tid; idx < 4 * nkg * nng * 8; idx += TC_THREADS) {
-                            // 16-byte pieces: matrix m, kg, ng, row-in-core
-                            const int rr = idx & 7;
-                            const int ng = (idx >> 3) % nng;
-                            const int kg = ((idx >> 3) / nng) % nkg;
-                            const int m = (idx >> 3) / (nng * nkg);
-                            const size_t src = m * mat + (((size_t)(k0 / 8 + kg) * ngt + blk * nng + ng) * 64 + rr * 8);
-                            const uint32_t dst = m * TC_B_BYTES + (kg * nng + ng) * 128 + rr * 16;
-                            *(uint4 *)(sB + dst) = *(const uint4 *)(g.bt + src);
-                        }
-                    }
+                    // ---- B: chunk 0 is resident; later chunks go to sB1
+                    if (k0 > 0) copy_b_chunk(g, sB1, k0, blk, tid);
+                    uint8_t *sB = k0 > 0 ? sB1 : sB0;
                     fence_proxy_async_smem();
                     __syncthreads();
                     if (tid == 0) {
@@ -348,7 +412,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                             for (int b = 0; b < NB; ++b) acc[b] = fmaf(sw[b * TC_INST + i], s, acc[b]);
                         }
 #pragma unroll
-                        for (int b = 0; b < NB; ++b) uacc[r][b] += (double)acc[b];
+                        for (int b = 0; b < NB; ++b) {   // two-sum: (uh + ul) += acc exactly-rounded
+                            const float sum = uh[r][b] + acc[b];
+                            const float bp = sum - uh[r][b];
+                            ul[r][b] += (uh[r][b] - (sum - bp)) + (acc[b] - bp);
+                            uh[r][b] = sum;
+                        }
                     }
                     __syncthreads();
                 }
@@ -367,7 +436,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                             if (b < v.n_bin) {
                                 const double f = v.frac[(size_t)b * v.n_comp + comp];
                                 atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
-                                          f * uacc[r][b] * f2);
+                                          f * ((double)uh[r][b] + (double)ul[r][b]) * f2);
                             }
                         }
                     }
@@ -423,19 +492,17 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     const size_t smem = TC_SMEM_BYTES;
     cudaError_t e = cudaSuccess;
     ctx_pre_launch(ctx);
-    if (d.n_bin <= 1) {
-        e = cudaFuncSetAttribute(k_tab_s12_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tab_s12_tc<1><<<grid, TC_THREADS, smem, st>>>(a);
-    } else if (d.n_bin <= 2) {
-        e = cudaFuncSetAttribute(k_tab_s12_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tab_s12_tc<2><<<grid, TC_THREADS, smem, st>>>(a);
-    } else if (d.n_bin <= 4) {
-        e = cudaFuncSetAttribute(k_tab_s12_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tab_s12_tc<4><<<grid, TC_THREADS, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(k_tab_s12_tc<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tab_s12_tc<8><<<grid, TC_THREADS, smem, st>>>(a);
+#define TC_LAUNCH(NBV)                                                                                   \
+    case NBV:                                                                                            \
+        e = cudaFuncSetAttribute(k_tab_s12_tc<NBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        k_tab_s12_tc<NBV><<<grid, TC_THREADS, smem, st>>>(a);                                            \
+        break;
+    switch (d.n_bin) {
+        TC_LAUNCH(1) TC_LAUNCH(2) TC_LAUNCH(3) TC_LAUNCH(4) TC_LAUNCH(5) TC_LAUNCH(6) TC_LAUNCH(7)
+        default:
+        TC_LAUNCH(8)
     }
+#undef TC_LAUNCH
     GBMIE_TRY(ctx_cuda(ctx, e, "k_tab_s12_tc smem attribute"));
     return ctx_check_launch(ctx, "k_tab_s12_tc");
 }

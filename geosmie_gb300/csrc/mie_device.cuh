@@ -116,6 +116,20 @@ struct EffSums {
         a1 = a;
         b1 = b;
     }
+    // the same with the reciprocals 1/n and 1/(n+1) supplied:
+    // n (n+2)/(n+1) = (n+1) - 1/(n+1) and (2n+1)/(n (n+1)) = 1/n + 1/(n+1)
+    __device__ __forceinline__ void add_rcp(int n, cplx a, cplx b, double inv_n, double inv_n1) {
+        const double dn = (double)n;
+        const double cn = 2.0 * dn + 1.0;
+        ext += cn * (a.re + b.re);
+        sca += cn * (abs2(a) + abs2(b));
+        const double sg = (n & 1) ? -cn : cn;
+        qb = qb + (a - b) * sg;
+        asy += ((dn + 1.0) - inv_n1) * (a.re * a1.re + a.im * a1.im + b.re * b1.re + b.im * b1.im)
+             + (inv_n + inv_n1) * (a.re * b.re + a.im * b.im);
+        a1 = a;
+        b1 = b;
+    }
     // qext, qsca, qabs, qb, asy, qratio for outer size y
     __device__ __forceinline__ void finish(double y, double *e) const {
         const double y2 = y * y;
@@ -150,18 +164,29 @@ __device__ __forceinline__ cplx mie_ratio(cplx d, double psin, double chin, doub
 // row1: psi/chi of x for orders 1..nmax at row1[n-1]; it may alias the
 // emitter's a_n output (row n is consumed before a_n is written).
 // ---------------------------------------------------------------------------
-template <class Emit>
+template <class Emit, class Sums>
 __device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, const double2 *row1,
-                                               int nmax, Emit &emit, EffSums &es)
+                                               int nmax, Emit &emit, Sums &es)
 {
     const cplx z = csqrt(eps * mu) * x;
     const cplx m = csqrt(eps / mu);
-    const int nmx = (int)rint(fmax((double)nmax, cabs(z)) + 16.0);
+    const double az = cabs(z);
+    const int nmx = (int)rint(fmax((double)nmax, az) + 16.0);
     const cplx zinv = cinv(z);
     const cplx minv = cinv(m);
     const double xinv = 1.0 / x;
+    // Warm-up steps above nmax.  The reference runs nmx - 1 - nmax of them
+    // from D = 0.  For n > |z| the recurrence damps the start error by
+    // (|z| / (2n+1))^2 per step, so when |z| < (nmax+1)/2 fewer steps reach
+    // the same converged D_nmax (damping below 1e-17, plus two spare steps).
+    int warm = nmx - 1 - nmax;
+    if (az < 0.5 * (nmax + 1)) {
+        const double q = 2.0 * log((2.0 * (nmax + 1) + 1.0) / az);   // -ln(damping) per step
+        const int need = (int)ceil(39.2 / q) + 2;
+        if (need < warm) warm = need;
+    }
     cplx D = cx(0.0, 0.0);
-    for (int k = nmx - 1; k > nmax; --k) {
+    for (int k = nmax + warm; k > nmax; --k) {
         const cplx r = zinv * (double)(k + 1);
         D = r - cinv(D + r);
     }
@@ -169,15 +194,40 @@ __device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, cons
     sincos(x, &sx, &cxv);
     double2 pcn = row1[nmax - 1];
     es.init();
+    // One reciprocal per order: at order k the denominators of a_k, b_k and
+    // of the next D step (D_k + r_{k-1}) and k itself are inverted together,
+    // 1/(A B C k), and the four reciprocals recovered by multiplication.
+    cplx w = D + zinv * (double)(nmax + 1);            // D_{nmax+1} + r_nmax
+    double inv_w2 = 1.0 / abs2(w);                    // 1/|w|^2 for D_nmax
+    double inv_n1 = 1.0 / (double)(nmax + 1);          // 1/(k+1)
     for (int k = nmax; k >= 1; --k) {
         const cplx r = zinv * (double)(k + 1);
-        D = r - cinv(D + r);
+        D = r - cx(w.re * inv_w2, -w.im * inv_w2);      // D_k
         const double2 pcm = (k > 1) ? row1[k - 2] : make_double2(sx, cxv);
         const double nx = (double)k * xinv;
-        const cplx a = mie_ratio(D * minv + nx, pcn.x, pcn.y, pcm.x, pcm.y);
-        const cplx b = mie_ratio(D * m + nx, pcn.x, pcn.y, pcm.x, pcm.y);
+        const cplx da = D * minv + nx;
+        const cplx db = D * m + nx;
+        const cplx Na = cx(da.re * pcn.x - pcm.x, da.im * pcn.x);
+        const cplx Ma = cx(da.re * pcn.y - pcm.y, da.im * pcn.y);
+        const cplx Nb = cx(db.re * pcn.x - pcm.x, db.im * pcn.x);
+        const cplx Mb = cx(db.re * pcn.y - pcm.y, db.im * pcn.y);
+        const cplx qa = cx(Na.re + Ma.im, Na.im - Ma.re);   // N - i M
+        const cplx qbv = cx(Nb.re + Mb.im, Nb.im - Mb.re);
+        const double A = abs2(qa), B = abs2(qbv);
+        w = D + zinv * (double)k;                          // D_k + r_{k-1}
+        const double C = (k > 1) ? abs2(w) : 1.0;
+        const double AB = A * B, ABC = AB * C;
+        const double inv = 1.0 / (ABC * (double)k);
+        const double inv_n = ABC * inv;                    // 1/k
+        const double t = (double)k * inv;                  // 1/(A B C)
+        inv_w2 = AB * t;                                   // 1/C
+        const double u = C * t;                            // 1/(A B)
+        const double ia = B * u, ib = A * u;               // 1/A, 1/B
+        const cplx a = cx((Na.re * qa.re + Na.im * qa.im) * ia, (Na.im * qa.re - Na.re * qa.im) * ia);
+        const cplx b = cx((Nb.re * qbv.re + Nb.im * qbv.im) * ib, (Nb.im * qbv.re - Nb.re * qbv.im) * ib);
         emit(k, a, b);
-        es.add(k, a, b);
+        es.add_rcp(k, a, b, inv_n, inv_n1);
+        inv_n1 = inv_n;
         pcn = pcm;
     }
 }

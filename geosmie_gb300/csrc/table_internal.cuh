@@ -19,7 +19,7 @@ struct gbmie_table_plan {
     int nmax_max;
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
     // mixed precision (tensor-core) path
-    size_t o_cf, o_eexp, o_eunit, o_bt, o_counter;
+    size_t o_cf, o_eexp, o_eunit, o_bt, o_counter, o_wf;
     int n_pad_total;     // angles padded to whole 192-column blocks
     int k_pad;           // orders padded to 32
     int *unit_order;     // [n_units] units by decreasing work (plan-owned)
@@ -66,6 +66,7 @@ struct TabView {
     const int64_t *off, *unit_base;
     double2 *pc, *an, *bn;
     double *eff4, *W, *sums, *reff0, *pacc, *sraw, *nlraw;
+    float *Wf;   // FP32 copy of W (mixed path), or NULL
     const double2 *pq;
     // PSD weights, their radius moments and reff0 do not depend on the
     // wavelength when the grid is a radius grid and the PSD is analytic

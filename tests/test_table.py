@@ -128,16 +128,19 @@ def _mixed_vs_plain(spec, n_gsf):
 @pytest.mark.parametrize("n_gsf", [0, 64])
 def test_mixed_precision_within_1e6_gpu(n_gsf):
     """Tensor-core (split FP16, FP32 accumulation) table vs the FP64 table:
-    phase elements within 1e-6 of P11 at the same angle, the FP64 scalars
-    identical, GSF moments within 1e-6 of the entry's largest alpha1."""
+    phase elements within 1e-6 of P11 at the same angle, bulk scalars within
+    1e-6 relative (qabs: 1e-6 of qext), GSF moments within 1e-6 of the
+    entry's largest alpha1."""
     spec = synthetic_spec(nl=3, nrh=3, ns=400, nbin=5, nang=181)
     a, b = _mixed_vs_plain(spec, n_gsf)
     p11 = np.abs(a["p11"])
     for k in SCAT:
         assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, k
     assert np.max(np.abs(b["pback"] - a["pback"]) / np.abs(a["pback"][..., :1])) < 1e-6
-    for k in TIGHT + LOOSE + ["qabs"]:
-        assert np.array_equal(a[k], b[k]), k
+    # efficiencies of the mixed path: qb in FP64, qext/qsca/g sums in FP32
+    for k in TIGHT + LOOSE:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, k
+    assert np.max(np.abs(b["qabs"] - a["qabs"]) / np.abs(a["qext"])) < 1e-6
     if n_gsf:
         scale = np.max(np.abs(a["pmom"][..., 0, :]), axis=-1)[..., None, None]
         assert np.max(np.abs(b["pmom"] - a["pmom"]) / scale) < 1e-6
@@ -156,4 +159,4 @@ def test_mixed_reference_layout_and_many_angles_gpu():
     for k in SCAT:
         assert np.max(np.abs(got[k] - g["out_" + k]) / p11) < 1e-6, k
     for k in TIGHT:
-        assert np.max(np.abs(got[k] - g["out_" + k]) / np.abs(g["out_" + k])) < 1e-10, k
+        assert np.max(np.abs(got[k] - g["out_" + k]) / np.abs(g["out_" + k])) < 1e-6, k
