@@ -43,12 +43,29 @@ __global__ void k_tab_make_x(int n_le, int n_size, int grid_kind, const double *
 // run kernels
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_tab_psi_chi(int64_t nrows, const double *__restrict__ xg,
-                                                     const int64_t *__restrict__ off, double2 *__restrict__ pc)
+                                                     const int64_t *__restrict__ off, double2 *__restrict__ pc,
+                                                     double4 *__restrict__ rowc)
 {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nrows) return;
     const int64_t o = off[j];
-    psi_chi_row(xg[j], (int)(off[j + 1] - o), pc + o);
+    const double x = xg[j];
+    psi_chi_row(x, (int)(off[j + 1] - o), pc + o);
+    double s, c;
+    sincos(x, &s, &c);
+    rowc[j] = make_double4(s, c, 1.0 / x, 0.0);
+}
+
+// Medium constants per (lam, rh, comp) unit (eps = m^2, mu = 1 as the
+// reference's Mie(m=...) sets them); a non-finite index raises the invalid flag.
+__global__ void k_tab_index(int64_t n_units, const double2 *__restrict__ m, HomogIndex *__restrict__ hidx,
+                            int *flags)
+{
+    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= n_units) return;
+    const cplx mu = cx(m[u]);
+    if (!isfinite(mu.re) || !isfinite(mu.im)) atomicOr(flags, GBMIE_FLAG_INVALID);
+    hidx[u] = homog_index(mu * mu, cx(1.0, 0.0));
 }
 
 // PSD weights of (lam, rh, bin, comp): lognormal dN/dx x dgrid or r^-4 x
@@ -145,11 +162,11 @@ __global__ void __launch_bounds__(128) k_tab_coeffs(TabView v, int64_t n_inst, i
     const int nmax = (int)(v.off[row + 1] - o);
     const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
     const double x = v.xg[row];
-    const cplx m = cx(v.m[unit]);
-    if (!isfinite(m.re) || !isfinite(m.im)) atomicOr(flags, GBMIE_FLAG_INVALID);
+    const double4 rc = v.rowc[row];
+    const HomogIndex h = v.hidx[unit];
     EmitTab emit{v.an + c, v.bn + c};
     EffSums es;
-    homog_instance(x, m * m, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
+    homog_core(x, rc.z, rc.x, rc.y, h, v.pc + o, nmax, emit, es);
     double e[6];
     es.finish(x, e);
     double *o4 = v.eff4 + t * 4;
@@ -261,47 +278,93 @@ __global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int
 }
 
 // Scalar integration of integratePSD ('dumix', dointegration.py:1064-1209),
-// one block per (lam, rh, bin).  sraw: qext qsca qabs qb g csca cext bsca
+// one block per (lam, rh) covering every bin: the per-size features
+//   A, qext A, qsca A, qabs A, qb A, g A qsca, csca A qsca, cext A qsca, A qsca
+// (the weight becomes A qsca from 'g' on, the reference's aliasing) are
+// formed once and weighted with each bin's PSD.  Plain: FP64 sums.  Mixed:
+// FP32 with Kahan compensation.  sraw: qext qsca qabs qb g csca cext bsca
 // bext bbck; nlraw: mass volume area rEff rMass (before division by mass0).
+template <typename T>
+struct KSum {
+    T s, c;
+    __device__ __forceinline__ void zero() { s = c = (T)0; }
+    __device__ __forceinline__ void add(T v) {
+        if (sizeof(T) == 8) {
+            s += v;
+        } else {   // Kahan
+            const T y = v - c;
+            const T t = s + y;
+            c = (t - s) - y;
+            s = t;
+        }
+    }
+    __device__ __forceinline__ double val() const { return (double)s - (double)c; }
+};
+
+template <int NB, typename T>
 __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
 {
-    const int blk = blockIdx.x;   // (lam * n_rh + rh) * n_bin + bin
-    const int bin = blk % v.n_bin;
-    const int64_t lr = blk / v.n_bin;
+    __shared__ double sR[NB][15];
+    __shared__ double sRed[8][NB * 9];
+    __shared__ double sS[NB * 9];
+    const int64_t lr = blockIdx.x;   // lam * n_rh + rh
     const int rh = (int)(lr % v.n_rh), lam = (int)(lr / v.n_rh);
-    const double rhop = v.rhop[(size_t)bin * v.n_rh + rh];
-    const double rhop0 = v.rhop0[bin];
-    double R[15];
-#pragma unroll
-    for (int k = 0; k < 15; ++k) R[k] = 0.0;   // frac-weighted accumulated results
+    if (threadIdx.x < NB * 15) sR[threadIdx.x / 15][threadIdx.x % 15] = 0.0;
+    // radii are scaled by a power of two that brings the largest to [1, 2):
+    // exact, and A^2 qsca of nanometre particles stays inside the FP32 range
+    const double rscale = ldexp(1.0, -ilogb(v.radius(lam, v.n_size - 1)));
+    const double ascale = ldexp(1.0, 2 * ilogb(v.radius(lam, v.n_size - 1)));   // 1 / rscale^2
     for (int comp = 0; comp < v.n_comp; ++comp) {
         const int64_t unit = lr * v.n_comp + comp;
-        const double *W = v.W + v.wlam(lam) + (((size_t)rh * v.n_bin + bin) * v.n_comp + comp) * v.n_size;
         const double *E = v.eff4 + (size_t)unit * v.n_size * 4;
-        double s[9];
+        KSum<T> acc[NB][9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) s[k] = 0.0;
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int j = 0; j < 9; ++j) acc[b][j].zero();
         for (int i = threadIdx.x; i < v.n_size; i += blockDim.x) {
-            const double w = W[i];
-            const double r = v.radius(lam, i);
-            const double A = PI_D * r * r;
-            const double qext = E[4 * i], qsca = E[4 * i + 1], qb = E[4 * i + 2], g = E[4 * i + 3];
-            const double wa = w * A, was = wa * qsca;
-            s[0] += wa;                     // sum w A
-            s[1] += qext * wa;
-            s[2] += qsca * wa;
-            s[3] += (qext - qsca) * wa;
-            s[4] += qb * wa;
-            s[5] += g * was;                // weights aliased to A qsca from 'g' on
-            s[6] += qsca * A * was;         // csca_i = qsca_i pi r^2
-            s[7] += qext * A * was;         // cext_i = qext_i pi r^2
-            s[8] += was;
+            const T r = (T)(v.radius(lam, i) * rscale);
+            const T A = (T)PI_D * r * r;
+            const T qext = (T)E[4 * i], qsca = (T)E[4 * i + 1], qb = (T)E[4 * i + 2], g = (T)E[4 * i + 3];
+            const T qabs = (T)(E[4 * i] - E[4 * i + 1]);
+            const T as = A * qsca;
+            const T f[9] = {A, qext * A, qsca * A, qabs * A, qb * A, g * as, qsca * A * as, qext * A * as, as};
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                if (b < v.n_bin) {
+                    const size_t wi = v.wlam(lam) + (((size_t)rh * v.n_bin + b) * v.n_comp + comp) * v.n_size + i;
+                    const T w = sizeof(T) == 8 ? (T)v.W[wi] : (T)v.Wf[wi];
+#pragma unroll
+                    for (int j = 0; j < 9; ++j) acc[b][j].add(w * f[j]);
+                }
+            }
         }
-        block_sum<9>(s);
-        if (threadIdx.x == 0) {
-            const double *m4 = v.sums + ((((size_t)v.wl(lam) * v.n_rh + rh) * v.n_bin + bin) * v.n_comp + comp) * 4;
+        // block reduction of the NB x 9 sums: warp shuffles, then one thread
+        // per sum over the warps
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                double t = acc[b][j].val();
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                if ((threadIdx.x & 31) == 0) sRed[threadIdx.x >> 5][b * 9 + j] = t;
+            }
+        __syncthreads();
+        if (threadIdx.x < NB * 9) {
+            double t = 0.0;
+            for (int wq = 0; wq < (int)(blockDim.x >> 5); ++wq) t += sRed[wq][threadIdx.x];
+            sS[threadIdx.x] = t;
+        }
+        __syncthreads();
+        // one thread per bin: bulk values of (bin, comp), weighted by frac
+        const int b = threadIdx.x;
+        if (b < v.n_bin && b < NB) {
+            const double *s = sS + b * 9;
+            const double rhop = v.rhop[(size_t)b * v.n_rh + rh];
+            const double rhop0 = v.rhop0[b];
+            const double *m4 = v.sums + ((((size_t)v.wl(lam) * v.n_rh + rh) * v.n_bin + b) * v.n_comp + comp) * 4;
             const double num = m4[0], s2 = m4[1], s3 = m4[2], s4 = m4[3];
-            const double reff0 = v.reff0[((size_t)v.wl(lam) * v.n_bin + bin) * v.n_comp + comp];
+            const double reff0 = v.reff0[((size_t)v.wl(lam) * v.n_bin + b) * v.n_comp + comp];
             const double area = PI_D * s2 / num;
             const double volume = 4.0 / 3.0 * PI_D * s3 / num;
             const double mass = volume * rhop;
@@ -309,23 +372,35 @@ __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
             const double reffm = s4 / s3;
             const double rmass = 4.0 / 3.0 * PI_D * rhop * reffm * reffm * reffm;
             const double rmass0 = 4.0 / 3.0 * PI_D * rhop0 * reff0 * reff0 * reff0;
-            const double qext = s[1] / s[0], qsca = s[2] / s[0], qabs = s[3] / s[0];
-            const double qb = s[4] / s[2] * qsca;   // p11back qsca / (4 pi)
-            const double g = s[5] / s[8], csca = s[6] / s[8], cext = s[7] / s[8];
-            const double conv = 1.0 / rhop / reff * rmass / rmass0;
-            const double f = v.frac[(size_t)bin * v.n_comp + comp];
-            const double vals[15] = {qext, qsca, qabs, qb, g, csca, cext, 0.75 * qsca * conv, 0.75 * qext * conv,
-                                     0.75 * qb * conv / (4.0 * PI_D), mass, volume, area, reff, rmass};
+            const double i0 = 1.0 / s[0], i8 = 1.0 / s[8];
+            const double qext = s[1] * i0, qsca = s[2] * i0, qabs = s[3] * i0;
+            const double qbv = s[4] / s[2] * qsca;   // p11back qsca / (4 pi)
+            const double g = s[5] * i8, csca = s[6] * i8 * ascale, cext = s[7] * i8 * ascale;
+            const double conv = rmass / (rhop * reff * rmass0);
+            const double f = v.frac[(size_t)b * v.n_comp + comp];
+            const double vals[15] = {qext, qsca, qabs, qbv, g, csca, cext, 0.75 * qsca * conv, 0.75 * qext * conv,
+                                     0.75 * qbv * conv / (4.0 * PI_D), mass, volume, area, reff, rmass};
 #pragma unroll
-            for (int k = 0; k < 15; ++k) R[k] += f * vals[k];
+            for (int k = 0; k < 15; ++k) sR[b][k] += f * vals[k];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        double *so = v.sraw + (size_t)blk * 10;
-        for (int k = 0; k < 10; ++k) so[k] = R[k];
-        double *no = v.nlraw + (size_t)blk * 5;
-        for (int k = 0; k < 5; ++k) no[k] = R[10 + k];
+    __syncthreads();
+    for (int t = threadIdx.x; t < v.n_bin * 15 && t < NB * 15; t += blockDim.x) {
+        const int b = t / 15, k = t % 15;
+        const size_t e = (size_t)lr * v.n_bin + b;
+        if (k < 10) v.sraw[e * 10 + k] = sR[b][k];
+        else v.nlraw[e * 5 + (k - 10)] = sR[b][k];
+    }
+}
+
+// trapz weights of the angle grid: sum_a f_a tw_a = trapz(f sin(theta), theta)
+__global__ void k_tab_trapz(int nang, const double *__restrict__ theta, double *__restrict__ tw)
+{
+    for (int a = threadIdx.x; a < nang; a += blockDim.x) {
+        const double left = a > 0 ? theta[a] - theta[a - 1] : 0.0;
+        const double right = a < nang - 1 ? theta[a + 1] - theta[a] : 0.0;
+        tw[a] = 0.5 * (left + right) * sin(theta[a]);
     }
 }
 
@@ -338,20 +413,18 @@ __global__ void __launch_bounds__(256) k_tab_finalize(TabView v, gbmie_table_out
     const int rh = (int)(lr % v.n_rh), lam = (int)(lr / v.n_rh);
     const int nang = v.n_ang;
     const double *P = v.pacc + (size_t)blk * 4 * nang;
-    // trapz(p11 sin(theta), theta)
+    // trapz(p11 sin(theta), theta) with the precomputed weights
     double tr[1] = {0.0};
-    for (int a = threadIdx.x; a < nang - 1; a += blockDim.x) {
-        const double t0 = v.theta[a], t1 = v.theta[a + 1];
-        tr[0] += (t1 - t0) * (P[a] * sin(t0) + P[a + 1] * sin(t1)) * 0.5;
-    }
+    for (int a = threadIdx.x; a < nang; a += blockDim.x) tr[0] += P[a] * v.tw[a];
     block_sum<1>(tr);
+    const double scale = 2.0 / tr[0];   // p11n / p11, the same at every angle
     const size_t e = ((size_t)bin * v.n_lambda + lam) * v.n_rh + rh;   // output entry
     double *ph = out.phase + e * 6 * nang;
     for (int a = threadIdx.x; a < nang; a += blockDim.x) {
         const double p11 = P[a], p12 = P[nang + a], p33 = P[2 * nang + a], p34 = P[3 * nang + a];
-        const double p11n = 2.0 * p11 / tr[0];
-        const double p12n = p12 * p11n / p11, p22n = p11 * p11n / p11;
-        const double p33n = p33 * p11n / p11, p34n = p34 * p11n / p11;
+        const double p11n = p11 * scale;
+        const double p12n = p12 * scale, p22n = p11n;
+        const double p33n = p33 * scale, p34n = p34 * scale;
         ph[a] = p11n;
         ph[nang + a] = p12n;
         ph[2 * nang + a] = p22n;
@@ -451,6 +524,9 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.sraw = (double *)(scr + p->o_sraw);
     v.nlraw = (double *)(scr + p->o_nlraw);
     v.Wf = p->d.precision == GBMIE_MIXED ? (float *)(scr + p->o_wf) : nullptr;
+    v.tw = (double *)(scr + p->o_tw);
+    v.rowc = (double4 *)(scr + p->o_rowc);
+    v.hidx = (HomogIndex *)(scr + p->o_hidx);
     return v;
 }
 
@@ -612,6 +688,9 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_bt = carve(mixed ? 4 * 2 * (size_t)p->n_pad_total * p->k_pad : 16);
         p->o_counter = carve(16);
         p->o_wf = carve(mixed ? sizeof(float) * nW * d.n_size : 16);
+        p->o_tw = carve(sizeof(double) * d.n_ang);
+        p->o_rowc = carve(sizeof(double4) * (size_t)p->n_le * d.n_size);
+        p->o_hidx = carve(sizeof(HomogIndex) * (size_t)p->n_units);
         p->o_sraw = carve(sizeof(double) * (size_t)p->n_entries * 10);
         p->o_nlraw = carve(sizeof(double) * (size_t)p->n_entries * 5);
         p->bytes = o;
@@ -637,16 +716,31 @@ static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, co
 {
     const gbmie_table_desc &d = p->d;
     cudaStream_t st = ctx->stream;
+    const unsigned nlr = (unsigned)((int64_t)d.n_lambda * d.n_rh);
+    const bool mixed = d.precision == GBMIE_MIXED;
     ctx_pre_launch(ctx);
-    k_tab_scalars<<<(unsigned)p->n_entries, 256, 0, st>>>(v);
+#define SC_LAUNCH(NBV)                                                                 \
+    case NBV:                                                                          \
+        if (mixed) k_tab_scalars<NBV, float><<<nlr, 256, 0, st>>>(v);                  \
+        else k_tab_scalars<NBV, double><<<nlr, 256, 0, st>>>(v);                       \
+        break;
+    switch (d.n_bin) {
+        SC_LAUNCH(1) SC_LAUNCH(2) SC_LAUNCH(3) SC_LAUNCH(4) SC_LAUNCH(5) SC_LAUNCH(6) SC_LAUNCH(7)
+        default:
+        SC_LAUNCH(8)
+    }
+#undef SC_LAUNCH
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_scalars"));
+    ctx_pre_launch(ctx);
+    k_tab_trapz<<<1, 256, 0, st>>>(d.n_ang, d.theta, v.tw);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_trapz"));
     ctx_pre_launch(ctx);
     k_tab_finalize<<<(unsigned)p->n_entries, 256, 0, st>>>(v, *out);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
     if (p->has_gsf) {
         GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
         GBMIE_TRY(launch_gsf_expand(ctx, &p->gsf, (int)p->n_entries, out->phase, (int64_t)6 * d.n_ang, d.n_ang, map,
-                                    out->pmom, (int64_t)6 * d.n_gsf, d.n_gsf, nullptr));
+                                    out->pmom, (int64_t)6 * d.n_gsf, d.n_gsf, nullptr, d.precision));
     }
     return GBMIE_OK;
 }
@@ -667,8 +761,11 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     cudaStream_t st = ctx->stream;
     const int64_t nrows = (int64_t)p->n_le * d.n_size;
     ctx_pre_launch(ctx);
-    k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc);
+    k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc, v.rowc);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_psi_chi"));
+    ctx_pre_launch(ctx);
+    k_tab_index<<<(unsigned)ceil_div64(p->n_units, 128), 128, 0, st>>>(p->n_units, v.m, v.hidx, ctx->d_flags);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_index"));
     const int64_t nW = (int64_t)(v.lam_shared ? 1 : d.n_lambda) * d.n_rh * d.n_bin * d.n_comp;
     ctx_pre_launch(ctx);
     k_tab_weights<<<(unsigned)nW, 256, 0, st>>>(v, d.weights);

@@ -39,7 +39,8 @@
 // c = a + b and d = a - b,
 //   Re a + Re b = Re c,   |a|^2 + |b|^2 = (|c|^2 + |d|^2) / 2,
 //   Re(a_n a*_{n+1} + b_n b*_{n+1}) = (Re(c_n c*_{n+1}) + Re(d_n d*_{n+1})) / 2,
-//   Re(a_n b*_n) = (|c|^2 - |d|^2) / 4.
+// while Re(a_n b*_n) is formed from the FP64 a_n, b_n ((|c|^2 - |d|^2) / 4
+// would cancel for small particles, where |a_1| >> |b_1|).
 // qext, qsca and the asymmetry sum are accumulated in FP32 with Kahan
 // compensation (the accumulated rounding then stays at the FP32 unit
 // roundoff whatever nmax is, and the terms do not cancel in the PSD-weighted
@@ -73,9 +74,11 @@ struct EmitMixed {
         const float c2 = q.x * q.x + q.y * q.y, d2v = q.z * q.z + q.w * q.w;
         kahan(ext, ext_c, cn * q.x);
         kahan(sca, sca_c, cn * 0.5f * (c2 + d2v));
+        // Re(a b*) from FP64 a, b: (|c|^2 - |d|^2) / 4 cancels when |a| >> |b|
+        const float rab = (float)fma(a.re, b.re, a.im * b.im);
         kahan(asy, asy_c, ((fk + 1.f) - inv_n1) * 0.5f * (q.x * prev.x + q.y * prev.y + q.z * prev.z + q.w * prev.w) +
-                              (inv_n + inv_n1) * 0.25f * (c2 - d2v));
-        const double sg = (k & 1) ? -(2.0 * k + 1.0) : (2.0 * k + 1.0);
+                              (inv_n + inv_n1) * rab);
+        const double sg = (double)((k & 1) ? -(2 * k + 1) : (2 * k + 1));   // (2k+1)(-1)^k
         qbr = fma(sg, dr, qbr);
         qbi = fma(sg, di, qbi);
         prev = q;
@@ -87,6 +90,7 @@ struct EmitMixed {
 // accumulated by EmitMixed): same D_n, psi/chi and a_n/b_n arithmetic as
 // homog_instance.
 struct NoSums {
+    static constexpr bool needs_inv_n = false;
     __device__ __forceinline__ void init() {}
     __device__ __forceinline__ void add_rcp(int, cplx, cplx, double, double) {}
 };
@@ -106,8 +110,8 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_i
     const int nmax = (int)(v.off[row + 1] - o);
     const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
     const double x = v.xg[row];
-    const cplx m = cx(v.m[unit]);
-    if (!isfinite(m.re) || !isfinite(m.im)) atomicOr(flags, GBMIE_FLAG_INVALID);
+    const double4 rc = v.rowc[row];
+    const HomogIndex h = v.hidx[unit];
     EmitMixed emit;
     emit.cf = cf + c;
     emit.amax = 0.f;
@@ -117,15 +121,15 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_i
     emit.prev = make_float4(0.f, 0.f, 0.f, 0.f);
     emit.inv_n1 = 1.f / (float)(nmax + 1);
     NoSums ns;
-    homog_instance(x, m * m, cx(1.0, 0.0), v.pc + o, nmax, emit, ns);
-    const double y2 = x * x;
-    const double qext = 2.0 * (double)emit.ext / y2;
-    const double qsca = 2.0 * (double)emit.sca / y2;
+    homog_core(x, rc.z, rc.x, rc.y, h, v.pc + o, nmax, emit, ns);
+    const double iy2 = rc.z * rc.z;   // 1 / x^2
+    const double qext = 2.0 * (double)emit.ext * iy2;
+    const double qsca = 2.0 * (double)emit.sca * iy2;
     double *o4 = v.eff4 + t * 4;
     o4[0] = qext;
     o4[1] = qsca;
-    o4[2] = (emit.qbr * emit.qbr + emit.qbi * emit.qbi) / y2;
-    o4[3] = 4.0 / y2 * (double)emit.asy / qsca;
+    o4[2] = (emit.qbr * emit.qbr + emit.qbi * emit.qbi) * iy2;
+    o4[3] = 2.0 * (double)emit.asy / (double)emit.sca;   // 4/x^2 asy / qsca
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
@@ -201,8 +205,8 @@ struct TcArgs {
 // shared-memory carve (bytes)
 #define TC_A_BYTES (TC_KC * 128 * 2)                   // one A matrix chunk: 8 KB
 #define TC_B_BYTES (TC_KC * TC_NBLK * 2)               // one B matrix chunk: 12 KB
-#define TC_STAGE_PITCH (TC_INST + 1)                   // padded row: conflict-free reads
-#define TC_STAGE_FLOATS (4 * 64 * TC_STAGE_PITCH)      // Mueller staging [k][col][size]: 65 KB
+#define TC_STAGE_PITCH 66                              // 64 columns + 2: conflict-free pair writes
+#define TC_STAGE_FLOATS (4 * TC_INST * TC_STAGE_PITCH) // Mueller staging [k][size][col]: 66 KB
 #define TC_SMEM_BYTES (4 * TC_A_BYTES + 8 * TC_B_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
 
 // One K chunk (TC_KC orders from k0) of angle block blk of the four B
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
     uint8_t *sB0 = sA + 4 * TC_A_BYTES;                     // chunk 0 of the angle block, resident
     uint8_t *sB1 = sB0 + 4 * TC_B_BYTES;                    // later chunks
     float *stage = (float *)(sB1 + 4 * TC_B_BYTES);         // [4][64][65]
-    float *sw = stage + TC_STAGE_FLOATS;                    // [NB][64]
+    float *sw = stage + TC_STAGE_FLOATS;                    // [64 sizes][8 bins]
     uint64_t *bar = (uint64_t *)(sw + 8 * TC_INST);
     uint32_t *s_tmem = (uint32_t *)(bar + 1);
     int *s_unit = (int *)(s_tmem + 1);
@@ -274,12 +278,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         const float *Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
 
         for (int blk = 0; blk < nblocks; ++blk) {
-            // per-unit sums as unevaluated FP32 pairs (hi + lo, two-sum)
-            float uh[TC_ROUNDS][NB], ul[TC_ROUNDS][NB];
+            // per-unit sums of this thread's two columns per round as
+            // unevaluated FP32 pairs (hi + lo, two-sum)
+            float uh[TC_ROUNDS][2][NB], ul[TC_ROUNDS][2][NB];
 #pragma unroll
             for (int r = 0; r < TC_ROUNDS; ++r)
 #pragma unroll
-                for (int b = 0; b < NB; ++b) uh[r][b] = ul[r][b] = 0.f;
+                for (int c = 0; c < 2; ++c)
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) uh[r][c][b] = ul[r][c][b] = 0.f;
             if (blk != s_blk_loaded) {   // uniform: chunk 0 of this angle block into sB0
                 copy_b_chunk(g, sB0, 0, blk, tid);
                 s_blk_loaded = blk;
@@ -290,12 +297,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);   // largest nmax of the tile
                 const int ktile = (kt + TC_KC - 1) / TC_KC * TC_KC;
                 // scaled weights of the tile
-                for (int idx = tid; idx < NB * TC_INST; idx += TC_THREADS) {
-                    const int b = idx / TC_INST, i = idx % TC_INST;
+                for (int idx = tid; idx < 8 * TC_INST; idx += TC_THREADS) {
+                    const int b = idx & 7, i = idx >> 3;
                     float w = 0.f;
-                    if (i < ntile && b < v.n_bin)
+                    if (i < ntile && b < v.n_bin && b < NB)
                         w = ldexpf(Wb[(size_t)b * v.n_comp * v.n_size + t0 + i], max(-300, 2 * (ex[t0 + i] - E)));
-                    sw[b * TC_INST + i] = w;
+                    sw[idx] = w;
                 }
                 // A-row data of this thread: size i = tid / 4, orders 8 (tid % 4) .. + 8 of each chunk
                 const int ia = tid >> 2, seg = tid & 3;
@@ -374,69 +381,102 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                     __syncthreads();
                     if (*s_abort) goto done;
                 }
-                // ---- epilogue: S+/S- -> Mueller -> weighted sums over the tile's sizes
-                const int q = warp & 3;            // TMEM lane quarter
-                const int row = 32 * q + lane;     // 2 i + (0 Re, 1 Im)
-                const int il = row >> 1;
-                for (int r = 0; r < TC_ROUNDS; ++r) {
+                // ---- epilogue: S+/S- -> Mueller -> weighted sums over the tile's sizes.
+                // Mueller phase: warp (q = TMEM lane quarter, half = warp / 4)
+                // holds rows 32 q .. + 31 (sizes 16 q .. + 15, Re/Im lane
+                // pairs) for 32 columns.  Lanes exchange one value per column
+                // pair so that the even lane forms column 2p and the odd lane
+                // column 2p + 1 (no idle lanes).
+                // Reduction phase: warp w sums element kk = w / 2, columns
+                // 32 (w % 2) + 2 cp + {0, 1} (cp = lane % 16) over sizes
+                // 32 h .. + 31 (h = lane / 16) for every bin; the two size
+                // halves meet by a shuffle.
+                const int q = warp & 3;
+                const int il = 16 * q + (lane >> 1);
+                const bool odd = lane & 1;
+                const int kk = warp >> 1, cg = warp & 1, hh = lane >> 4, cp = lane & 15;
+#pragma unroll
+                for (int r = 0; r < TC_ROUNDS; ++r) {   // unrolled: uh/ul stay in registers
                     const int chunk = 2 * r + (warp >> 2);
                     float sp[32], sm[32];
                     tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * chunk, sp);
                     tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 256 + 32 * chunk, sm);
+                    float *strow = stage + il * TC_STAGE_PITCH + 32 * (warp >> 2) + (odd ? 1 : 0);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const float spo = __shfl_xor_sync(0xffffffffu, sp[j], 1);
-                        const float smo = __shfl_xor_sync(0xffffffffu, sm[j], 1);
-                        if (!(lane & 1)) {
-                            const float pr = sp[j], pi = spo, mr = sm[j], mi = smo;
-                            const float A2 = pr * pr + pi * pi, B2 = mr * mr + mi * mi;
-                            // [k][col][size]: the 16 even lanes write 16 consecutive sizes
-                            const int col = (warp >> 2) * 32 + j;
-                            float *st = stage + col * TC_STAGE_PITCH + il;
-                            st[0 * 64 * TC_STAGE_PITCH] = 0.25f * (A2 + B2);
-                            st[1 * 64 * TC_STAGE_PITCH] = -0.5f * (pr * mr + pi * mi);
-                            st[2 * 64 * TC_STAGE_PITCH] = 0.25f * (A2 - B2);
-                            st[3 * 64 * TC_STAGE_PITCH] = -0.5f * (mr * pi - mi * pr);
-                        }
+                    for (int pj = 0; pj < 16; ++pj) {
+                        const int j0 = 2 * pj, j1 = 2 * pj + 1;
+                        const float rp = __shfl_xor_sync(0xffffffffu, odd ? sp[j0] : sp[j1], 1);
+                        const float rm = __shfl_xor_sync(0xffffffffu, odd ? sm[j0] : sm[j1], 1);
+                        const float pr = odd ? rp : sp[j0], pi = odd ? sp[j1] : rp;
+                        const float mr = odd ? rm : sm[j0], mi = odd ? sm[j1] : rm;
+                        const float A2 = pr * pr + pi * pi, B2 = mr * mr + mi * mi;
+                        float *st = strow + j0;
+                        st[0 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 + B2);
+                        st[1 * TC_INST * TC_STAGE_PITCH] = -0.5f * (pr * mr + pi * mi);
+                        st[2 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 - B2);
+                        st[3 * TC_INST * TC_STAGE_PITCH] = -0.5f * (mr * pi - mi * pr);
                     }
                     __syncthreads();
                     {
-                        const int kk = tid >> 6, col = tid & 63;
-                        float acc[NB];
+                        float acc[2][NB];
 #pragma unroll
-                        for (int b = 0; b < NB; ++b) acc[b] = 0.f;
-                        const float *srow = stage + (kk * 64 + col) * TC_STAGE_PITCH;
-                        for (int i = 0; i < TC_INST; ++i) {
-                            const float s = srow[i];
+                        for (int c = 0; c < 2; ++c)
 #pragma unroll
-                            for (int b = 0; b < NB; ++b) acc[b] = fmaf(sw[b * TC_INST + i], s, acc[b]);
+                            for (int b = 0; b < NB; ++b) acc[c][b] = 0.f;
+                        const float *src = stage + (kk * TC_INST + 32 * hh) * TC_STAGE_PITCH + 32 * cg + 2 * cp;
+                        const float *wsrc = sw + 32 * hh * 8;
+#pragma unroll 4
+                        for (int i = 0; i < 32; ++i) {
+                            const float2 sv = *(const float2 *)(src + i * TC_STAGE_PITCH);
+                            const float4 w0 = *(const float4 *)(wsrc + 8 * i);
+                            float wv[8] = {w0.x, w0.y, w0.z, w0.w, 0.f, 0.f, 0.f, 0.f};
+                            if (NB > 4) {
+                                const float4 w1 = *(const float4 *)(wsrc + 8 * i + 4);
+                                wv[4] = w1.x;
+                                wv[5] = w1.y;
+                                wv[6] = w1.z;
+                                wv[7] = w1.w;
+                            }
+#pragma unroll
+                            for (int b = 0; b < NB; ++b) {
+                                acc[0][b] = fmaf(wv[b], sv.x, acc[0][b]);
+                                acc[1][b] = fmaf(wv[b], sv.y, acc[1][b]);
+                            }
                         }
 #pragma unroll
-                        for (int b = 0; b < NB; ++b) {   // two-sum: (uh + ul) += acc exactly-rounded
-                            const float sum = uh[r][b] + acc[b];
-                            const float bp = sum - uh[r][b];
-                            ul[r][b] += (uh[r][b] - (sum - bp)) + (acc[b] - bp);
-                            uh[r][b] = sum;
-                        }
+                        for (int c = 0; c < 2; ++c)
+#pragma unroll
+                            for (int b = 0; b < NB; ++b) {
+                                const float a = acc[c][b] + __shfl_xor_sync(0xffffffffu, acc[c][b], 16);
+                                // two-sum: (uh + ul) += a exactly-rounded
+                                const float sum = uh[r][c][b] + a;
+                                const float bp = sum - uh[r][c][b];
+                                ul[r][c][b] += (uh[r][c][b] - (sum - bp)) + (a - bp);
+                                uh[r][c][b] = sum;
+                            }
                     }
                     __syncthreads();
                 }
                 tc_fence_before();
             }
-            // unit results of this angle block: (element kk, column) per thread
-            {
-                const int kk = tid >> 6;
+            // unit results of this angle block: lanes of the first size half
+            // hold the combined sums of (element kk, two columns) per round
+            if ((lane >> 4) == 0) {
+                const int kk = warp >> 1;
                 const double f2 = ldexp(1.0, 2 * (E - SHIFT_BITS));
 #pragma unroll
                 for (int r = 0; r < TC_ROUNDS; ++r) {
-                    const int col = blk * TC_NBLK + 64 * r + (tid & 63);
-                    if (col < v.n_ang) {
 #pragma unroll
-                        for (int b = 0; b < NB; ++b) {
-                            if (b < v.n_bin) {
-                                const double f = v.frac[(size_t)b * v.n_comp + comp];
-                                atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
-                                          f * ((double)uh[r][b] + (double)ul[r][b]) * f2);
+                    for (int c = 0; c < 2; ++c) {
+                        const int col = blk * TC_NBLK + 64 * r + 32 * (warp & 1) + 2 * (lane & 15) + c;
+                        if (col < v.n_ang) {
+#pragma unroll
+                            for (int b = 0; b < NB; ++b) {
+                                if (b < v.n_bin) {
+                                    const double f = v.frac[(size_t)b * v.n_comp + comp];
+                                    atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
+                                              f * ((double)uh[r][c][b] + (double)ul[r][c][b]) * f2);
+                                }
                             }
                         }
                     }

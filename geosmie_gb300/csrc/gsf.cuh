@@ -7,6 +7,7 @@ struct GsfTables {
     void *mem;        // one cudaMalloc block holding everything below
     double *z, *w;    // nodes (ascending) and weights [ng]
     double *P;        // [4][ng][L] generalized spherical functions P1..P4
+    float *Ph, *Pl;   // P split into FP32 hi + lo (P = Ph + Pl to ~2^-48)
     double *frac;     // [ng] interpolation fraction
     int *base;        // [ng] interpolation interval start
 };
@@ -21,6 +22,8 @@ struct GsfMap {
 
 int gsf_prepare(gbmie_ctx *ctx, int ng, int nang, const double *theta_rad, GsfTables *t);
 void gsf_release(GsfTables *t);
+// precision: GBMIE_PLAIN_FP64 (FP64 sums) or GBMIE_MIXED (split-FP32
+// products, Kahan-compensated FP32 sums)
 int launch_gsf_expand(gbmie_ctx *ctx, const GsfTables *t, int ntab, const double *F, int64_t entry_stride,
                       int64_t row_stride, GsfMap map, double *coef, int64_t out_stride, int64_t out_row_stride,
-                      double *cnorm);
+                      double *cnorm, int precision);

@@ -92,6 +92,7 @@ __device__ __forceinline__ void psi_row_complex(cplx z, int nmax, double2 *out, 
 // Running efficiency sums of pymiecoated/mie_props.py:28-70, accumulated in
 // the order coefficients are produced.
 struct EffSums {
+    static constexpr bool needs_inv_n = true;   // add_rcp takes 1/n
     double ext, sca, asy;
     cplx qb;
     cplx a1, b1;   // a_{n+1}, b_{n+1} of the previous (higher) order
@@ -164,25 +165,47 @@ __device__ __forceinline__ cplx mie_ratio(cplx d, double psin, double chin, doub
 // row1: psi/chi of x for orders 1..nmax at row1[n-1]; it may alias the
 // emitter's a_n output (row n is consumed before a_n is written).
 // ---------------------------------------------------------------------------
-template <class Emit, class Sums>
-__device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, const double2 *row1,
-                                               int nmax, Emit &emit, Sums &es)
+// Medium constants of the homogeneous recurrences: z = zm x with
+// zm = sqrt(eps mu) and the relative index m = sqrt(eps / mu)
+// (pymiecoated/mie_coeffs.py:144-145), their reciprocals and |zm|.  They
+// depend on the medium only, so a table computes them once per
+// (wavelength, RH, component) unit.
+struct HomogIndex {
+    cplx zm, zminv, m, minv;
+    double azm;
+};
+
+__device__ __forceinline__ HomogIndex homog_index(cplx eps, cplx mu)
 {
-    const cplx z = csqrt(eps * mu) * x;
-    const cplx m = csqrt(eps / mu);
-    const double az = cabs(z);
+    HomogIndex h;
+    h.zm = csqrt(eps * mu);
+    h.m = csqrt(eps / mu);
+    h.zminv = cinv(h.zm);
+    h.minv = cinv(h.m);
+    h.azm = cabs(h.zm);
+    return h;
+}
+
+// The recurrences of one instance given the medium constants and the size
+// constants 1/x, sin x, cos x (a table computes those once per size row).
+template <class Emit, class Sums>
+__device__ __forceinline__ void homog_core(double x, double xinv, double sx, double cxv, const HomogIndex &h,
+                                           const double2 *row1, int nmax, Emit &emit, Sums &es)
+{
+    const cplx m = h.m;
+    const cplx minv = h.minv;
+    const double az = h.azm * x;
     const int nmx = (int)rint(fmax((double)nmax, az) + 16.0);
-    const cplx zinv = cinv(z);
-    const cplx minv = cinv(m);
-    const double xinv = 1.0 / x;
+    const cplx zinv = h.zminv * xinv;
     // Warm-up steps above nmax.  The reference runs nmx - 1 - nmax of them
-    // from D = 0.  For n > |z| the recurrence damps the start error by
-    // (|z| / (2n+1))^2 per step, so when |z| < (nmax+1)/2 fewer steps reach
-    // the same converged D_nmax (damping below 1e-17, plus two spare steps).
+    // from D = 0 (mie_coeffs.py:150, 168-170).  For n > |z| the recurrence
+    // damps the start error by (|z| / (2n+1))^2 per step, so when
+    // |z| < (nmax+1)/2 fewer steps reach the same converged D_nmax (damping
+    // below 1e-17, plus two spare steps; the step count needs no FP64 log).
     int warm = nmx - 1 - nmax;
     if (az < 0.5 * (nmax + 1)) {
-        const double q = 2.0 * log((2.0 * (nmax + 1) + 1.0) / az);   // -ln(damping) per step
-        const int need = (int)ceil(39.2 / q) + 2;
+        const float q = 2.f * logf((2.f * (float)(nmax + 1) + 1.f) / (float)az);   // -ln(damping) per step
+        const int need = (int)ceilf(39.2f / q) + 2;
         if (need < warm) warm = need;
     }
     cplx D = cx(0.0, 0.0);
@@ -190,23 +213,24 @@ __device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, cons
         const cplx r = zinv * (double)(k + 1);
         D = r - cinv(D + r);
     }
-    double sx, cxv;
-    sincos(x, &sx, &cxv);
     double2 pcn = row1[nmax - 1];
     es.init();
     // One reciprocal per order: at order k the denominators of a_k, b_k and
     // of the next D step (D_k + r_{k-1}) and k itself are inverted together,
     // 1/(A B C k), and the four reciprocals recovered by multiplication.
-    cplx w = D + zinv * (double)(nmax + 1);            // D_{nmax+1} + r_nmax
-    double inv_w2 = 1.0 / abs2(w);                    // 1/|w|^2 for D_nmax
+    cplx rk1 = zinv * (double)(nmax + 1);             // r_nmax = (nmax+1)/z
+    cplx w = D + rk1;                                  // D_{nmax+1} + r_nmax
+    double inv_w2 = 1.0 / abs2(w);                     // 1/|w|^2 for D_nmax
     double inv_n1 = 1.0 / (double)(nmax + 1);          // 1/(k+1)
     for (int k = nmax; k >= 1; --k) {
-        const cplx r = zinv * (double)(k + 1);
-        D = r - cx(w.re * inv_w2, -w.im * inv_w2);      // D_k
+        const double dk = (double)k;
+        const cplx r = rk1;                            // (k+1)/z
+        D = cx(fma(-w.re, inv_w2, r.re), fma(w.im, inv_w2, r.im));   // D_k = r - 1/w
         const double2 pcm = (k > 1) ? row1[k - 2] : make_double2(sx, cxv);
-        const double nx = (double)k * xinv;
-        const cplx da = D * minv + nx;
-        const cplx db = D * m + nx;
+        const double nx = dk * xinv;
+        // da = D/m + k/x, db = D m + k/x
+        const cplx da = cx(fma(D.re, minv.re, fma(-D.im, minv.im, nx)), fma(D.re, minv.im, D.im * minv.re));
+        const cplx db = cx(fma(D.re, m.re, fma(-D.im, m.im, nx)), fma(D.re, m.im, D.im * m.re));
         const cplx Na = cx(da.re * pcn.x - pcm.x, da.im * pcn.x);
         const cplx Ma = cx(da.re * pcn.y - pcm.y, da.im * pcn.y);
         const cplx Nb = cx(db.re * pcn.x - pcm.x, db.im * pcn.x);
@@ -214,12 +238,18 @@ __device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, cons
         const cplx qa = cx(Na.re + Ma.im, Na.im - Ma.re);   // N - i M
         const cplx qbv = cx(Nb.re + Mb.im, Nb.im - Mb.re);
         const double A = abs2(qa), B = abs2(qbv);
-        w = D + zinv * (double)k;                          // D_k + r_{k-1}
+        rk1 = zinv * dk;                                   // r_{k-1} = k/z
+        w = D + rk1;                                       // D_k + r_{k-1}
         const double C = (k > 1) ? abs2(w) : 1.0;
         const double AB = A * B, ABC = AB * C;
-        const double inv = 1.0 / (ABC * (double)k);
-        const double inv_n = ABC * inv;                    // 1/k
-        const double t = (double)k * inv;                  // 1/(A B C)
+        double t, inv_n = 0.0;                             // 1/(A B C), 1/k
+        if (Sums::needs_inv_n) {
+            const double inv = 1.0 / (ABC * dk);
+            inv_n = ABC * inv;
+            t = dk * inv;
+        } else {
+            t = 1.0 / ABC;
+        }
         inv_w2 = AB * t;                                   // 1/C
         const double u = C * t;                            // 1/(A B)
         const double ia = B * u, ib = A * u;               // 1/A, 1/B
@@ -230,6 +260,17 @@ __device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, cons
         inv_n1 = inv_n;
         pcn = pcm;
     }
+}
+
+// One instance from (x, eps, mu) alone.
+template <class Emit, class Sums>
+__device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, const double2 *row1, int nmax,
+                                               Emit &emit, Sums &es)
+{
+    const HomogIndex h = homog_index(eps, mu);
+    double sx, cxv;
+    sincos(x, &sx, &cxv);
+    homog_core(x, 1.0 / x, sx, cxv, h, row1, nmax, emit, es);
 }
 
 // ---------------------------------------------------------------------------

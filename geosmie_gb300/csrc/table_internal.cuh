@@ -3,6 +3,7 @@
 #pragma once
 #include "common.cuh"
 #include "gsf.cuh"
+#include "mie_device.cuh"
 
 #define TWO_PI 6.28318530717958647692
 #define PI_D 3.14159265358979323846
@@ -19,7 +20,7 @@ struct gbmie_table_plan {
     int nmax_max;
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
     // mixed precision (tensor-core) path
-    size_t o_cf, o_eexp, o_eunit, o_bt, o_counter, o_wf;
+    size_t o_cf, o_eexp, o_eunit, o_bt, o_counter, o_wf, o_tw, o_rowc, o_hidx;
     int n_pad_total;     // angles padded to whole 192-column blocks
     int k_pad;           // orders padded to 32
     int *unit_order;     // [n_units] units by decreasing work (plan-owned)
@@ -67,6 +68,9 @@ struct TabView {
     double2 *pc, *an, *bn;
     double *eff4, *W, *sums, *reff0, *pacc, *sraw, *nlraw;
     float *Wf;   // FP32 copy of W (mixed path), or NULL
+    double *tw;  // trapz weights of the angle grid [n_ang]
+    double4 *rowc;      // per size row: sin x, cos x, 1/x
+    HomogIndex *hidx;   // per unit: medium constants of the recurrences
     const double2 *pq;
     // PSD weights, their radius moments and reff0 do not depend on the
     // wavelength when the grid is a radius grid and the PSD is analytic
