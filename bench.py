@@ -32,6 +32,10 @@ METRIC = "Mie instance-evals/s + table gen time, mixed vs FP64 plain on 1 GB300 
 UNIT = "instance-evals/s"
 # CPU sample: wavelength and RH indices of the stratified sample of units
 SAMPLE_LAMBDA = [0, 12, 24, 36, 48, 59]
+# DRAM bytes (read + write) per (wavelength, RH, component) unit from one ncu
+# capture of the 12-wavelength sulfate table (432 units; profiles/
+# k_tab_coeffs_mixed_k_tab_s12_tc_sulfate12.md), scaled to a run by its units
+NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": 138.586112e6 / 432, "k_tab_s12_tc": 175.143168e6 / 432}
 SAMPLE_RH = [0, 35]
 
 
@@ -135,7 +139,7 @@ class Clocks(object):
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
-                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
@@ -166,7 +170,7 @@ class Clocks(object):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -186,7 +190,7 @@ def main():
         dist.init_process_group("nccl")
     dev = local
     from geosmie_gb300 import _native, workloads
-    from geosmie_gb300.table import TablePlan
+    from geosmie_gb300.table import NL_ORDER, SCALAR_ORDER, SCATKEYS, TablePlan
     ctx = _native.context(dev)
     if args.small:
         spec, desc = workloads.sulfate_table(n_rh=6, n_lambda=10, n_radii=500)
@@ -201,28 +205,27 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:%d" % dev)
     stream = torch.cuda.current_stream(dev)
 
-    def timed(precision, with_clocks=False):
+    def timed(plan, graph=False, with_clocks=False):
         """Warm-up, then K tables between barriers + syncs, L2 flushed before
         each (256 MB write, inside the timed region).  Returns (ms, launches,
-        kernel times, clocks, plan)."""
-        plan = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=dev)
-        for _ in range(args.warmup):
-            plan.run()
-        plan.sync()
+        kernel times, clocks)."""
         clocks = Clocks(dev)
+        if with_clocks:
+            clocks.start()   # sampling spans the last warm-up tables and the timed region
+        for _ in range(args.warmup):
+            plan.run(graph=graph)
+        plan.sync()
         ctx.set_timing(True)
         launches0 = ctx.launches()
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
-        if with_clocks:
-            clocks.start()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             flush.zero_()
-            plan.run()
+            plan.run(graph=graph)
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
@@ -230,27 +233,44 @@ def main():
         launches = ctx.launches() - launches0
         kt = ctx.kernel_times()
         ctx.set_timing(False)
+        plan.sync()   # device error flags -> status
         if ws > 1:
             t = torch.tensor([ms], dtype=torch.float64, device="cuda:%d" % dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             ms = float(t.item())
             torch.distributed.barrier()
-        return ms, launches, kt, clk, plan
+        return ms, launches, kt, clk
 
-    ms_plain, _, kt_plain, _, plan_plain = timed(_native.GBMIE_PLAIN_FP64)
-    ms, launches, ktimes, clk, plan_mixed = timed(_native.GBMIE_MIXED, with_clocks=True)
+    plan_plain = TablePlan(spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=n_gsf, device=dev)
+    ms_plain, _, kt_plain, _ = timed(plan_plain)
+    ra = plan_plain.results()
+    plan_plain.close()
+    del plan_plain
+    plan_mixed = TablePlan(spec, precision=_native.GBMIE_MIXED, n_gsf=n_gsf, device=dev)
+    # eager launches with per-kernel CUDA events: kernel shares and the roofline
+    ms_eager, _, ktimes, _ = timed(plan_mixed)
+    # the product path: the whole table replayed as one CUDA graph
+    ms, launches, _, clk = timed(plan_mixed, graph=True, with_clocks=True)
     ms_step = ms / args.steps
     value = ws * counts["instances"] * args.steps / (ms * 1e-3)
-    # accuracy of the mixed table against the FP64 table (same run)
-    ra, rb = plan_plain.results(), plan_mixed.results()
+    # accuracy of the mixed table against the FP64 table (same run), every output
+    rb = plan_mixed.results()
     p11 = np.abs(ra["p11"])
-    acc = {"phase_max_abs_err_over_p11": float(max(np.max(np.abs(rb[k] - ra[k]) / p11)
-                                                  for k in ["p11", "p12", "p22", "p33", "p34", "p44"])),
-           "pmom_max_abs_err_over_max_alpha1": float(np.max(np.abs(rb["pmom"] - ra["pmom"]) / np.max(
-               np.abs(ra["pmom"][..., 0, :]), axis=-1)[..., None, None])),
+    acc = {"phase_max_abs_err_over_p11": {k: float(np.max(np.abs(rb[k] - ra[k]) / p11)) for k in SCATKEYS},
+           "pback_max_abs_err_over_p11back": float(np.max(np.abs(rb["pback"] - ra["pback"]) /
+                                                          np.abs(ra["pback"][..., :1]))),
+           "pmom_max_abs_err_over_max_alpha1": {
+               nm: float(np.max(np.abs(rb["pmom"][..., j, :] - ra["pmom"][..., j, :]) /
+                                np.max(np.abs(ra["pmom"][..., 0, :]), axis=-1)[..., None]))
+               for j, nm in enumerate(["alpha1", "beta1", "alpha3", "beta2", "alpha2", "alpha4"])},
            "scalars_max_rel_err": {k: float(np.max(np.abs(rb[k] - ra[k]) / np.maximum(np.abs(ra[k]), 1e-300)))
-                                   for k in ["qext", "qsca", "g", "qb", "ssa", "bext", "bsca"]}}
-    del plan_plain
+                                   for k in SCALAR_ORDER},
+           "wavelength_independent_max_rel_err": {
+               k: float(np.max(np.abs(rb["nl_" + k] - ra["nl_" + k]) / np.maximum(np.abs(ra["nl_" + k]), 1e-300)))
+               for k in NL_ORDER}}
+    acc["qabs_max_abs_err_over_qext"] = float(np.max(np.abs(rb["qabs"] - ra["qabs"]) / np.abs(ra["qext"])))
+    plan_mixed.close()
+    del plan_mixed
 
     # ---- end to end through the public API: host inputs in, host table out ----
     e2e_times = []
@@ -278,7 +298,10 @@ def main():
         "k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * counts["instances"]) * nang,
         # D_n steps (12 flop), a_n/b_n and efficiency sums (89 flop per order)
         "k_tab_coeffs": coef_flop,
-        "k_tab_coeffs_mixed": coef_flop,
+        # FP64 part of the mixed recurrences: 19 flop per warm-up D_n step, 36 per
+        # order (D_n, its Newton reciprocal, Re of the a_n/b_n numerators and
+        # denominators); the ratio and the efficiency sums are FP32
+        "k_tab_coeffs_mixed": 19.0 * counts["sum_warm"] + 36.0 * counts["sum_nmax"],
     }
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -298,8 +321,10 @@ def main():
     if top[0] in flops:
         nl_, tms = top[1]
         ach = flops[top[0]] / (tms / nl_ * 1e-3) / 1e9
+        tb = NCU_BYTES_PER_UNIT.get(top[0])
         roof = {"bound": "fp64", "kernel": top[0], "achieved": ach, "peak": fp64_peak, "unit": "GFLOP/s",
-                "frac": ach / fp64_peak, "traffic": None,
+                "frac": ach / fp64_peak, "traffic": tb * counts["units"] if tb else None,
+                "traffic_unit": "bytes per launch (ncu capture scaled by units)",
                 "peak_source": "DFMA throughput measured in this run (gbmie_measure_fp64_peak); "
                                "MEASURED_PEAKS.json has no FP64 figure",
                 "algorithmic_flop_per_launch": flops[top[0]]}
@@ -309,15 +334,16 @@ def main():
         nl_, tms = ktimes["k_tab_s12_tc"]
         sec = tms / nl_ * 1e-3
         alg = 8.0 * counts["sum_nmax"] * nang
-        # 6 MMAs (M 128 x N 192 x K 16) per 16 orders of a tile, per 192-angle block
-        exe = counts["sum_ktile"] / 16.0 * 6 * 2 * 128 * 192 * 16 * (-(-nang // 192))
+        # 6 MMAs (M 128 x N 64 x K 16) per 16-order chunk of a tile, per 64-angle block
+        exe = counts["sum_kc16"] * 6 * 2 * 128 * 64 * 16 * (-(-nang // 64))
         kernels["k_tab_s12_tc"]["algorithmic_tflops"] = alg / sec / 1e12
         kernels["k_tab_s12_tc"]["executed_mma_tflops"] = exe / sec / 1e12
         kernels["k_tab_s12_tc"]["tensor_peak_tflops"] = peaks.get("bf16_tflops")
         if top[0] == "k_tab_s12_tc":
             roof = {"bound": "tensor", "kernel": "k_tab_s12_tc", "achieved": exe / sec / 1e12,
                     "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-                    "frac": exe / sec / 1e12 / peaks.get("bf16_tflops"), "traffic": None,
+                    "frac": exe / sec / 1e12 / peaks.get("bf16_tflops"),
+                    "traffic": NCU_BYTES_PER_UNIT["k_tab_s12_tc"] * counts["units"],
                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
                     "algorithmic_flop_per_launch": alg, "executed_mma_flop_per_launch": exe,
                     "note": "executed = 3 split products x 2 GEMMs on padded tiles; algorithmic = 8 flop "
@@ -338,8 +364,10 @@ def main():
         "config": {"workload": desc, "instances": counts["instances"], "sum_nmax": counts["sum_nmax"],
                    "gsf_moments": n_gsf, "precision": "mixed: FP64 recurrences, tcgen05 split-FP16 contractions "
                    "with FP32 accumulation", "parallelism": "replicas" if ws > 1 else "1 GPU",
-                   "l2": "flushed before every table (256 MB write inside the timed region)"},
-        "table_gen_ms": {"mixed": ms_step, "plain_fp64": ms_plain / args.steps},
+                   "l2": "flushed before every table (256 MB write inside the timed region)",
+                   "launch": "whole table replayed as one CUDA graph (gbmie_table_run_graph)"},
+        "table_gen_ms": {"mixed": ms_step, "mixed_eager_launches": ms_eager / args.steps,
+                         "plain_fp64": ms_plain / args.steps},
         "mixed_vs_plain_speedup": ms_plain / ms,
         "plain_fp64": {"value": ws * counts["instances"] * args.steps / (ms_plain * 1e-3), "unit": UNIT,
                        "kernels": kernel_table(kt_plain)},

@@ -287,21 +287,21 @@ __global__ void k_gsf_split(size_t n, const double *__restrict__ P, float *__res
     Pl[i] = (float)(P[i] - (double)h);
 }
 
-int gsf_prepare(gbmie_ctx *ctx, int ng, int nang, const double *theta, GsfTables *t)
+int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, GsfTables *t)
 {
     t->ng = ng;
-    t->L = ng;
+    t->L = L;
     t->nang = nang;
-    const size_t bytes = sizeof(double) * (2 * (size_t)ng + 4 * (size_t)ng * ng + ng) +
-                         sizeof(float) * 8 * (size_t)ng * ng + sizeof(int) * ng;
+    const size_t bytes = sizeof(double) * (2 * (size_t)ng + 4 * (size_t)ng * L + ng) +
+                         sizeof(float) * 8 * (size_t)ng * L + sizeof(int) * ng;
     GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&t->mem, bytes), "gsf tables"));
     char *p = (char *)t->mem;
     t->z = (double *)p; p += sizeof(double) * ng;
     t->w = (double *)p; p += sizeof(double) * ng;
-    t->P = (double *)p; p += sizeof(double) * 4 * (size_t)ng * ng;
+    t->P = (double *)p; p += sizeof(double) * 4 * (size_t)ng * L;
     t->frac = (double *)p; p += sizeof(double) * ng;
-    t->Ph = (float *)p; p += sizeof(float) * 4 * (size_t)ng * ng;
-    t->Pl = (float *)p; p += sizeof(float) * 4 * (size_t)ng * ng;
+    t->Ph = (float *)p; p += sizeof(float) * 4 * (size_t)ng * L;
+    t->Pl = (float *)p; p += sizeof(float) * 4 * (size_t)ng * L;
     t->base = (int *)p;
     const int tb = 128, nb = (ng + tb - 1) / tb;
     ctx_pre_launch(ctx);
@@ -310,7 +310,7 @@ int gsf_prepare(gbmie_ctx *ctx, int ng, int nang, const double *theta, GsfTables
     ctx_pre_launch(ctx);
     k_gsf_gener<<<nb, tb, 0, ctx->stream>>>(ng, t->L, t->z, t->P);
     GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_gener"));
-    const size_t np = 4 * (size_t)ng * ng;
+    const size_t np = 4 * (size_t)ng * L;
     ctx_pre_launch(ctx);
     k_gsf_split<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(np, t->P, t->Ph, t->Pl);
     GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_split"));
@@ -372,7 +372,7 @@ extern "C" int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const doubl
     k_deg2rad<<<(nang + 127) / 128, 128, 0, ctx->stream>>>(nang, ang_deg, theta, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_deg2rad"));
     GsfTables t{};
-    GBMIE_TRY(gsf_prepare(ctx, nnodes, nang, theta, &t));
+    GBMIE_TRY(gsf_prepare(ctx, nnodes, nnodes, nang, theta, &t));
     GsfMap map;
     for (int i = 0; i < 6; ++i) map.f[i] = i, map.o[i] = i;
     int st = launch_gsf_expand(ctx, &t, ntab, F, (int64_t)6 * nang, nang, map, coef, (int64_t)6 * nnodes, nnodes,

@@ -527,6 +527,7 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.tw = (double *)(scr + p->o_tw);
     v.rowc = (double4 *)(scr + p->o_rowc);
     v.hidx = (HomogIndex *)(scr + p->o_hidx);
+    v.pcf = p->d.precision == GBMIE_MIXED ? (float2 *)(scr + p->o_pcf) : nullptr;
     return v;
 }
 
@@ -537,6 +538,10 @@ static void plan_free(gbmie_table_plan *p)
     if (p->off) cudaFree(p->off);
     if (p->unit_base) cudaFree(p->unit_base);
     if (p->unit_order) cudaFree(p->unit_order);
+    if (p->tile_cbase) cudaFree(p->tile_cbase);
+    if (p->unit_cbase) cudaFree(p->unit_cbase);
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
     gsf_release(&p->gsf);
     free(p);
 }
@@ -559,9 +564,11 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     *out = nullptr;
     const gbmie_table_desc &d = *desc;
     if (d.n_lambda < 1 || d.n_rh < 1 || d.n_size < 2 || d.n_bin < 1 || d.n_comp < 1 || d.n_ang < 2 ||
-        d.n_bin > 8 || d.n_gsf < 0 || (d.n_gsf > 0 && d.n_gsf < 3) || d.rh0_index < 0 || d.rh0_index >= d.n_rh)
+        d.n_bin > 8 || d.n_gsf < 0 || (d.n_gsf > 0 && d.n_gsf < 3) || d.rh0_index < 0 || d.rh0_index >= d.n_rh ||
+        d.n_gsf_nodes < 0 || (d.n_gsf > 0 && d.n_gsf_nodes > 0 && d.n_gsf_nodes < d.n_gsf))
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad sizes (n_size >= 2, n_ang >= 2, "
-                                                "1 <= n_bin <= 8, n_gsf = 0 or >= 3)");
+                                                "1 <= n_bin <= 8, n_gsf = 0 or >= 3, n_gsf_nodes = 0 or "
+                                                ">= n_gsf)");
     if (d.grid_kind != GBMIE_GRID_X && d.grid_kind != GBMIE_GRID_RADIUS)
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad grid_kind");
     if (d.psd_kind < GBMIE_PSD_LOGNORM || d.psd_kind > GBMIE_PSD_WEIGHTS)
@@ -622,7 +629,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         }
         p->ab_total = acc;
         // mixed path: units in decreasing order of work (sum of nmax of their size row)
-        p->n_pad_total = (d.n_ang + 191) / 192 * 192;
+        p->n_pad_total = (d.n_ang + 63) / 64 * 64;
         p->k_pad = (p->nmax_max + 31) / 32 * 32;
         if (ub && d.precision == GBMIE_MIXED && st == GBMIE_OK) {
             int64_t *cost = (int64_t *)malloc(sizeof(int64_t) * p->n_units);
@@ -650,6 +657,42 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
                     free(keys);
                 }
             }
+            // chunks (16 orders up to a tile's largest nmax) of every 64-size tile
+            p->ntiles = (d.n_size + 63) / 64;
+            const int ntp = p->ntiles + 1;
+            int *tcb = st == GBMIE_OK ? (int *)malloc(sizeof(int) * (size_t)p->n_le * ntp) : nullptr;
+            int64_t *ucb = st == GBMIE_OK ? (int64_t *)malloc(sizeof(int64_t) * p->n_units) : nullptr;
+            if (st == GBMIE_OK && (!tcb || !ucb)) st = GBMIE_ERR_NOMEM;
+            for (int le = 0; st == GBMIE_OK && le < p->n_le; ++le) {
+                int acc_c = 0;
+                for (int t = 0; t < p->ntiles; ++t) {
+                    const int t0 = 64 * t, nt = d.n_size - t0 < 64 ? d.n_size - t0 : 64;
+                    const int64_t r = (int64_t)le * d.n_size + t0 + nt - 1;
+                    tcb[le * ntp + t] = acc_c;
+                    acc_c += (int)((hoff[r + 1] - hoff[r] + 15) / 16);
+                }
+                tcb[le * ntp + p->ntiles] = acc_c;
+            }
+            int64_t nch = 0;
+            for (int64_t u = 0; st == GBMIE_OK && u < p->n_units; ++u) {
+                const int lam = (int)(u / ((int64_t)d.n_rh * d.n_comp));
+                const int le = d.grid_kind == GBMIE_GRID_X ? 0 : lam;
+                ucb[u] = nch;
+                nch += tcb[le * ntp + p->ntiles];
+            }
+            p->n_chunks = nch;
+            if (st == GBMIE_OK)
+                st = ctx_cuda(ctx, cudaMalloc(&p->tile_cbase, sizeof(int) * (size_t)p->n_le * ntp), "tile chunks");
+            if (st == GBMIE_OK)
+                st = ctx_cuda(ctx, cudaMalloc(&p->unit_cbase, sizeof(int64_t) * p->n_units), "unit chunks");
+            if (st == GBMIE_OK)
+                st = ctx_cuda(ctx, cudaMemcpy(p->tile_cbase, tcb, sizeof(int) * (size_t)p->n_le * ntp,
+                                              cudaMemcpyHostToDevice), "tile chunks copy");
+            if (st == GBMIE_OK)
+                st = ctx_cuda(ctx, cudaMemcpy(p->unit_cbase, ucb, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice),
+                              "unit chunks copy");
+            free(tcb);
+            free(ucb);
             if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMalloc(&p->unit_order, sizeof(int) * p->n_units), "unit order");
             if (st == GBMIE_OK)
                 st = ctx_cuda(ctx, cudaMemcpy(p->unit_order, ord, sizeof(int) * p->n_units, cudaMemcpyHostToDevice),
@@ -686,7 +729,8 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_eexp = carve(mixed ? sizeof(int) * (size_t)p->n_inst : 16);
         p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
         p->o_bt = carve(mixed ? 4 * 2 * (size_t)p->n_pad_total * p->k_pad : 16);
-        p->o_counter = carve(16);
+        p->o_asplit = carve(mixed ? (size_t)16384 * (size_t)p->n_chunks : 16);
+        p->o_pcf = carve(mixed ? sizeof(float2) * (size_t)p->pc_total : 16);
         p->o_wf = carve(mixed ? sizeof(float) * nW * d.n_size : 16);
         p->o_tw = carve(sizeof(double) * d.n_ang);
         p->o_rowc = carve(sizeof(double4) * (size_t)p->n_le * d.n_size);
@@ -698,7 +742,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         st = ctx_scratch(ctx, p->bytes, &scr);
     }
     if (st == GBMIE_OK && d.n_gsf > 0) {
-        st = gsf_prepare(ctx, d.n_gsf, d.n_ang, d.theta, &p->gsf);
+        st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf);
         p->has_gsf = 1;
     }
     if (st == GBMIE_OK) st = gbmie_ctx_synchronize(ctx);
@@ -793,4 +837,70 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_s12_plain"));
     return launch_table_tail(ctx, p, v, out);
+}
+
+// ---------------------------------------------------------------------------
+// The whole table as one CUDA graph
+// ---------------------------------------------------------------------------
+static bool same_out(const gbmie_table_out &a, const gbmie_table_out &b)
+{
+    return a.phase == b.phase && a.pback == b.pback && a.scalar == b.scalar && a.nl == b.nl && a.pmom == b.pmom;
+}
+
+// Capture one gbmie_table_run on the plan's private stream.  Per-kernel event
+// timing is off while capturing; the launch count of one run is recorded so
+// that replays can report it.
+static int capture_table(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_table_out *out)
+{
+    if (p->gexec) {
+        cudaGraphExecDestroy(p->gexec);   // an in-flight replay finishes first
+        p->gexec = nullptr;
+    }
+    if (!p->cap_stream)
+        GBMIE_TRY(ctx_cuda(ctx, cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking), "capture stream"));
+    const cudaStream_t saved = ctx->stream;
+    const int saved_timing = ctx->timing;
+    const int64_t l0 = ctx->launches;
+    ctx->stream = p->cap_stream;
+    ctx->timing = 0;
+    int st = ctx_cuda(ctx, cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaGraph_t graph = nullptr;
+    if (st == GBMIE_OK) {
+        st = gbmie_table_run(ctx, p, out);
+        const int st2 = ctx_cuda(ctx, cudaStreamEndCapture(p->cap_stream, &graph), "end capture");
+        if (st == GBMIE_OK) st = st2;
+    }
+    ctx->stream = saved;
+    ctx->timing = saved_timing;
+    p->glaunches = ctx->launches - l0;
+    ctx->launches = l0;
+    if (st == GBMIE_OK && graph)
+        st = ctx_cuda(ctx, cudaGraphInstantiate(&p->gexec, graph, 0), "graph instantiate");
+    if (graph) cudaGraphDestroy(graph);
+    if (st != GBMIE_OK) {
+        if (p->gexec) cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+        cudaGetLastError();   // a failed capture leaves no sticky error behind
+        return st;
+    }
+    p->gout = *out;
+    p->gscratch = ctx->scratch;
+    return GBMIE_OK;
+}
+
+extern "C" int gbmie_table_run_graph(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_table_out *out)
+{
+    if (!ctx || !p || !out || p->ctx != ctx)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_run_graph: bad plan");
+    if (!out->phase || (p->has_gsf && !out->pmom))
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_run_graph: phase (and pmom with n_gsf) required");
+    cudaSetDevice(ctx->device);
+    void *s = nullptr;
+    GBMIE_TRY(ctx_scratch(ctx, p->bytes, &s));   // grows (and synchronises) outside the capture only
+    if (!p->gexec || !same_out(p->gout, *out) || p->gscratch != ctx->scratch) GBMIE_TRY(capture_table(ctx, p, out));
+    ctx_pre_launch(ctx);
+    GBMIE_TRY(ctx_cuda(ctx, cudaGraphLaunch(p->gexec, ctx->stream), "graph launch"));
+    const int st = ctx_check_launch(ctx, "gbmie_table_graph");
+    ctx->launches += p->glaunches - 1;   // the graph's kernels, not the graph launch itself
+    return st;
 }

@@ -2,19 +2,22 @@
 // the Mueller elements and the size-distribution integration fused into the
 // epilogue.
 //
-// The recurrences stay FP64 (k_tab_coeffs_mixed: D_n, psi/chi rows, a_n,
-// b_n and the efficiency sums).  The coefficients leave it as FP32
+// The recurrences keep FP64 where stability needs it (k_tab_coeffs_mixed:
+// D_n, psi/chi rows, the cancelling real parts of the a_n/b_n numerators and
+// denominators); the ratio and the efficiency sums are FP32.  The
+// coefficients leave it as FP32
 //   c_n = a_n + b_n,  d_n = a_n - b_n   (float4 per order)
 // with a per-instance exponent e_i = floor(log2 max |c|, |d|).  The two
 // contractions
 //   S+ = S1 + S2 = sum_n c_n (pi~_n + tau~_n),   S- = S1 - S2 = sum_n d_n (pi~_n - tau~_n)
 // are GEMMs [instances x orders] x [orders x angles]: rows are (instance,
 // Re/Im) pairs, 64 instances = M 128 per tile; columns are angles in blocks of
-// up to 192 (N).  Each operand is split into FP16 hi + lo halves (values
+// 64 (N).  Each operand is split into FP16 hi + lo halves (values
 // scaled by 2^(13 - e_i) so the row maximum sits just below 2^14), and
 //   C P ~ C_hi P_hi + C_hi P_lo + C_lo P_hi
 // is accumulated in FP32 in tensor memory: three tcgen05.mma per product and
-// K step of 16 orders, six per step for S+ and S-.  The epilogue reads S+/S-
+// K step of 16 orders, six per step for S+ and S- (in windows of 48 orders,
+// cross products first, see below).  The epilogue reads S+/S-
 // rows from TMEM (tcgen05.ld), pairs Re/Im lanes, forms s11, s12, s33, s34
 // and reduces them over the tile's 64 sizes with the PSD weights of every
 // bin (the weights absorb 2^(2(e_i - E)) with E the unit's largest
@@ -26,27 +29,40 @@
 #include "tc.cuh"
 
 #define TC_INST 64        // sizes per tile (M = 128 rows: Re, Im)
-#define TC_KC 32          // orders per K chunk (two MMA K steps)
-#define TC_NBLK 192       // angles per column block (N)
-#define TC_THREADS 256
-#define TC_ROUNDS (TC_NBLK / 64)
+#define TC_NBLK 64        // angles per column block (N)
 #define SHIFT_BITS 13
 
 // ---------------------------------------------------------------------------
-// FP64 coefficients -> FP32 (c, d) + exponent
+// Mixed-precision coefficients: FP32 (c, d) + exponent
 // ---------------------------------------------------------------------------
-// Emits FP32 (c, d) and accumulates the efficiency sums from them: with
-// c = a + b and d = a - b,
-//   Re a + Re b = Re c,   |a|^2 + |b|^2 = (|c|^2 + |d|^2) / 2,
-//   Re(a_n a*_{n+1} + b_n b*_{n+1}) = (Re(c_n c*_{n+1}) + Re(d_n d*_{n+1})) / 2,
-// while Re(a_n b*_n) is formed from the FP64 a_n, b_n ((|c|^2 - |d|^2) / 4
-// would cancel for small particles, where |a_1| >> |b_1|).
-// qext, qsca and the asymmetry sum are accumulated in FP32 with Kahan
-// compensation (the accumulated rounding then stays at the FP32 unit
-// roundoff whatever nmax is, and the terms do not cancel in the PSD-weighted
-// bulk values); the
-// back-scattering sum sum (2n+1)(-1)^n (a_n - b_n) cancels strongly for
-// large particles and stays FP64 from the FP64 d_n.
+// 1/c (c > 0) in FP64 from an FP32 seed and two Newton steps for the
+// reciprocal (e = 1 - c y, y <- y + y e; the error squares at each step, so
+// 2^-24 becomes ~1 ulp); values outside the FP32 normal range take the
+// IEEE division.
+__device__ __forceinline__ double rcp_newton(double c)
+{
+    if (!(c > 1e-30 && c < 1e30)) return 1.0 / c;
+    double y = (double)__frcp_rn((float)c);
+    double e = fma(-c, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-c, y, 1.0);
+    return fma(y, e, y);
+}
+
+// N / (N - i M) in FP32 for N = (nr, ni), M = (mr, mi), with both scaled by
+// the denominator's largest component (no overflow of |q|^2 for any size).
+__device__ __forceinline__ float2 mie_ratio_f32(float nr, float ni, float mr, float mi)
+{
+    float qr = nr + mi, qi = ni - mr;
+    const float s = __frcp_rn(fmaxf(fabsf(qr), fabsf(qi)));
+    qr *= s;
+    qi *= s;
+    nr *= s;
+    ni *= s;
+    const float inv = __frcp_rn(fmaf(qr, qr, qi * qi));
+    return make_float2(fmaf(nr, qr, ni * qi) * inv, fmaf(ni, qr, -nr * qi) * inv);
+}
+
 __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 {
     const float y = v - comp;
@@ -55,44 +71,104 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
     sum = t;
 }
 
+// The homogeneous recurrences of homog_core (pymiecoated/mie_coeffs.py:132-180)
+// with FP64 kept where stability needs it:
+//   * the downward D_n recurrence (its reciprocal by rcp_newton),
+//   * the real parts of N = D~ psi_n - psi_{n-1} and M = D~ chi_n - chi_{n-1}
+//     (D~ = D/m + n/x or D m + n/x), which cancel -- N for small x, both once
+//     psi and chi oscillate (n < x);
+// and the rest in FP32: D~ imaginary parts, the products N.im, M.im and the
+// ratio a = N / (N - i M).  Coefficients go to emit(k, a, b) from k = nmax
+// down to 1.  row1 / rowf: psi_n, chi_n of x (FP64 / FP32) at [n - 1].
+// Emulated against the FP64 recurrences for x in [1e-3, 650] and the
+// benchmark indices: within 2.2e-7 of each instance's largest coefficient.
+template <class Emit>
+__device__ __forceinline__ void homog_core_mixed(double x, double xinv, double sx, double cxv, const HomogIndex &h,
+                                                 const double2 *__restrict__ row1, const float2 *__restrict__ rowf,
+                                                 int nmax, Emit &emit)
+{
+    const cplx m = h.m, minv = h.minv;
+    const float mfr = (float)m.re, mfi = (float)m.im, mifr = (float)minv.re, mifi = (float)minv.im;
+    const double az = h.azm * x;
+    const int nmx = (int)rint(fmax((double)nmax, az) + 16.0);
+    const cplx zinv = h.zminv * xinv;
+    // warm-up steps above nmax: as homog_core
+    int warm = nmx - 1 - nmax;
+    if (az < 0.5 * (nmax + 1)) {
+        const float q = 2.f * logf((2.f * (float)(nmax + 1) + 1.f) / (float)az);
+        const int need = (int)ceilf(39.2f / q) + 2;
+        if (need < warm) warm = need;
+    }
+    cplx D = cx(0.0, 0.0);
+    for (int k = nmax + warm; k > nmax; --k) {
+        const cplx r = zinv * (double)(k + 1);
+        const cplx w = D + r;
+        const double iw = rcp_newton(abs2(w));
+        D = cx(fma(-w.re, iw, r.re), fma(w.im, iw, r.im));   // r - 1/w
+    }
+    cplx rk = zinv * (double)(nmax + 1);   // r_nmax = (nmax+1)/z
+    cplx w = D + rk;                        // D_{nmax+1} + r_nmax
+    double iw = rcp_newton(abs2(w));
+    double2 pn = row1[nmax - 1];
+    float2 pnf = rowf[nmax - 1];
+    for (int k = nmax; k >= 1; --k) {
+        D = cx(fma(-w.re, iw, rk.re), fma(w.im, iw, rk.im));   // D_k
+        const double dk = (double)k;
+        rk = zinv * dk;                                          // r_{k-1} = k/z
+        if (k > 1) {
+            w = D + rk;
+            iw = rcp_newton(abs2(w));
+        }
+        const double2 pm = (k > 1) ? row1[k - 2] : make_double2(sx, cxv);
+        const float2 pmf = (k > 1) ? rowf[k - 2] : make_float2((float)sx, (float)cxv);
+        const double nx = dk * xinv;
+        const double dar = fma(D.re, minv.re, fma(-D.im, minv.im, nx));   // Re(D/m) + k/x
+        const double dbr = fma(D.re, m.re, fma(-D.im, m.im, nx));         // Re(D m) + k/x
+        const float nar = (float)fma(dar, pn.x, -pm.x), nbr = (float)fma(dbr, pn.x, -pm.x);
+        const float mar = (float)fma(dar, pn.y, -pm.y), mbr = (float)fma(dbr, pn.y, -pm.y);
+        const float Dr = (float)D.re, Di = (float)D.im;
+        const float dai = fmaf(Dr, mifi, Di * mifr), dbi = fmaf(Dr, mfi, Di * mfr);
+        const float2 a = mie_ratio_f32(nar, dai * pnf.x, mar, dai * pnf.y);
+        const float2 b = mie_ratio_f32(nbr, dbi * pnf.x, mbr, dbi * pnf.y);
+        emit(k, a, b);
+        pn = pm;
+        pnf = pmf;
+    }
+}
+
+// Emits FP32 (c, d) = (a + b, a - b) and accumulates the efficiency sums of
+// pymiecoated/mie_props.py:28-70 from the FP32 a_n, b_n with Kahan
+// compensation (the accumulated rounding stays at the FP32 unit roundoff
+// whatever nmax is):
+//   ext = sum (2n+1) Re(a + b),  sca = sum (2n+1)(|a|^2 + |b|^2),
+//   asy = sum n(n+2)/(n+1) Re(a_n a*_{n+1} + b_n b*_{n+1}) + (2n+1)/(n(n+1)) Re(a_n b*_n),
+//   qb  = sum (2n+1)(-1)^n (a_n - b_n).
 struct EmitMixed {
     float4 *cf;
     float amax;
-    float ext, sca, asy;
-    float ext_c, sca_c, asy_c;   // Kahan compensations
-    double qbr, qbi;
-    float4 prev;         // (c, d) of order n+1 (zero above nmax)
-    float inv_n1;        // 1/(n+1)
-    __device__ __forceinline__ void operator()(int k, cplx a, cplx b) {
-        const double dr = a.re - b.re, di = a.im - b.im;
-        const float4 q = make_float4((float)(a.re + b.re), (float)(a.im + b.im), (float)dr, (float)di);
+    float ext, sca, asy, qbr, qbi;
+    float ext_c, sca_c, asy_c, qbr_c, qbi_c;   // Kahan compensations
+    float2 pa, pb;                             // a, b of order n+1 (zero above nmax)
+    float inv_n1;                              // 1/(n+1)
+    __device__ __forceinline__ void operator()(int k, float2 a, float2 b) {
+        const float4 q = make_float4(a.x + b.x, a.y + b.y, a.x - b.x, a.y - b.y);
         cf[k - 1] = q;
         amax = fmaxf(amax, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
         const float fk = (float)k;
         const float cn = 2.f * fk + 1.f;
-        const float inv_n = 1.f / fk;
-        const float c2 = q.x * q.x + q.y * q.y, d2v = q.z * q.z + q.w * q.w;
+        const float inv_n = __frcp_rn(fk);
         kahan(ext, ext_c, cn * q.x);
-        kahan(sca, sca_c, cn * 0.5f * (c2 + d2v));
-        // Re(a b*) from FP64 a, b: (|c|^2 - |d|^2) / 4 cancels when |a| >> |b|
-        const float rab = (float)fma(a.re, b.re, a.im * b.im);
-        kahan(asy, asy_c, ((fk + 1.f) - inv_n1) * 0.5f * (q.x * prev.x + q.y * prev.y + q.z * prev.z + q.w * prev.w) +
-                              (inv_n + inv_n1) * rab);
-        const double sg = (double)((k & 1) ? -(2 * k + 1) : (2 * k + 1));   // (2k+1)(-1)^k
-        qbr = fma(sg, dr, qbr);
-        qbi = fma(sg, di, qbi);
-        prev = q;
+        kahan(sca, sca_c, cn * (fmaf(a.x, a.x, a.y * a.y) + fmaf(b.x, b.x, b.y * b.y)));
+        const float up = fmaf(a.x, pa.x, fmaf(a.y, pa.y, fmaf(b.x, pb.x, b.y * pb.y)));
+        const float rab = fmaf(a.x, b.x, a.y * b.y);
+        kahan(asy, asy_c, ((fk + 1.f) - inv_n1) * up + (inv_n + inv_n1) * rab);
+        const float sg = (k & 1) ? -cn : cn;   // (2k+1)(-1)^k
+        kahan(qbr, qbr_c, sg * q.z);
+        kahan(qbi, qbi_c, sg * q.w);
+        pa = a;
+        pb = b;
         inv_n1 = inv_n;
     }
-};
-
-// The homogeneous recurrences without the FP64 efficiency sums (they are
-// accumulated by EmitMixed): same D_n, psi/chi and a_n/b_n arithmetic as
-// homog_instance.
-struct NoSums {
-    static constexpr bool needs_inv_n = false;
-    __device__ __forceinline__ void init() {}
-    __device__ __forceinline__ void add_rcp(int, cplx, cplx, double, double) {}
 };
 
 __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
@@ -115,30 +191,96 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_i
     EmitMixed emit;
     emit.cf = cf + c;
     emit.amax = 0.f;
-    emit.ext = emit.sca = emit.asy = 0.f;
-    emit.ext_c = emit.sca_c = emit.asy_c = 0.f;
-    emit.qbr = emit.qbi = 0.0;
-    emit.prev = make_float4(0.f, 0.f, 0.f, 0.f);
-    emit.inv_n1 = 1.f / (float)(nmax + 1);
-    NoSums ns;
-    homog_core(x, rc.z, rc.x, rc.y, h, v.pc + o, nmax, emit, ns);
+    emit.ext = emit.sca = emit.asy = emit.qbr = emit.qbi = 0.f;
+    emit.ext_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
+    emit.pa = emit.pb = make_float2(0.f, 0.f);
+    emit.inv_n1 = __frcp_rn((float)(nmax + 1));
+    homog_core_mixed(x, rc.z, rc.x, rc.y, h, v.pc + o, v.pcf + o, nmax, emit);
     const double iy2 = rc.z * rc.z;   // 1 / x^2
-    const double qext = 2.0 * (double)emit.ext * iy2;
-    const double qsca = 2.0 * (double)emit.sca * iy2;
+    const double qext = 2.0 * ((double)emit.ext - (double)emit.ext_c) * iy2;
+    const double sca = (double)emit.sca - (double)emit.sca_c;
+    const double qsca = 2.0 * sca * iy2;
+    const double qr = (double)emit.qbr - (double)emit.qbr_c, qi = (double)emit.qbi - (double)emit.qbi_c;
     double *o4 = v.eff4 + t * 4;
     o4[0] = qext;
     o4[1] = qsca;
-    o4[2] = (emit.qbr * emit.qbr + emit.qbi * emit.qbi) * iy2;
-    o4[3] = 2.0 * (double)emit.asy / (double)emit.sca;   // 4/x^2 asy / qsca
+    o4[2] = (qr * qr + qi * qi) * iy2;
+    o4[3] = 2.0 * ((double)emit.asy - (double)emit.asy_c) / sca;   // 4/x^2 asy / qsca
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
+}
+
+// FP32 copy of the psi/chi rows for the FP32 parts of the mixed recurrences.
+__global__ void k_f64x2_to_f32x2(int64_t n, const double2 *__restrict__ src, float2 *__restrict__ dst)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double2 v = src[i];
+        dst[i] = make_float2((float)v.x, (float)v.y);
+    }
 }
 
 __global__ void k_fill_int(int n, int *p, int val)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = val;
+}
+
+// ---------------------------------------------------------------------------
+// A operand of the contraction: FP32 (c, d) -> FP16 hi/lo scaled by
+// 2^(13 - e_i), written once per (unit, 64-size tile, 16-order chunk) as a
+// 16 KB block in the no-swizzle K-major shared-memory layout
+//   [matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
+// (rows 2 i, 2 i + 1 = Re, Im of size i), so that the contraction loads it
+// with one bulk copy per angle block.  Block = (unit, tile); thread =
+// (size i, 8-order half kg); orders past an instance's nmax are zero.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_tab_split_a(TabView v, int ntiles, const float4 *__restrict__ cf,
+                                                     const int *__restrict__ eexp,
+                                                     const int *__restrict__ tile_cbase,
+                                                     const int64_t *__restrict__ unit_cbase, uint8_t *__restrict__ asplit)
+{
+    const int64_t unit = blockIdx.x / ntiles;
+    const int tile = (int)(blockIdx.x % ntiles);
+    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+    const int le = v.le(lam);
+    const int64_t *off = v.off + (int64_t)le * v.n_size;
+    const int *tcb = tile_cbase + (size_t)le * (ntiles + 1);
+    const int nc = tcb[tile + 1] - tcb[tile];
+    uint8_t *dst = asplit + (size_t)(unit_cbase[unit] + tcb[tile]) * 16384;
+    const int t0 = 64 * tile, ntile = min(64, v.n_size - t0);
+    const int ia = threadIdx.x >> 1, kg = threadIdx.x & 1;
+    const bool has = ia < ntile;
+    const int64_t pa = has ? off[t0 + ia] : 0;
+    const int nma = has ? (int)(off[t0 + ia + 1] - pa) : 0;
+    const float4 *src = cf + (v.unit_base[unit] - off[0]) + pa;
+    const float sc = has ? ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - eexp[unit * v.n_size + t0 + ia]))) : 0.f;
+    const int r0 = 2 * ia, r1 = 2 * ia + 1;
+    const uint32_t o0 = (kg * 16 + (r0 >> 3)) * 128 + (r0 & 7) * 16;
+    const uint32_t o1 = (kg * 16 + (r1 >> 3)) * 128 + (r1 & 7) * 16;
+    for (int j = 0; j < nc; ++j) {
+        __half ch[4][8], cl[4][8];   // [c.re, c.im, d.re, d.im][order]
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+            const int k = 16 * j + 8 * kg + jj;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < nma) q = src[k];
+            split_f16(q.x * sc, ch[0][jj], cl[0][jj]);
+            split_f16(q.y * sc, ch[1][jj], cl[1][jj]);
+            split_f16(q.z * sc, ch[2][jj], cl[2][jj]);
+            split_f16(q.w * sc, ch[3][jj], cl[3][jj]);
+        }
+        uint8_t *blk = dst + (size_t)j * 16384;
+        *(uint4 *)(blk + 0 * 4096 + o0) = *(uint4 *)ch[0];
+        *(uint4 *)(blk + 0 * 4096 + o1) = *(uint4 *)ch[1];
+        *(uint4 *)(blk + 1 * 4096 + o0) = *(uint4 *)cl[0];
+        *(uint4 *)(blk + 1 * 4096 + o1) = *(uint4 *)cl[1];
+        *(uint4 *)(blk + 2 * 4096 + o0) = *(uint4 *)ch[2];
+        *(uint4 *)(blk + 2 * 4096 + o1) = *(uint4 *)ch[3];
+        *(uint4 *)(blk + 3 * 4096 + o0) = *(uint4 *)cl[2];
+        *(uint4 *)(blk + 3 * 4096 + o1) = *(uint4 *)cl[3];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -189,6 +331,38 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 
 // ---------------------------------------------------------------------------
 // The tensor-core contraction with the fused epilogue.
+//
+// Accuracy of the FP32 accumulation.  Measured on GB300 with a two-MMA probe
+// (kind::f16, FP32 accumulator): inside one MMA the 16 products and the
+// accumulator are aligned to the largest of them, every addend keeps only
+// the bits down to a quarter of that value's FP32 ulp (0.5 survives next to
+// 2^24, 0.25 does not), and the sum is truncated toward zero.  A long chain
+// of MMAs into one accumulator therefore loses a fraction of an ulp per
+// product, always in the same direction: at forward angles, where all terms
+// of S+ add coherently, x = 628 gave 1.4e-6 of P11.  Here every tile's
+// orders are split into windows of TC_WIN 16-order chunks; each window
+// starts a fresh accumulator, adds the two cross products of its orders
+// (C_hi P_lo, C_lo P_hi, 2^-11 of the result) while the accumulator is small
+// and then the C_hi P_hi products, and the epilogue adds the windows in FP32
+// registers with round-to-nearest.  Emulating the measured rule puts the
+// bulk P11 error at x = 628 near 2.6e-7 this way.
+//
+// Pipeline (one CTA per SM, persistent, 10 warps):
+//   warps 0-7   epilogue: TMEM -> window sums -> Mueller -> PSD-weighted sums
+//   warp 8      MMA issue (one thread)
+//   warp 9      producer (one thread): bulk copies of the split A operand
+//               (k_tab_split_a) and of B orders > 16 into a TC_NS-stage
+//               shared-memory ring
+// Angles go in blocks of 64 (MMA N = 64); TMEM holds TC_NSETS accumulator
+// sets (S+ 64 columns | S- 64 columns), so the MMAs run up to four windows
+// ahead of the epilogue.  The B chunk of orders 1..16 stays resident for up
+// to TC_B0_SLOTS angle blocks (loaded once: it is the same for every unit;
+// 84% of the sulfate-like table's 64-size tiles need no other order); with
+// more blocks one slot is reloaded at every block change.  mbarriers: stage
+// full/empty, resident-B full/empty, accumulator-set full/empty.  Every wait
+// is bounded and also ends when another role has raised the block's abort
+// flag; role-wide decisions are taken by one thread and shared through a
+// named barrier, so each role leaves its loops uniformly.
 // ---------------------------------------------------------------------------
 struct TcArgs {
     TabView v;
@@ -198,54 +372,91 @@ struct TcArgs {
     const __half *bt;
     int n_pad, k_pad;
     const int *unit_order;
-    int *counter;
+    const uint8_t *asplit;       // split A operand (k_tab_split_a)
+    const int *tile_cbase;       // [n_le][ntiles + 1]
+    const int64_t *unit_cbase;   // [n_units]
+    int ntiles;
     int *flags;
 };
 
-// shared-memory carve (bytes)
-#define TC_A_BYTES (TC_KC * 128 * 2)                   // one A matrix chunk: 8 KB
-#define TC_B_BYTES (TC_KC * TC_NBLK * 2)               // one B matrix chunk: 12 KB
+#define TC_KC16 16                                     // orders per chunk (one MMA K step)
+#define TC_NS 4                                        // ring stages
+#define TC_WIN 3                                       // chunks per accumulation window (<= TC_NS)
+#define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
+#define TC_B0_SLOTS 4                                  // resident B chunks (angle blocks)
+#define TC_A16_MAT (TC_KC16 * 128 * 2)                 // one A matrix of a chunk: 4 KB
+#define TC_A16_BYTES (4 * TC_A16_MAT)                  // C_hi C_lo D_hi D_lo: 16 KB
+#define TC_B16_MAT (TC_KC16 * TC_NBLK * 2)             // one B matrix of a chunk: 2 KB
+#define TC_B16_BYTES (4 * TC_B16_MAT)                  // P_hi P_lo Q_hi Q_lo: 8 KB
+#define TC_STAGE_BYTES (TC_A16_BYTES + TC_B16_BYTES)   // 24 KB
 #define TC_STAGE_PITCH 66                              // 64 columns + 2: conflict-free pair writes
 #define TC_STAGE_FLOATS (4 * TC_INST * TC_STAGE_PITCH) // Mueller staging [k][size][col]: 66 KB
-#define TC_SMEM_BYTES (4 * TC_A_BYTES + 8 * TC_B_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
+#define TC_EPI_THREADS 256
+#define TC_THREADS (TC_EPI_THREADS + 64)             // + the MMA warp and the producer warp
+#define TC_SMEM_BYTES                                                                                  \
+    (TC_B0_SLOTS * TC_B16_BYTES + TC_NS * TC_STAGE_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
+#define TC_BAR_EPI 1                                   // named barrier id of the epilogue warps
 
-// One K chunk (TC_KC orders from k0) of angle block blk of the four B
-// matrices into shared memory, [m][kg][ng][8][16 B]; plain 16-byte loads.
-__device__ __forceinline__ void copy_b_chunk(const TcArgs &g, uint8_t *dstbase, int k0, int blk, int tid)
+static_assert(TC_WIN <= TC_NS, "a window's chunks must fit the ring");
+static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
+
+// k-th unit of CTA `cta` among G CTAs: units in decreasing-work order,
+// dealt in a snake (c, then G-1-c) so that every CTA gets a similar mix.
+__device__ __forceinline__ int64_t tc_unit_index(int k, int cta, int G)
 {
-    const int nkg = TC_KC / 8, nng = TC_NBLK / 8, ngt = g.n_pad / 8;
+    return (int64_t)k * G + ((k & 1) ? (G - 1 - cta) : cta);
+}
+
+// Chunk j (orders 16 j + 1 .. 16 j + 16) of angle block blk of the four B
+// matrices, global [m][k/8][angle/8][8][8] -> shared [m][kg][ng][8][8]: per
+// (m, kg) one contiguous run of 8 core matrices (1 KB).  One thread; the
+// caller has armed `bar` with the bytes (mbar_arrive_expect_tx).
+__device__ __forceinline__ void tc_copy_b16(const TcArgs &g, uint8_t *dst, int j, int blk, uint64_t *bar)
+{
+    const int ngt = g.n_pad / 8, nng = TC_NBLK / 8;
     const size_t mat = (size_t)g.n_pad * g.k_pad;
-    for (int idx = tid; idx < 4 * nkg * nng * 8; idx += TC_THREADS) {
-        const int rr = idx & 7;
-        const int ng = (idx >> 3) % nng;
-        const int kg = ((idx >> 3) / nng) % nkg;
-        const int m = (idx >> 3) / (nng * nkg);
-        const size_t src = m * mat + (((size_t)(k0 / 8 + kg) * ngt + blk * nng + ng) * 64 + rr * 8);
-        const uint32_t dst = m * TC_B_BYTES + (kg * nng + ng) * 128 + rr * 16;
-        *(uint4 *)(dstbase + dst) = *(const uint4 *)(g.bt + src);
-    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int kg = 0; kg < 2; ++kg) {
+            const __half *src = g.bt + m * mat + ((size_t)(2 * j + kg) * ngt + (size_t)blk * nng) * 64;
+            bulk_g2s(dst + m * TC_B16_MAT + kg * nng * 128, src, nng * 128, bar);
+        }
 }
 
 template <int NB>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem;                                     // 4 x TC_A_BYTES
-    uint8_t *sB0 = sA + 4 * TC_A_BYTES;                     // chunk 0 of the angle block, resident
-    uint8_t *sB1 = sB0 + 4 * TC_B_BYTES;                    // later chunks
-    float *stage = (float *)(sB1 + 4 * TC_B_BYTES);         // [4][64][65]
-    float *sw = stage + TC_STAGE_FLOATS;                    // [64 sizes][8 bins]
-    uint64_t *bar = (uint64_t *)(sw + 8 * TC_INST);
-    uint32_t *s_tmem = (uint32_t *)(bar + 1);
-    int *s_unit = (int *)(s_tmem + 1);
-    int *s_abort = s_unit + 1;
+    uint8_t *sB0 = smem;                                            // resident B chunks, orders 1..16
+    uint8_t *sStage = sB0 + TC_B0_SLOTS * TC_B16_BYTES;             // TC_NS x (A 16 KB | B 8 KB)
+    float *stage = (float *)(sStage + TC_NS * TC_STAGE_BYTES);     // Mueller staging [4][64][66]
+    float *sw = stage + TC_STAGE_FLOATS;                            // [64 sizes][8 bins]
+    uint64_t *bars = (uint64_t *)(sw + 8 * TC_INST);
+    uint64_t *full = bars, *empty = bars + TC_NS;
+    uint64_t *b0_full = bars + 2 * TC_NS, *b0_empty = b0_full + 1;
+    uint64_t *acc_full = b0_full + 2, *acc_empty = acc_full + TC_NSETS, *drain = acc_empty + TC_NSETS;
+    uint32_t *s_tmem = (uint32_t *)(drain + 1);
+    volatile int *s_abort = (volatile int *)(s_tmem + 1);
+    volatile int *s_epi_go = s_abort + 1;    // [2] epilogue: 1 = accumulator set ready, 0 = stop
 
     const TabView &v = g.v;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    int s_blk_loaded = -1;   // angle block whose chunk 0 sits in sB0 (same value in every thread)
+    const int nblocks = g.n_pad / TC_NBLK;
+    const bool reload = nblocks > TC_B0_SLOTS;   // one resident slot, reloaded per block
     if (warp == 0) tmem_alloc(s_tmem, 512);
     if (tid == 0) {
-        mbar_init(bar, 1);
+        for (int i = 0; i < TC_NS; ++i) {
+            mbar_init(full + i, 1);    // the producer's arrival with the copies' bytes
+            mbar_init(empty + i, 1);   // tcgen05.commit
+        }
+        mbar_init(b0_full, 1);
+        mbar_init(b0_empty, 1);
+        for (int i = 0; i < TC_NSETS; ++i) {
+            mbar_init(acc_full + i, 1);
+            mbar_init(acc_empty + i, TC_EPI_THREADS / 32);
+        }
+        mbar_init(drain, 1);
         fence_mbar_init();
         *s_abort = 0;
     }
@@ -253,162 +464,243 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *s_tmem;
-    const uint32_t idesc = idesc_f16_f32(128, TC_NBLK);
-    uint32_t phase = 0;
     const int64_t n_units = (int64_t)v.n_lambda * v.n_rh * v.n_comp;
-    const int nblocks = g.n_pad / TC_NBLK;
+    const int G = gridDim.x, cta = blockIdx.x;
 
-    for (;;) {
-        if (tid == 0) *s_unit = atomicAdd(g.counter, 1);
-        __syncthreads();
-        const int uidx = *s_unit;
-        __syncthreads();
-        if (uidx >= n_units) break;
-        const int64_t unit = g.unit_order[uidx];
-        const int comp = (int)(unit % v.n_comp);
-        const int64_t lr = unit / v.n_comp;
-        const int lam = (int)(lr / v.n_rh);
-        const int le = v.le(lam);
-        const int64_t *off = v.off + (int64_t)le * v.n_size;
-        const int64_t cbase = v.unit_base[unit] - off[0];
-        const float4 *cf = g.cf + cbase;
-        const int *ex = g.eexp + unit * v.n_size;
-        const int E = g.eunit[unit];
-        const int rhi = (int)(lr % v.n_rh);
-        const float *Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
-
-        for (int blk = 0; blk < nblocks; ++blk) {
-            // per-unit sums of this thread's two columns per round as
-            // unevaluated FP32 pairs (hi + lo, two-sum)
-            float uh[TC_ROUNDS][2][NB], ul[TC_ROUNDS][2][NB];
-#pragma unroll
-            for (int r = 0; r < TC_ROUNDS; ++r)
+    if (warp == 8) {
+        // ================= MMA issue =================
+        if (lane == 0) {
+            const uint32_t idesc = idesc_f16_f32(128, TC_NBLK);
+            uint32_t it = 0, item = 0, b0_loads = 0;
+            int prev_blk = -1;
+            bool ok = true;
+            if (!reload) {   // every block's resident chunk, loaded once
+                ok = mbar_wait_or_abort(b0_full, 0, s_abort);
+                b0_loads = 1;
+            }
+            for (int k = 0; ok; ++k) {
+                const int64_t uidx = tc_unit_index(k, cta, G);
+                if (uidx >= n_units) break;
+                const int64_t unit = g.unit_order[uidx];
+                const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+                const int64_t *off = v.off + (int64_t)v.le(lam) * v.n_size;
+                for (int blk = 0; blk < nblocks && ok; ++blk) {
+                    if (reload && blk != prev_blk) {   // the producers reload the resident slot
+                        if (prev_blk >= 0) mma_commit(b0_empty);
+                        if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort)) {
+                            ok = false;
+                            break;
+                        }
+                        ++b0_loads;
+                        prev_blk = blk;
+                    }
+                    const uint32_t aB0 = smem_u32(sB0 + (reload ? 0 : blk) * TC_B16_BYTES);
+                    for (int t0 = 0; t0 < v.n_size && ok; t0 += TC_INST) {
+                        const int ntile = min(TC_INST, v.n_size - t0);
+                        const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
+                        const int nc = (kt + TC_KC16 - 1) / TC_KC16;
+                        for (int w0 = 0; w0 < nc && ok; w0 += TC_WIN) {
+                            const int nj = min(TC_WIN, nc - w0);
+                            const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
+                            if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort)) {
+                                ok = false;
+                                break;
+                            }
+                            for (int j = 0; j < nj && ok; ++j) {
+                                const uint32_t c = it + j;
+                                ok = mbar_wait_or_abort(full + c % TC_NS, (c / TC_NS) & 1u, s_abort);
+                            }
+                            if (!ok) break;
+                            tc_fence_after();
+                            const uint32_t d = tmem + set * 128;   // S+ at d, S- at d + 64
+                            for (int pass = 0; pass < 2; ++pass) {
+                                for (int j = 0; j < nj; ++j) {
+                                    const uint32_t c = it + j;
+                                    const uint32_t aA = smem_u32(sStage + (c % TC_NS) * TC_STAGE_BYTES);
+                                    const uint32_t aB = (w0 + j) == 0 ? aB0 : aA + TC_A16_BYTES;
+                                    // A: LBO (K step of 8 orders) = 16 core matrices; B: 8
+                                    const uint64_t a_chi = smem_desc(aA + 0 * TC_A16_MAT, 16 * 128, 128);
+                                    const uint64_t a_dhi = smem_desc(aA + 2 * TC_A16_MAT, 16 * 128, 128);
+                                    const uint64_t b_phi = smem_desc(aB + 0 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
+                                    const uint64_t b_qhi = smem_desc(aB + 2 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
+                                    if (pass == 0) {   // cross products: small accumulator
+                                        const uint64_t a_clo = smem_desc(aA + 1 * TC_A16_MAT, 16 * 128, 128);
+                                        const uint64_t a_dlo = smem_desc(aA + 3 * TC_A16_MAT, 16 * 128, 128);
+                                        const uint64_t b_plo =
+                                            smem_desc(aB + 1 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
+                                        const uint64_t b_qlo =
+                                            smem_desc(aB + 3 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
+                                        mma_f16(d, a_chi, b_plo, idesc, j == 0 ? 0u : 1u);
+                                        mma_f16(d, a_clo, b_phi, idesc, 1u);
+                                        mma_f16(d + 64, a_dhi, b_qlo, idesc, j == 0 ? 0u : 1u);
+                                        mma_f16(d + 64, a_dlo, b_qhi, idesc, 1u);
+                                    } else {
+                                        mma_f16(d, a_chi, b_phi, idesc, 1u);
+                                        mma_f16(d + 64, a_dhi, b_qhi, idesc, 1u);
+                                        mma_commit(empty + c % TC_NS);   // stage free when its MMAs are done
+                                    }
+                                }
+                            }
+                            it += nj;
+                            mma_commit(acc_full + set);
+                            ++item;
+                        }
+                    }
+                }
+            }
+            if (!ok) {
+                *s_abort = 1;
+                atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
+            }
+            // every issued MMA has finished before TMEM is released
+            mma_commit(drain);
+            if (!mbar_wait(drain, 0)) atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
+        }
+        __syncwarp();
+    } else if (warp == 9) {
+        // ================= producer: bulk copies (one thread) =================
+        if (lane == 0) {
+            uint32_t it = 0, b0_loads = 0;
+            int prev_blk = -1;
+            uint64_t *last_tx = nullptr;   // barrier of the last bulk copy, and its phase
+            uint32_t last_tx_phase = 0;
+            bool ok = true;
+            if (!reload) {
+                mbar_arrive_expect_tx(b0_full, (uint32_t)(nblocks * TC_B16_BYTES));
+                for (int b = 0; b < nblocks; ++b) tc_copy_b16(g, sB0 + b * TC_B16_BYTES, 0, b, b0_full);
+                last_tx = b0_full;
+                last_tx_phase = 0;
+            }
+            for (int k = 0; ok; ++k) {
+                const int64_t uidx = tc_unit_index(k, cta, G);
+                if (uidx >= n_units) break;
+                const int64_t unit = g.unit_order[uidx];
+                const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+                const int *tcb = g.tile_cbase + (size_t)v.le(lam) * (g.ntiles + 1);
+                const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * TC_A16_BYTES;
+                for (int blk = 0; blk < nblocks && ok; ++blk) {
+                    if (reload && blk != prev_blk) {
+                        if (prev_blk >= 0 && !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(b0_full, TC_B16_BYTES);
+                        tc_copy_b16(g, sB0, 0, blk, b0_full);
+                        last_tx = b0_full;
+                        last_tx_phase = b0_loads & 1u;
+                        ++b0_loads;
+                        prev_blk = blk;
+                    }
+                    for (int tile = 0; tile < g.ntiles && ok; ++tile) {
+                        const int nc = tcb[tile + 1] - tcb[tile];
+                        for (int j = 0; j < nc; ++j) {
+                            const uint32_t c = it++;
+                            const int st = (int)(c % TC_NS);
+                            uint8_t *sA = sStage + st * TC_STAGE_BYTES;
+                            if (c >= TC_NS && !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort)) {
+                                ok = false;
+                                break;
+                            }
+                            mbar_arrive_expect_tx(full + st, TC_A16_BYTES + (j > 0 ? TC_B16_BYTES : 0));
+                            bulk_g2s(sA, ua + (size_t)(tcb[tile] + j) * TC_A16_BYTES, TC_A16_BYTES, full + st);
+                            if (j > 0) tc_copy_b16(g, sA + TC_A16_BYTES, j, blk, full + st);
+                            last_tx = full + st;
+                            last_tx_phase = (c / TC_NS) & 1u;
+                        }
+                    }
+                }
+            }
+            if (!ok || *s_abort) {
+                *s_abort = 1;
+                atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
+                // a bulk copy still in flight must land before shared memory is released
+                if (last_tx) mbar_wait(last_tx, last_tx_phase, 1u << 20);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ================= epilogue (warps 0-7) =================
+        uint32_t item = 0;
+        bool ok = true;
+        const int q = warp & 3, half = warp >> 2;
+        const int il = 16 * q + (lane >> 1);
+        const bool odd = lane & 1;
+        const int kk = warp >> 1, cg = warp & 1, hh = lane >> 4, cp = lane & 15;
+        for (int k = 0; ok; ++k) {
+            const int64_t uidx = tc_unit_index(k, cta, G);
+            if (uidx >= n_units) break;
+            const int64_t unit = g.unit_order[uidx];
+            const int comp = (int)(unit % v.n_comp);
+            const int64_t lr = unit / v.n_comp;
+            const int lam = (int)(lr / v.n_rh);
+            const int64_t *off = v.off + (int64_t)v.le(lam) * v.n_size;
+            const int *ex = g.eexp + unit * v.n_size;
+            const int E = g.eunit[unit];
+            const int rhi = (int)(lr % v.n_rh);
+            const float *Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
+            for (int blk = 0; blk < nblocks && ok; ++blk) {
+                // per-unit sums of this thread's two columns as unevaluated FP32
+                // pairs (hi + lo, two-sum)
+                float uh[2][NB], ul[2][NB];
 #pragma unroll
                 for (int c = 0; c < 2; ++c)
 #pragma unroll
-                    for (int b = 0; b < NB; ++b) uh[r][c][b] = ul[r][c][b] = 0.f;
-            if (blk != s_blk_loaded) {   // uniform: chunk 0 of this angle block into sB0
-                copy_b_chunk(g, sB0, 0, blk, tid);
-                s_blk_loaded = blk;
-            }
-
-            for (int t0 = 0; t0 < v.n_size; t0 += TC_INST) {
-                const int ntile = min(TC_INST, v.n_size - t0);
-                const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);   // largest nmax of the tile
-                const int ktile = (kt + TC_KC - 1) / TC_KC * TC_KC;
-                // scaled weights of the tile
-                for (int idx = tid; idx < 8 * TC_INST; idx += TC_THREADS) {
-                    const int b = idx & 7, i = idx >> 3;
-                    float w = 0.f;
-                    if (i < ntile && b < v.n_bin && b < NB)
-                        w = ldexpf(Wb[(size_t)b * v.n_comp * v.n_size + t0 + i], max(-300, 2 * (ex[t0 + i] - E)));
-                    sw[idx] = w;
-                }
-                // A-row data of this thread: size i = tid / 4, orders 8 (tid % 4) .. + 8 of each chunk
-                const int ia = tid >> 2, seg = tid & 3;
-                const bool has = ia < ntile;
-                const int64_t pa = has ? off[t0 + ia] : 0;
-                const int nma = has ? (int)(off[t0 + ia + 1] - pa) : 0;
-                const float sc = has ? ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - ex[t0 + ia]))) : 0.f;
-
-                for (int k0 = 0; k0 < ktile; k0 += TC_KC) {
-                    // ---- A: FP32 (c, d) -> scaled FP16 hi/lo, rows 2i (Re), 2i+1 (Im)
-                    {
-                        __half ch[4][8], cl[4][8];   // [c.re, c.im, d.re, d.im][order]
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const int k = k0 + 8 * seg + j;
-                            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                            if (k < nma) q = cf[pa + k];
-                            split_f16(q.x * sc, ch[0][j], cl[0][j]);
-                            split_f16(q.y * sc, ch[1][j], cl[1][j]);
-                            split_f16(q.z * sc, ch[2][j], cl[2][j]);
-                            split_f16(q.w * sc, ch[3][j], cl[3][j]);
-                        }
-                        // core matrix (kg = seg, mg = row / 8): offset (kg * 16 + mg) * 128 + (row % 8) * 16
-                        const int r0 = 2 * ia, r1 = 2 * ia + 1;
-                        const uint32_t o0 = (seg * 16 + (r0 >> 3)) * 128 + (r0 & 7) * 16;
-                        const uint32_t o1 = (seg * 16 + (r1 >> 3)) * 128 + (r1 & 7) * 16;
-                        // matrices: 0 C_hi, 1 C_lo, 2 D_hi, 3 D_lo
-                        *(uint4 *)(sA + 0 * TC_A_BYTES + o0) = *(uint4 *)ch[0];
-                        *(uint4 *)(sA + 0 * TC_A_BYTES + o1) = *(uint4 *)ch[1];
-                        *(uint4 *)(sA + 1 * TC_A_BYTES + o0) = *(uint4 *)cl[0];
-                        *(uint4 *)(sA + 1 * TC_A_BYTES + o1) = *(uint4 *)cl[1];
-                        *(uint4 *)(sA + 2 * TC_A_BYTES + o0) = *(uint4 *)ch[2];
-                        *(uint4 *)(sA + 2 * TC_A_BYTES + o1) = *(uint4 *)ch[3];
-                        *(uint4 *)(sA + 3 * TC_A_BYTES + o0) = *(uint4 *)cl[2];
-                        *(uint4 *)(sA + 3 * TC_A_BYTES + o1) = *(uint4 *)cl[3];
+                    for (int b = 0; b < NB; ++b) uh[c][b] = ul[c][b] = 0.f;
+                for (int t0 = 0; t0 < v.n_size && ok; t0 += TC_INST) {
+                    const int ntile = min(TC_INST, v.n_size - t0);
+                    const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
+                    const int nwin = ((kt + TC_KC16 - 1) / TC_KC16 + TC_WIN - 1) / TC_WIN;
+                    // scaled weights of the tile (the previous tile's readers have
+                    // passed the last epilogue barrier of its reduction)
+                    for (int idx = tid; idx < 8 * TC_INST; idx += TC_EPI_THREADS) {
+                        const int b = idx & 7, i = idx >> 3;
+                        float w = 0.f;
+                        if (i < ntile && b < v.n_bin && b < NB)
+                            w = ldexpf(Wb[(size_t)b * v.n_comp * v.n_size + t0 + i], max(-300, 2 * (ex[t0 + i] - E)));
+                        sw[idx] = w;
                     }
-                    // ---- B: chunk 0 is resident; later chunks go to sB1
-                    if (k0 > 0) copy_b_chunk(g, sB1, k0, blk, tid);
-                    uint8_t *sB = k0 > 0 ? sB1 : sB0;
-                    fence_proxy_async_smem();
-                    __syncthreads();
-                    if (tid == 0) {
+                    // window sums of S+ and S- (Re/Im of this lane's row, 32 columns)
+                    float rp[32], rm[32];
+                    for (int w = 0; w < nwin; ++w) {
+                        const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
+                        if (tid == 0)
+                            s_epi_go[item & 1] = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
+                        named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
+                        if (!s_epi_go[item & 1]) {
+                            ok = false;
+                            break;
+                        }
                         tc_fence_after();
-                        const uint32_t aA = smem_u32(sA), aB = smem_u32(sB);
+                        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * half;
+                        if (w == 0) {
+                            tmem_ld32(ta, rp);
+                            tmem_ld32(ta + 64, rm);
+                        } else {
+                            float t[32];
+                            tmem_ld32(ta, t);
 #pragma unroll
-                        for (int ks = 0; ks < TC_KC / 16; ++ks) {
-                            const uint32_t acc = (k0 > 0 || ks > 0) ? 1u : 0u;
-                            // A: LBO (K step of 8) = 16 core matrices, SBO (8 rows) = 128 B
-                            const uint32_t ao = ks * 2 * 16 * 128;
-                            const uint32_t bo = ks * 2 * (TC_NBLK / 8) * 128;
-                            const uint64_t a_chi = smem_desc(aA + 0 * TC_A_BYTES + ao, 16 * 128, 128);
-                            const uint64_t a_clo = smem_desc(aA + 1 * TC_A_BYTES + ao, 16 * 128, 128);
-                            const uint64_t a_dhi = smem_desc(aA + 2 * TC_A_BYTES + ao, 16 * 128, 128);
-                            const uint64_t a_dlo = smem_desc(aA + 3 * TC_A_BYTES + ao, 16 * 128, 128);
-                            const uint64_t b_phi = smem_desc(aB + 0 * TC_B_BYTES + bo, (TC_NBLK / 8) * 128, 128);
-                            const uint64_t b_plo = smem_desc(aB + 1 * TC_B_BYTES + bo, (TC_NBLK / 8) * 128, 128);
-                            const uint64_t b_qhi = smem_desc(aB + 2 * TC_B_BYTES + bo, (TC_NBLK / 8) * 128, 128);
-                            const uint64_t b_qlo = smem_desc(aB + 3 * TC_B_BYTES + bo, (TC_NBLK / 8) * 128, 128);
-                            mma_f16(tmem, a_chi, b_phi, idesc, acc);
-                            mma_f16(tmem, a_chi, b_plo, idesc, 1u);
-                            mma_f16(tmem, a_clo, b_phi, idesc, 1u);
-                            mma_f16(tmem + 256, a_dhi, b_qhi, idesc, acc);
-                            mma_f16(tmem + 256, a_dhi, b_qlo, idesc, 1u);
-                            mma_f16(tmem + 256, a_dlo, b_qhi, idesc, 1u);
+                            for (int i = 0; i < 32; ++i) rp[i] += t[i];
+                            tmem_ld32(ta + 64, t);
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) rm[i] += t[i];
                         }
-                        mma_commit(bar);
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(acc_empty + set);
+                        ++item;
                     }
-                    // the MMAs read shared memory until the commit arrives; a wait
-                    // that runs out aborts the whole block (uniformly, after a barrier)
-                    if (!mbar_wait(bar, phase)) {
-                        *s_abort = 1;
-                        atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
-                    }
-                    phase ^= 1u;
-                    tc_fence_after();
-                    __syncthreads();
-                    if (*s_abort) goto done;
-                }
-                // ---- epilogue: S+/S- -> Mueller -> weighted sums over the tile's sizes.
-                // Mueller phase: warp (q = TMEM lane quarter, half = warp / 4)
-                // holds rows 32 q .. + 31 (sizes 16 q .. + 15, Re/Im lane
-                // pairs) for 32 columns.  Lanes exchange one value per column
-                // pair so that the even lane forms column 2p and the odd lane
-                // column 2p + 1 (no idle lanes).
-                // Reduction phase: warp w sums element kk = w / 2, columns
-                // 32 (w % 2) + 2 cp + {0, 1} (cp = lane % 16) over sizes
-                // 32 h .. + 31 (h = lane / 16) for every bin; the two size
-                // halves meet by a shuffle.
-                const int q = warp & 3;
-                const int il = 16 * q + (lane >> 1);
-                const bool odd = lane & 1;
-                const int kk = warp >> 1, cg = warp & 1, hh = lane >> 4, cp = lane & 15;
-#pragma unroll
-                for (int r = 0; r < TC_ROUNDS; ++r) {   // unrolled: uh/ul stay in registers
-                    const int chunk = 2 * r + (warp >> 2);
-                    float sp[32], sm[32];
-                    tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * chunk, sp);
-                    tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 256 + 32 * chunk, sm);
-                    float *strow = stage + il * TC_STAGE_PITCH + 32 * (warp >> 2) + (odd ? 1 : 0);
+                    if (!ok) break;
+                    // Mueller phase: warp (q = TMEM lane quarter, half = warp / 4) holds
+                    // rows 32 q .. + 31 (sizes 16 q .. + 15, Re/Im lane pairs) for 32
+                    // columns; the even lane forms column 2p and the odd lane 2p + 1.
+                    float *strow = stage + il * TC_STAGE_PITCH + 32 * half + (odd ? 1 : 0);
 #pragma unroll
                     for (int pj = 0; pj < 16; ++pj) {
                         const int j0 = 2 * pj, j1 = 2 * pj + 1;
-                        const float rp = __shfl_xor_sync(0xffffffffu, odd ? sp[j0] : sp[j1], 1);
-                        const float rm = __shfl_xor_sync(0xffffffffu, odd ? sm[j0] : sm[j1], 1);
-                        const float pr = odd ? rp : sp[j0], pi = odd ? sp[j1] : rp;
-                        const float mr = odd ? rm : sm[j0], mi = odd ? sm[j1] : rm;
+                        const float xp = __shfl_xor_sync(0xffffffffu, odd ? rp[j0] : rp[j1], 1);
+                        const float xm = __shfl_xor_sync(0xffffffffu, odd ? rm[j0] : rm[j1], 1);
+                        const float pr = odd ? xp : rp[j0], pi = odd ? rp[j1] : xp;
+                        const float mr = odd ? xm : rm[j0], mi = odd ? rm[j1] : xm;
                         const float A2 = pr * pr + pi * pi, B2 = mr * mr + mi * mi;
                         float *st = strow + j0;
                         st[0 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 + B2);
@@ -416,7 +708,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         st[2 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 - B2);
                         st[3 * TC_INST * TC_STAGE_PITCH] = -0.5f * (mr * pi - mi * pr);
                     }
-                    __syncthreads();
+                    named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
+                    // Reduction phase: warp w sums element kk = w / 2 over columns
+                    // 32 (w % 2) + 2 cp + {0, 1} (cp = lane % 16) and sizes 32 h .. + 31
+                    // (h = lane / 16) for every bin; the two halves meet by a shuffle.
                     {
                         float acc[2][NB];
 #pragma unroll
@@ -449,33 +744,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                             for (int b = 0; b < NB; ++b) {
                                 const float a = acc[c][b] + __shfl_xor_sync(0xffffffffu, acc[c][b], 16);
                                 // two-sum: (uh + ul) += a exactly-rounded
-                                const float sum = uh[r][c][b] + a;
-                                const float bp = sum - uh[r][c][b];
-                                ul[r][c][b] += (uh[r][c][b] - (sum - bp)) + (a - bp);
-                                uh[r][c][b] = sum;
+                                const float sum = uh[c][b] + a;
+                                const float bp = sum - uh[c][b];
+                                ul[c][b] += (uh[c][b] - (sum - bp)) + (a - bp);
+                                uh[c][b] = sum;
                             }
                     }
-                    __syncthreads();
+                    named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
                 }
-                tc_fence_before();
-            }
-            // unit results of this angle block: lanes of the first size half
-            // hold the combined sums of (element kk, two columns) per round
-            if ((lane >> 4) == 0) {
-                const int kk = warp >> 1;
-                const double f2 = ldexp(1.0, 2 * (E - SHIFT_BITS));
-#pragma unroll
-                for (int r = 0; r < TC_ROUNDS; ++r) {
+                if (!ok) break;
+                // unit results of this angle block: lanes of the first size half
+                // hold the combined sums of (element kk, two columns)
+                if (hh == 0) {
+                    const double f2 = ldexp(1.0, 2 * (E - SHIFT_BITS));
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
-                        const int col = blk * TC_NBLK + 64 * r + 32 * (warp & 1) + 2 * (lane & 15) + c;
+                        const int col = blk * TC_NBLK + 32 * cg + 2 * cp + c;
                         if (col < v.n_ang) {
 #pragma unroll
                             for (int b = 0; b < NB; ++b) {
                                 if (b < v.n_bin) {
                                     const double f = v.frac[(size_t)b * v.n_comp + comp];
                                     atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
-                                              f * ((double)uh[r][c][b] + (double)ul[r][c][b]) * f2);
+                                              f * ((double)uh[c][b] + (double)ul[c][b]) * f2);
                                 }
                             }
                         }
@@ -483,8 +774,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 }
             }
         }
+        if (!ok && tid == 0) {
+            *s_abort = 1;
+            atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
+        }
     }
-done:
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -502,7 +796,9 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     int *eexp = (int *)(scr + p->o_eexp);
     int *eunit = (int *)(scr + p->o_eunit);
     __half *bt = (__half *)(scr + p->o_bt);
-    int *counter = (int *)(scr + p->o_counter);
+    ctx_pre_launch(ctx);
+    k_f64x2_to_f32x2<<<(unsigned)ceil_div64(p->pc_total, 256), 256, 0, st>>>(p->pc_total, v.pc, v.pcf);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_f64x2_to_f32x2"));
     ctx_pre_launch(ctx);
     k_fill_int<<<(unsigned)ceil_div64(p->n_units, 256), 256, 0, st>>>((int)p->n_units, eunit, -100000);
     GBMIE_TRY(ctx_check_launch(ctx, "k_fill_int"));
@@ -514,7 +810,11 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     k_tab_bt_f16<<<(p->n_pad_total + 127) / 128, 128, 0, st>>>(d.n_ang, p->n_pad_total, p->k_pad, p->nmax_max,
                                                                 d.cos_theta, bt);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_bt_f16"));
-    GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(counter, 0, sizeof(int), st), "counter clear"));
+    uint8_t *asplit = (uint8_t *)(scr + p->o_asplit);
+    ctx_pre_launch(ctx);
+    k_tab_split_a<<<(unsigned)(p->n_units * p->ntiles), 128, 0, st>>>(v, p->ntiles, cf, eexp, p->tile_cbase,
+                                                                      p->unit_cbase, asplit);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_split_a"));
     TcArgs a;
     a.v = v;
     a.cf = cf;
@@ -524,7 +824,10 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     a.n_pad = p->n_pad_total;
     a.k_pad = p->k_pad;
     a.unit_order = p->unit_order;
-    a.counter = counter;
+    a.asplit = asplit;
+    a.tile_cbase = p->tile_cbase;
+    a.unit_cbase = p->unit_cbase;
+    a.ntiles = p->ntiles;
     a.flags = ctx->d_flags;
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);

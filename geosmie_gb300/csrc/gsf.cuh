@@ -6,7 +6,7 @@ struct GsfTables {
     int ng, L, nang;
     void *mem;        // one cudaMalloc block holding everything below
     double *z, *w;    // nodes (ascending) and weights [ng]
-    double *P;        // [4][ng][L] generalized spherical functions P1..P4
+    double *P;        // [4][ng][L] generalized spherical functions P1..P4, l < L
     float *Ph, *Pl;   // P split into FP32 hi + lo (P = Ph + Pl to ~2^-48)
     double *frac;     // [ng] interpolation fraction
     int *base;        // [ng] interpolation interval start
@@ -20,7 +20,8 @@ struct GsfMap {
     int o[6];
 };
 
-int gsf_prepare(gbmie_ctx *ctx, int ng, int nang, const double *theta_rad, GsfTables *t);
+// ng Gauss nodes, the first L <= ng coefficients
+int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta_rad, GsfTables *t);
 void gsf_release(GsfTables *t);
 // precision: GBMIE_PLAIN_FP64 (FP64 sums) or GBMIE_MIXED (split-FP32
 // products, Kahan-compensated FP32 sums)

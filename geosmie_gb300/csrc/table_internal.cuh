@@ -20,12 +20,26 @@ struct gbmie_table_plan {
     int nmax_max;
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
     // mixed precision (tensor-core) path
-    size_t o_cf, o_eexp, o_eunit, o_bt, o_counter, o_wf, o_tw, o_rowc, o_hidx;
-    int n_pad_total;     // angles padded to whole 192-column blocks
+    size_t o_cf, o_eexp, o_eunit, o_bt, o_wf, o_tw, o_rowc, o_hidx, o_pcf;
+    int n_pad_total;     // angles padded to whole 64-column blocks
     int k_pad;           // orders padded to 32
     int *unit_order;     // [n_units] units by decreasing work (plan-owned)
+    // split A operand of the tensor-core contraction: per unit, per 64-size
+    // tile, per 16-order chunk one 16 KB block in the shared-memory layout
+    int ntiles;          // 64-size tiles per unit
+    int *tile_cbase;     // [n_le][ntiles + 1] chunk offset of a tile within its unit (plan-owned)
+    int64_t *unit_cbase; // [n_units] first chunk of a unit (plan-owned)
+    int64_t n_chunks;    // chunks of the whole table
+    size_t o_asplit;
     GsfTables gsf;
     int has_gsf;
+    // CUDA graph of one gbmie_table_run (gbmie_table_run_graph): captured on
+    // a private stream, replayed on the context stream
+    cudaStream_t cap_stream;
+    cudaGraphExec_t gexec;
+    gbmie_table_out gout;   // output pointers the graph was captured with
+    void *gscratch;         // context scratch block the graph was captured with
+    int64_t glaunches;      // kernel launches in one replay
 };
 
 // ---------------------------------------------------------------------------
@@ -72,6 +86,7 @@ struct TabView {
     double4 *rowc;      // per size row: sin x, cos x, 1/x
     HomogIndex *hidx;   // per unit: medium constants of the recurrences
     const double2 *pq;
+    float2 *pcf;        // FP32 copy of pc (mixed path)
     // PSD weights, their radius moments and reff0 do not depend on the
     // wavelength when the grid is a radius grid and the PSD is analytic
     // (x = 2 pi r / lambda: the lognormal argument ln(x / x_mode) and the

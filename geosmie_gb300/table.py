@@ -41,7 +41,7 @@ class _Desc(ctypes.Structure):
                 ["n_lambda", "n_rh", "n_size", "n_bin", "n_comp", "n_ang", "grid_kind", "psd_kind",
                  "precision", "n_gsf"]] + \
                [(n, ctypes.c_void_p) for n in ["lambda_", "grid", "dgrid", "m", "psd_param", "gf_psd"]] + \
-               [("rh0_index", ctypes.c_int32), ("pad0", ctypes.c_int32)] + \
+               [("rh0_index", ctypes.c_int32), ("n_gsf_nodes", ctypes.c_int32)] + \
                [(n, ctypes.c_void_p) for n in ["frac", "weights", "rhop", "rhop0", "gf", "rlow", "rup",
                                                 "cos_theta", "theta"]]
 
@@ -70,7 +70,7 @@ class TablePlan(object):
     synchronisation, capturable in a CUDA graph).
     """
 
-    def __init__(self, spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=0, device=0):
+    def __init__(self, spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=0, device=0, n_gsf_nodes=0):
         self.ctx = _native.context(device)
         dv = self.ctx.device
         ang = np.asarray(spec["ang"], np.float64)
@@ -105,6 +105,7 @@ class TablePlan(object):
         desc.psd_kind = psd_kind
         desc.precision = int(precision)
         desc.n_gsf = int(n_gsf)
+        desc.n_gsf_nodes = int(n_gsf_nodes)   # 0: n_gsf nodes, as the reference
         desc.rh0_index = int(spec.get("rh0_index", 0))
 
         def p(k):
@@ -140,9 +141,11 @@ class TablePlan(object):
         self.n_entries = ne
         self.n_instances = nl * nrh * ncomp * ns
 
-    def run(self):
-        """Launch the table pipeline on torch's current stream."""
-        self.ctx.call("gbmie_table_run", self.h, ctypes.byref(self.out))
+    def run(self, graph=False):
+        """Launch the table pipeline on the context stream.  graph=True
+        replays it as one CUDA graph (captured on the first such call,
+        gbmie_table_run_graph)."""
+        self.ctx.call("gbmie_table_run_graph" if graph else "gbmie_table_run", self.h, ctypes.byref(self.out))
 
     def sync(self):
         self.ctx.sync()

@@ -16,7 +16,8 @@ geosmie_gb300.table.TablePlan) plus a short description.
                        mixed index of 1.43 + 1e-8i with water 1.333 + 1e-9i
   seasalt_large        m = 1.50 + 1e-8i, 20 wavelengths 0.2-4 um, 4000 radii
                        0.03-20 um (x up to ~630), lognormal r_g = 1 um,
-                       sigma_g = 2.0
+                       sigma_g = 2.0; angles at the 4000 Gauss-Legendre
+                       nodes, expanded to 1000 GSF moments on those nodes
 """
 import numpy as np
 
@@ -96,12 +97,23 @@ def dust_bins(n_lambda=40, n_sub=1000, nang=181):
     return specs, "dust-like: 40 wavelengths x 5 bins x 1000 radii x %d angles" % nang
 
 
-def seasalt_large(n_lambda=20, n_radii=4000, nang=181):
+def gauss_angles(n):
+    """Scattering angles (degrees, ascending) at the n Gauss-Legendre nodes
+    of [-1, 1]."""
+    z, _ = np.polynomial.legendre.leggauss(n)
+    return np.degrees(np.arccos(z))[::-1].copy()
+
+
+def seasalt_large(n_lambda=20, n_radii=4000, n_nodes=4000, n_moments=1000):
+    """Returns (spec, description, n_moments, n_nodes): the angle grid is the
+    GSF quadrature itself, so the expansion needs no interpolation."""
     lam = np.logspace(np.log10(0.2e-6), np.log10(4e-6), n_lambda)
     r = np.logspace(np.log10(0.03e-6), np.log10(20e-6), n_radii)
     m = np.full((n_lambda, 1, 1), 1.50 + 1e-8j)
-    spec = _lognormal_spec(lam, r, m, [1.0], [1e-6], 2.0, 2200.0, np.linspace(0.0, 180.0, nang))
-    return spec, "sea-salt-like: %d wavelengths x %d radii x %d angles" % (n_lambda, n_radii, nang)
+    spec = _lognormal_spec(lam, r, m, [1.0], [1e-6], 2.0, 2200.0, gauss_angles(n_nodes))
+    desc = ("sea-salt-like: %d wavelengths x %d radii x %d Gauss-node angles, %d GSF moments"
+            % (n_lambda, n_radii, n_nodes, n_moments))
+    return spec, desc, n_moments, n_nodes
 
 
 def nmax_of(x):
@@ -120,6 +132,7 @@ def work_counts(spec):
     le = np.arange(nl) if int(spec["grid_kind"]) == 1 else np.zeros(nl, np.int64)
     sum_nmax = 0
     sum_nmx = 0
+    sum_warm = 0   # D_n steps above nmax of the mixed kernel (warm-up shortened where it converges)
     for li in range(nl):
         xs = x[le[li]]
         nmi = nm[le[li]]
@@ -129,13 +142,20 @@ def work_counts(spec):
                 nmx = np.rint(np.maximum(nmi, z) + 16.0)
                 sum_nmax += int(nmi.sum())
                 sum_nmx += int(nmx.sum())
-    # tensor-core tiles: 64 sizes, K padded to 32 orders, per unit
-    sum_ktile = 0
+                warm = nmx - 1 - nmi
+                short = z < 0.5 * (nmi + 1)
+                q = 2.0 * np.log((2.0 * (nmi + 1) + 1.0) / np.where(short, z, 1.0))
+                need = np.ceil(39.2 / np.where(short, q, 1.0)) + 2
+                sum_warm += int(np.where(short, np.minimum(warm, need), warm).sum())
+    # tensor-core tiles: 64 sizes, orders in chunks of 16 up to the tile's
+    # largest nmax, per unit
+    sum_kc16 = 0
     for li in range(nl):
         nmi = nm[le[li]]
         last = nmi[np.minimum(np.arange(63, grid.size + 63, 64), grid.size - 1)]
-        sum_ktile += int(np.sum((last + 31) // 32 * 32)) * nrh * ncomp
-    return {"instances": int(nl * nrh * ncomp * grid.size), "sum_nmax": sum_nmax, "sum_nmx": sum_nmx,
-            "sum_ktile": sum_ktile,
+        sum_kc16 += int(np.sum((last + 15) // 16)) * nrh * ncomp
+    return {"instances": int(nl * nrh * ncomp * grid.size), "units": int(nl * nrh * ncomp),
+            "sum_nmax": sum_nmax, "sum_nmx": sum_nmx, "sum_warm": sum_warm,
+            "sum_kc16": sum_kc16,
             "rows": int(x.shape[0] * grid.size), "nbin": int(np.asarray(spec["frac"]).shape[0]),
             "nang": int(np.asarray(spec["ang"]).size)}

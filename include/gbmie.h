@@ -174,7 +174,8 @@ typedef struct {
     int32_t grid_kind;          /* GBMIE_GRID_* */
     int32_t psd_kind;           /* GBMIE_PSD_* */
     int32_t precision;          /* GBMIE_PLAIN_FP64 or GBMIE_MIXED */
-    int32_t n_gsf;              /* Gauss nodes = moments of the GSF expansion
+    int32_t n_gsf;              /* moments of the GSF expansion (reference
+                                   129 = its Gauss node count); 0 = none
                                    (reference 129); 0 = no expansion */
     const double *lambda;       /* [n_lambda] m */
     const double *grid;         /* [n_size] ascending, see grid_kind */
@@ -186,7 +187,11 @@ typedef struct {
                                    (particleparams.py:85-91) */
     int32_t rh0_index;          /* rh index whose growth defines the dry
                                    effective radius reff0 (dointegration.py:841) */
-    int32_t pad0;
+    int32_t n_gsf_nodes;        /* Gauss nodes of the GSF expansion, >= n_gsf;
+                                   0 = n_gsf nodes (the reference's
+                                   L1MAX = NG, spher_expan.f:156).  The first
+                                   n_gsf coefficients of an expansion do not
+                                   depend on how many are kept. */
     const double *frac;         /* [n_bin][n_comp] */
     const double *weights;      /* GBMIE_PSD_WEIGHTS: [n_lambda][n_rh][n_bin]
                                    [n_comp][n_size]; weights of rh0_index give
@@ -225,6 +230,16 @@ int gbmie_table_plan_destroy(gbmie_table_plan *plan);
  * the pygeos pass of gsf/convertncdf.py:319-401 + gsf/spher_expan.f.
  * Asynchronous; uses context scratch sized by the plan. */
 int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_out *out);
+/* The same table as one CUDA graph: the first call (and any call whose
+ * output pointers differ from the captured ones, or after the context's
+ * scratch block was reallocated by a larger plan) captures gbmie_table_run
+ * on a private stream and instantiates it; every call then launches the
+ * graph on the context stream.  Results equal gbmie_table_run's up to the
+ * order of the FP64 atomic additions of the angular sums.  With timing
+ * enabled the whole graph is timed as one record, "gbmie_table_graph".  No
+ * counterpart in the reference (its table loop is Python,
+ * geosmie/dointegration.py:786-1031). */
+int gbmie_table_run_graph(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_out *out);
 
 /* ---- GSF expansion ------------------------------------------------------ */
 /* Expansion coefficients of ntab scattering matrices given on one angle grid:

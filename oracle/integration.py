@@ -381,12 +381,14 @@ def run_table(params, mlist, waterm, ang=None, batch=True, lambdas=None):
     return out
 
 
-def run_spec(spec, n_gsf=0):
+def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
     """CPU evaluation of a table spec (the arrays of geosmie_gb300's
     TablePlan / gbmie_table_desc) with the restated reference formulas:
     raw_mie, lognormal / r^-4 / given PSD weights, integrate_psd,
     finalize_unit, the RH=0 mass normalisation, and (n_gsf > 0) the GSF
-    expansion of oracle/spher_expan.c on the normalised phase matrix.
+    expansion of oracle/spher_expan.c on the normalised phase matrix
+    (n_gsf_nodes > n_gsf: an expansion on that many nodes, its first n_gsf
+    coefficients kept).
 
     Returns arrays shaped like the GPU results: scatkeys [nbin, nl, nrh,
     nang], scalar keys [nbin, nl, nrh], pback [nbin, nl, nrh, 6], 'nl_<key>'
@@ -455,7 +457,8 @@ def run_spec(spec, n_gsf=0):
                     out["nl_" + k][b, li, ri] = fin[k]
     if n_gsf:
         F = np.stack([out[k] for k in ["p11", "p22", "p33", "p44", "p12", "p34"]], axis=3)
-        coef, _ = ogsf.expand(ang, F.reshape(-1, 6, ang.size), n_gsf)
-        coef = coef.reshape(nbin, nl, nrh, 6, n_gsf)
+        ng = max(n_gsf, n_gsf_nodes)
+        coef, _ = ogsf.expand(ang, F.reshape(-1, 6, ang.size), ng)
+        coef = coef.reshape(nbin, nl, nrh, 6, ng)[..., :n_gsf]
         out["pmom"] = coef[:, :, :, [0, 4, 2, 5, 1, 3], :]
     return out

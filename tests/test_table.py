@@ -164,3 +164,39 @@ def test_mixed_reference_layout_and_many_angles_gpu():
         assert np.max(np.abs(got[k] - g["out_" + k]) / p11) < 1e-6, k
     for k in TIGHT:
         assert np.max(np.abs(got[k] - g["out_" + k]) / np.abs(g["out_" + k])) < 1e-6, k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_table_as_cuda_graph_gpu(precision):
+    """gbmie_table_run_graph: the whole table captured once and replayed.
+    Replays equal the eager run up to the order of the FP64 atomic additions
+    (1e-12 of P11, 1e-12 relative for the scalars); new output buffers force
+    a fresh capture that writes to them."""
+    import torch
+    from geosmie_gb300.table import TablePlan
+    spec = synthetic_spec(nl=2, nrh=3, ns=300, nbin=3, nang=181)
+    plan = TablePlan(spec, precision=precision, n_gsf=16)
+    plan.run()
+    a = plan.results()
+    for _ in range(2):
+        plan.run(graph=True)
+    b = plan.results()
+    assert plan.h.value and plan.ctx.launches() > 0
+    p11 = np.abs(a["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-12, k
+    for k in TIGHT + LOOSE:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-12, k
+    assert np.max(np.abs(b["pmom"] - a["pmom"])) < 1e-12
+    # fresh output buffers: the next replay is re-captured against them
+    old = {k: v for k, v in plan.out_t.items()}
+    for k, v in old.items():
+        plan.out_t[k] = torch.full_like(v, float("nan"))
+        setattr(plan.out, k, plan.out_t[k].data_ptr())
+    plan.run(graph=True)
+    c = plan.results()
+    assert np.all(np.isfinite(c["p11"]))
+    assert np.max(np.abs(c["p11"] - a["p11"]) / p11) < 1e-12
+    assert not np.isnan(old["phase"].cpu().numpy()).any()   # the old buffers kept their values
+    plan.close()

@@ -1,0 +1,109 @@
+"""The benchmark workloads (homogeneous single wavelength, dust-like bins,
+sea-salt-like large sizes on Gauss nodes) through the table pipeline.
+
+Parity: the GPU FP64 table against the oracle's restatement on the same
+seeded inputs (reduced sizes where the oracle would take minutes), and the
+mixed-precision table against the FP64 table at full size.  Tolerances: FP64
+phase elements 1e-9 of P11 at the same angle, qext/qsca/g 1e-10 relative,
+the other scalars 1e-9, GSF moments 1e-9 absolute (alpha1(0) = 1); mixed
+path 1e-6 (phase elements of P11, scalars relative, moments of max alpha1).
+"""
+import numpy as np
+import pytest
+
+from geosmie_gb300 import workloads
+from test_table import LOOSE, SCAT, TIGHT, _check_table
+
+
+def test_workload_specs_cpu():
+    """Shapes and seeded inputs of the workloads (no GPU)."""
+    spec, _ = workloads.homogeneous_single()
+    assert spec["m"].shape == (1, 1, 1) and spec["grid"].size == 1000 and spec["ang"].size == 181
+    specs, _ = workloads.dust_bins()
+    assert len(specs) == 5 and all(s["m"].shape == (40, 1, 1) for s in specs)
+    again, _ = workloads.dust_bins()
+    assert np.array_equal(specs[0]["m"], again[0]["m"])   # seeded
+    mr, mi = specs[0]["m"][:, 0, 0].real, specs[0]["m"][:, 0, 0].imag
+    assert np.all((mr >= 1.45) & (mr <= 1.60)) and np.all((mi >= 1e-4) & (mi <= 1e-2))
+    spec, _, nm, nn = workloads.seasalt_large()
+    ang = spec["ang"]
+    assert ang.size == nn == 4000 and nm == 1000 and np.all(np.diff(ang) > 0)
+    z, _ = np.polynomial.legendre.leggauss(8)
+    assert np.allclose(np.cos(np.radians(workloads.gauss_angles(8)))[::-1], z, atol=1e-15)
+    counts = workloads.work_counts(spec)
+    assert counts["instances"] == 20 * 4000 and counts["units"] == 20
+
+
+def _mixed_plain(spec, n_gsf=0, n_gsf_nodes=0):
+    from geosmie_gb300.table import TablePlan
+    out = []
+    for prec in (0, 1):
+        plan = TablePlan(spec, precision=prec, n_gsf=n_gsf, n_gsf_nodes=n_gsf_nodes)
+        plan.run()
+        out.append(plan.results())
+        plan.close()
+    return out
+
+
+def _check_mixed(a, b, n_gsf):
+    p11 = np.abs(a["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, k
+    for k in TIGHT + LOOSE:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, k
+    assert np.max(np.abs(b["qabs"] - a["qabs"]) / np.abs(a["qext"])) < 1e-6
+    if n_gsf:
+        scale = np.max(np.abs(a["pmom"][..., 0, :]), axis=-1)[..., None, None]
+        assert np.max(np.abs(b["pmom"] - a["pmom"]) / scale) < 1e-6
+
+
+@pytest.mark.gpu
+def test_homogeneous_single_full_gpu():
+    """One wavelength, m = 1.53 + 0.008i, 1000 radii 0.01-10 um, 181 angles:
+    the whole workload against the oracle, and mixed against FP64."""
+    from oracle import integration
+    spec, _ = workloads.homogeneous_single()
+    a, b = _mixed_plain(spec, n_gsf=64)
+    ref = integration.run_spec(spec, n_gsf=64)
+    _check_table(a, ref)
+    assert np.max(np.abs(a["pmom"] - ref["pmom"])) < 1e-9
+    _check_mixed(a, b, 64)
+
+
+@pytest.mark.gpu
+def test_dust_bins_gpu():
+    """Random index per wavelength, r^-4 law inside each of 5 bins: reduced
+    (3 wavelengths x 5 bins x 150 radii) against the oracle, the full
+    40 x 5 x 1000 workload mixed against FP64."""
+    from oracle import integration
+    small, _ = workloads.dust_bins(n_lambda=3, n_sub=150)
+    for spec in small:
+        a, _ = _mixed_plain(spec)
+        _check_table(a, integration.run_spec(spec))
+    full, _ = workloads.dust_bins()
+    for spec in full:
+        a, b = _mixed_plain(spec, n_gsf=32)
+        _check_mixed(a, b, 32)
+
+
+@pytest.mark.gpu
+def test_seasalt_large_gauss_nodes_gpu():
+    """x up to ~630 (nmax up to 665) on Gauss-node angles with more nodes
+    than moments: reduced (2 wavelengths x 300 radii x 600 nodes, 150
+    moments) against the oracle; the full 20 x 4000 x 4000-node, 1000-moment
+    workload mixed against FP64, including the forward peak (theta < 1 deg)."""
+    from oracle import integration
+    spec, _, nm, nn = workloads.seasalt_large(n_lambda=2, n_radii=300, n_nodes=600, n_moments=150)
+    a, b = _mixed_plain(spec, n_gsf=nm, n_gsf_nodes=nn)
+    ref = integration.run_spec(spec, n_gsf=nm, n_gsf_nodes=nn)
+    _check_table(a, ref)
+    assert np.max(np.abs(a["pmom"] - ref["pmom"])) < 1e-9
+    _check_mixed(a, b, nm)
+    spec, _, nm, nn = workloads.seasalt_large()
+    a, b = _mixed_plain(spec, n_gsf=nm, n_gsf_nodes=nn)
+    _check_mixed(a, b, nm)
+    fwd = spec["ang"] < 1.0
+    assert fwd.sum() >= 10
+    err = np.max(np.abs(b["p11"][..., fwd] - a["p11"][..., fwd]) / a["p11"][..., fwd])
+    assert err < 1e-6, err
+    assert np.allclose(a["pmom"][..., 0, 0], 1.0, atol=1e-12)
