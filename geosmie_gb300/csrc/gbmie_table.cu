@@ -163,12 +163,35 @@ __global__ void __launch_bounds__(128) k_tab_coeffs(TabView v, int64_t n_inst, i
     const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
     const double x = v.xg[row];
     const double4 rc = v.rowc[row];
-    const HomogIndex h = v.hidx[unit];
     EmitTab emit{v.an + c, v.bn + c};
     EffSums es;
-    homog_core(x, rc.z, rc.x, rc.y, h, v.pc + o, nmax, emit, es);
+    homog_core(x, rc.z, rc.x, rc.y, v.hidx[unit], v.pc + o, nmax, emit, es);
     double e[6];
     es.finish(x, e);
+    double *o4 = v.eff4 + t * 4;
+    o4[0] = e[0];
+    o4[1] = e[1];
+    o4[2] = e[3];
+    o4[3] = e[4];
+}
+
+__global__ void __launch_bounds__(128) k_tab_coeffs_coated(TabView v, int64_t n_inst, int *flags)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_inst) return;
+    const int i = (int)(t % v.n_size);
+    const int64_t unit = t / v.n_size;
+    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+    const int le = v.le(lam);
+    const int64_t row = (int64_t)le * v.n_size + i;
+    const int64_t o = v.off[row];
+    const int nmax = (int)(v.off[row + 1] - o);
+    const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
+    EmitTab emit{v.an + c, v.bn + c};
+    EffSums es;
+    coated_table_instance(v, unit, c, o, nmax, v.xg[row], emit, es, flags);
+    double e[6];
+    es.finish(v.xg[row], e);
     double *o4 = v.eff4 + t * 4;
     o4[0] = e[0];
     o4[1] = e[1];
@@ -509,6 +532,9 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.rup = d.rup;
     v.theta = d.theta;
     v.m = (const double2 *)d.m;
+    v.m_core = (const double2 *)d.m_core;
+    v.core_ratio = d.core_ratio;
+    v.dscr = d.m_core ? (double2 *)(scr + p->o_dscr) : nullptr;
     v.xg = p->xg;
     v.off = p->off;
     v.unit_base = p->unit_base;
@@ -539,6 +565,7 @@ static void plan_free(gbmie_table_plan *p)
     if (p->unit_base) cudaFree(p->unit_base);
     if (p->unit_order) cudaFree(p->unit_order);
     if (p->tile_cbase) cudaFree(p->tile_cbase);
+    if (p->bt) cudaFree(p->bt);
     if (p->unit_cbase) cudaFree(p->unit_cbase);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
@@ -575,6 +602,8 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad psd_kind");
     if (d.precision != GBMIE_PLAIN_FP64 && d.precision != GBMIE_MIXED)
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: bad precision");
+    if ((d.m_core == nullptr) != (d.core_ratio == nullptr))
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_create: m_core and core_ratio go together");
     if (!d.lambda || !d.grid || !d.dgrid || !d.m || !d.frac || !d.rhop || !d.rhop0 || !d.gf || !d.rlow || !d.rup ||
         !d.cos_theta || !d.theta || (d.psd_kind != GBMIE_PSD_WEIGHTS && (!d.psd_param || !d.gf_psd)) ||
         (d.psd_kind == GBMIE_PSD_WEIGHTS && !d.weights))
@@ -728,9 +757,9 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_cf = carve(mixed ? sizeof(float4) * (size_t)p->ab_total : 16);
         p->o_eexp = carve(mixed ? sizeof(int) * (size_t)p->n_inst : 16);
         p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
-        p->o_bt = carve(mixed ? 4 * 2 * (size_t)p->n_pad_total * p->k_pad : 16);
         p->o_asplit = carve(mixed ? (size_t)16384 * (size_t)p->n_chunks : 16);
         p->o_pcf = carve(mixed ? sizeof(float2) * (size_t)p->pc_total : 16);
+        p->o_dscr = carve(d.m_core ? 5 * sizeof(double2) * (size_t)p->ab_total : 16);
         p->o_wf = carve(mixed ? sizeof(float) * nW * d.n_size : 16);
         p->o_tw = carve(sizeof(double) * d.n_ang);
         p->o_rowc = carve(sizeof(double4) * (size_t)p->n_le * d.n_size);
@@ -741,6 +770,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         void *scr = nullptr;
         st = ctx_scratch(ctx, p->bytes, &scr);
     }
+    if (st == GBMIE_OK && d.precision == GBMIE_MIXED) st = build_table_bt(ctx, p);
     if (st == GBMIE_OK && d.n_gsf > 0) {
         st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf);
         p->has_gsf = 1;
@@ -821,8 +851,13 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
         GBMIE_TRY(launch_table_mixed(ctx, p, v, scr));
         return launch_table_tail(ctx, p, v, out);
     }
-    k_tab_coeffs<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs"));
+    if (d.m_core) {
+        k_tab_coeffs_coated<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
+        GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_coated"));
+    } else {
+        k_tab_coeffs<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
+        GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs"));
+    }
     GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
     GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
                        "pacc clear"));

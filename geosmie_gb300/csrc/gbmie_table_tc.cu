@@ -171,6 +171,50 @@ struct EmitMixed {
     }
 };
 
+// Coated units of the mixed table: the FP64 coated recurrences (the
+// Toon-Ackerman ratio chain of mie_coeffs.py:183-251) with FP64 efficiency
+// sums; the coefficients leave as FP32 (c, d) like the homogeneous ones.
+struct EmitCf {
+    float4 *cf;
+    float amax;
+    __device__ __forceinline__ void operator()(int k, cplx a, cplx b) {
+        const float4 q = make_float4((float)(a.re + b.re), (float)(a.im + b.im), (float)(a.re - b.re),
+                                     (float)(a.im - b.im));
+        cf[k - 1] = q;
+        amax = fmaxf(amax, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
+    }
+};
+
+__global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int64_t n_inst, float4 *__restrict__ cf,
+                                                                 int *__restrict__ eexp, int *__restrict__ eunit,
+                                                                 int *flags)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_inst) return;
+    const int i = (int)(t % v.n_size);
+    const int64_t unit = t / v.n_size;
+    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+    const int le = v.le(lam);
+    const int64_t row = (int64_t)le * v.n_size + i;
+    const int64_t o = v.off[row];
+    const int nmax = (int)(v.off[row + 1] - o);
+    const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
+    const double x = v.xg[row];
+    EmitCf emit{cf + c, 0.f};
+    EffSums es;
+    coated_table_instance(v, unit, c, o, nmax, x, emit, es, flags);
+    double e[6];
+    es.finish(x, e);
+    double *o4 = v.eff4 + t * 4;
+    o4[0] = e[0];
+    o4[1] = e[1];
+    o4[2] = e[3];
+    o4[3] = e[4];
+    const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
+    eexp[t] = ex;
+    atomicMax(eunit + unit, ex);
+}
+
 __global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
                                                           int *__restrict__ eexp, int *__restrict__ eunit,
                                                           int *flags)
@@ -620,159 +664,210 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         __syncwarp();
     } else {
         // ================= epilogue (warps 0-7) =================
+        // One flat sequence of tiles s = (unit k, angle block, 64-size tile);
+        // the PSD weights of tile s + 1 are fetched into registers while tile
+        // s is processed and land in shared memory after its last barrier.
         uint32_t item = 0;
         bool ok = true;
         const int q = warp & 3, half = warp >> 2;
         const int il = 16 * q + (lane >> 1);
         const bool odd = lane & 1;
         const int kk = warp >> 1, cg = warp & 1, hh = lane >> 4, cp = lane & 15;
-        for (int k = 0; ok; ++k) {
-            const int64_t uidx = tc_unit_index(k, cta, G);
-            if (uidx >= n_units) break;
-            const int64_t unit = g.unit_order[uidx];
-            const int comp = (int)(unit % v.n_comp);
-            const int64_t lr = unit / v.n_comp;
-            const int lam = (int)(lr / v.n_rh);
-            const int64_t *off = v.off + (int64_t)v.le(lam) * v.n_size;
-            const int *ex = g.eexp + unit * v.n_size;
-            const int E = g.eunit[unit];
-            const int rhi = (int)(lr % v.n_rh);
-            const float *Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
-            for (int blk = 0; blk < nblocks && ok; ++blk) {
-                // per-unit sums of this thread's two columns as unevaluated FP32
-                // pairs (hi + lo, two-sum)
-                float uh[2][NB], ul[2][NB];
+        const int ntl = g.ntiles;
+        // per-unit constants of this CTA's kq-th unit (valid = false past its last unit)
+        struct UnitC {
+            bool valid;
+            int comp, lr, lam, E;
+            const float *Wb;
+            const int *ex;
+            const int64_t *off;
+        };
+        auto unit_c = [&](int kq) -> UnitC {
+            UnitC u;
+            const int64_t uidx = tc_unit_index(kq, cta, G);
+            u.valid = uidx < n_units;
+            if (!u.valid) return u;
+            const int unit = g.unit_order[uidx];
+            u.comp = unit % v.n_comp;
+            u.lr = unit / v.n_comp;
+            u.lam = u.lr / v.n_rh;
+            const int rhi = u.lr - u.lam * v.n_rh;
+            u.Wb = v.Wf + v.wlam(u.lam) + ((size_t)rhi * v.n_bin * v.n_comp + u.comp) * v.n_size;
+            u.ex = g.eexp + (size_t)unit * v.n_size;
+            u.E = g.eunit[unit];
+            u.off = v.off + (int64_t)v.le(u.lam) * v.n_size;
+            return u;
+        };
+        // PSD weights of a tile scaled by 2^(2 (e_i - E)) (E is the unit's largest
+        // exponent, so the power is <= 1; below 2^-126 the weight is dropped) for
+        // this thread's two entries idx = tid, tid + 256 of [64 sizes][8 bins]
+        auto fetch_w = [&](const UnitC &u, int tile, float &w0, float &w1) {
+            const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
+            float w[2];
+#pragma unroll
+            for (int h2 = 0; h2 < 2; ++h2) {
+                const int idx = tid + h2 * TC_EPI_THREADS, b = idx & 7, i = idx >> 3;
+                w[h2] = 0.f;
+                if (i < ntile && b < v.n_bin && b < NB) {
+                    const int e = 2 * (u.ex[t0 + i] - u.E);
+                    const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
+                    w[h2] = u.Wb[(size_t)b * v.n_comp * v.n_size + t0 + i] * p2;
+                }
+            }
+            w0 = w[0];
+            w1 = w[1];
+        };
+        float wn0 = 0.f, wn1 = 0.f;
+        UnitC cu = unit_c(0);
+        if (cu.valid) {
+            fetch_w(cu, 0, wn0, wn1);
+            sw[tid] = wn0;
+            sw[tid + TC_EPI_THREADS] = wn1;
+        }
+        float uh[2][NB], ul[2][NB];   // per-(unit, block) sums, unevaluated FP32 pairs (two-sum)
+        int kq = 0, blk = 0, tile = 0;   // the tile sequence: units, angle blocks, 64-size tiles
+        while (ok && cu.valid) {
+            const int comp = cu.comp, lr = cu.lr;
+            const int64_t *off = cu.off;
+            const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
+            const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
+            const int nwin = ((kt + TC_KC16 - 1) / TC_KC16 + TC_WIN - 1) / TC_WIN;
+            if (tile == 0) {
 #pragma unroll
                 for (int c = 0; c < 2; ++c)
 #pragma unroll
                     for (int b = 0; b < NB; ++b) uh[c][b] = ul[c][b] = 0.f;
-                for (int t0 = 0; t0 < v.n_size && ok; t0 += TC_INST) {
-                    const int ntile = min(TC_INST, v.n_size - t0);
-                    const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
-                    const int nwin = ((kt + TC_KC16 - 1) / TC_KC16 + TC_WIN - 1) / TC_WIN;
-                    // scaled weights of the tile (the previous tile's readers have
-                    // passed the last epilogue barrier of its reduction)
-                    for (int idx = tid; idx < 8 * TC_INST; idx += TC_EPI_THREADS) {
-                        const int b = idx & 7, i = idx >> 3;
-                        float w = 0.f;
-                        if (i < ntile && b < v.n_bin && b < NB)
-                            w = ldexpf(Wb[(size_t)b * v.n_comp * v.n_size + t0 + i], max(-300, 2 * (ex[t0 + i] - E)));
-                        sw[idx] = w;
-                    }
-                    // window sums of S+ and S- (Re/Im of this lane's row, 32 columns)
-                    float rp[32], rm[32];
-                    for (int w = 0; w < nwin; ++w) {
-                        const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
-                        if (tid == 0)
-                            s_epi_go[item & 1] = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
-                        named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
-                        if (!s_epi_go[item & 1]) {
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * half;
-                        if (w == 0) {
-                            tmem_ld32(ta, rp);
-                            tmem_ld32(ta + 64, rm);
-                        } else {
-                            float t[32];
-                            tmem_ld32(ta, t);
-#pragma unroll
-                            for (int i = 0; i < 32; ++i) rp[i] += t[i];
-                            tmem_ld32(ta + 64, t);
-#pragma unroll
-                            for (int i = 0; i < 32; ++i) rm[i] += t[i];
-                        }
-                        tc_fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(acc_empty + set);
-                        ++item;
-                    }
-                    if (!ok) break;
-                    // Mueller phase: warp (q = TMEM lane quarter, half = warp / 4) holds
-                    // rows 32 q .. + 31 (sizes 16 q .. + 15, Re/Im lane pairs) for 32
-                    // columns; the even lane forms column 2p and the odd lane 2p + 1.
-                    float *strow = stage + il * TC_STAGE_PITCH + 32 * half + (odd ? 1 : 0);
-#pragma unroll
-                    for (int pj = 0; pj < 16; ++pj) {
-                        const int j0 = 2 * pj, j1 = 2 * pj + 1;
-                        const float xp = __shfl_xor_sync(0xffffffffu, odd ? rp[j0] : rp[j1], 1);
-                        const float xm = __shfl_xor_sync(0xffffffffu, odd ? rm[j0] : rm[j1], 1);
-                        const float pr = odd ? xp : rp[j0], pi = odd ? rp[j1] : xp;
-                        const float mr = odd ? xm : rm[j0], mi = odd ? rm[j1] : xm;
-                        const float A2 = pr * pr + pi * pi, B2 = mr * mr + mi * mi;
-                        float *st = strow + j0;
-                        st[0 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 + B2);
-                        st[1 * TC_INST * TC_STAGE_PITCH] = -0.5f * (pr * mr + pi * mi);
-                        st[2 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 - B2);
-                        st[3 * TC_INST * TC_STAGE_PITCH] = -0.5f * (mr * pi - mi * pr);
-                    }
-                    named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
-                    // Reduction phase: warp w sums element kk = w / 2 over columns
-                    // 32 (w % 2) + 2 cp + {0, 1} (cp = lane % 16) and sizes 32 h .. + 31
-                    // (h = lane / 16) for every bin; the two halves meet by a shuffle.
-                    {
-                        float acc[2][NB];
-#pragma unroll
-                        for (int c = 0; c < 2; ++c)
-#pragma unroll
-                            for (int b = 0; b < NB; ++b) acc[c][b] = 0.f;
-                        const float *src = stage + (kk * TC_INST + 32 * hh) * TC_STAGE_PITCH + 32 * cg + 2 * cp;
-                        const float *wsrc = sw + 32 * hh * 8;
-#pragma unroll 4
-                        for (int i = 0; i < 32; ++i) {
-                            const float2 sv = *(const float2 *)(src + i * TC_STAGE_PITCH);
-                            const float4 w0 = *(const float4 *)(wsrc + 8 * i);
-                            float wv[8] = {w0.x, w0.y, w0.z, w0.w, 0.f, 0.f, 0.f, 0.f};
-                            if (NB > 4) {
-                                const float4 w1 = *(const float4 *)(wsrc + 8 * i + 4);
-                                wv[4] = w1.x;
-                                wv[5] = w1.y;
-                                wv[6] = w1.z;
-                                wv[7] = w1.w;
-                            }
-#pragma unroll
-                            for (int b = 0; b < NB; ++b) {
-                                acc[0][b] = fmaf(wv[b], sv.x, acc[0][b]);
-                                acc[1][b] = fmaf(wv[b], sv.y, acc[1][b]);
-                            }
-                        }
-#pragma unroll
-                        for (int c = 0; c < 2; ++c)
-#pragma unroll
-                            for (int b = 0; b < NB; ++b) {
-                                const float a = acc[c][b] + __shfl_xor_sync(0xffffffffu, acc[c][b], 16);
-                                // two-sum: (uh + ul) += a exactly-rounded
-                                const float sum = uh[c][b] + a;
-                                const float bp = sum - uh[c][b];
-                                ul[c][b] += (uh[c][b] - (sum - bp)) + (a - bp);
-                                uh[c][b] = sum;
-                            }
-                    }
-                    named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
+            }
+            int nk = kq, nb = blk, nt = tile + 1;   // the next tile
+            if (nt == ntl) {
+                nt = 0;
+                if (++nb == nblocks) {
+                    nb = 0;
+                    ++nk;
                 }
-                if (!ok) break;
+            }
+            const UnitC nu = nk == kq ? cu : unit_c(nk);
+            const bool have_next = nu.valid;
+            if (have_next) fetch_w(nu, nt, wn0, wn1);   // in flight during this tile
+            // window sums of S+ and S- (Re/Im of this lane's row, 32 columns)
+            float rp[32], rm[32];
+            for (int w = 0; w < nwin; ++w) {
+                const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
+                if (tid == 0) s_epi_go[item & 1] = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
+                named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
+                if (!s_epi_go[item & 1]) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * half;
+                if (w == 0) {
+                    tmem_ld32(ta, rp);
+                    tmem_ld32(ta + 64, rm);
+                } else {
+                    float t[32];
+                    tmem_ld32(ta, t);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) rp[i] += t[i];
+                    tmem_ld32(ta + 64, t);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) rm[i] += t[i];
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(acc_empty + set);
+                ++item;
+            }
+            if (!ok) break;
+            // Mueller phase: warp (q = TMEM lane quarter, half = warp / 4) holds
+            // rows 32 q .. + 31 (sizes 16 q .. + 15, Re/Im lane pairs) for 32
+            // columns; the even lane forms column 2p and the odd lane 2p + 1.
+            float *strow = stage + il * TC_STAGE_PITCH + 32 * half + (odd ? 1 : 0);
+#pragma unroll
+            for (int pj = 0; pj < 16; ++pj) {
+                const int j0 = 2 * pj, j1 = 2 * pj + 1;
+                const float xp = __shfl_xor_sync(0xffffffffu, odd ? rp[j0] : rp[j1], 1);
+                const float xm = __shfl_xor_sync(0xffffffffu, odd ? rm[j0] : rm[j1], 1);
+                const float pr = odd ? xp : rp[j0], pi = odd ? rp[j1] : xp;
+                const float mr = odd ? xm : rm[j0], mi = odd ? rm[j1] : xm;
+                const float A2 = pr * pr + pi * pi, B2 = mr * mr + mi * mi;
+                float *st = strow + j0;
+                st[0 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 + B2);
+                st[1 * TC_INST * TC_STAGE_PITCH] = -0.5f * (pr * mr + pi * mi);
+                st[2 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 - B2);
+                st[3 * TC_INST * TC_STAGE_PITCH] = -0.5f * (mr * pi - mi * pr);
+            }
+            named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
+            // Reduction phase: warp w sums element kk = w / 2 over columns
+            // 32 (w % 2) + 2 cp + {0, 1} (cp = lane % 16) and sizes 32 h .. + 31
+            // (h = lane / 16) for every bin; the two halves meet by a shuffle.
+            {
+                float acc[2][NB];
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) acc[c][b] = 0.f;
+                const float *src = stage + (kk * TC_INST + 32 * hh) * TC_STAGE_PITCH + 32 * cg + 2 * cp;
+                const float *wsrc = sw + 32 * hh * 8;
+#pragma unroll 4
+                for (int i = 0; i < 32; ++i) {
+                    const float2 sv = *(const float2 *)(src + i * TC_STAGE_PITCH);
+                    const float4 w0 = *(const float4 *)(wsrc + 8 * i);
+                    float wv[8] = {w0.x, w0.y, w0.z, w0.w, 0.f, 0.f, 0.f, 0.f};
+                    if (NB > 4) {
+                        const float4 w1 = *(const float4 *)(wsrc + 8 * i + 4);
+                        wv[4] = w1.x;
+                        wv[5] = w1.y;
+                        wv[6] = w1.z;
+                        wv[7] = w1.w;
+                    }
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) {
+                        acc[0][b] = fmaf(wv[b], sv.x, acc[0][b]);
+                        acc[1][b] = fmaf(wv[b], sv.y, acc[1][b]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) {
+                        const float a = acc[c][b] + __shfl_xor_sync(0xffffffffu, acc[c][b], 16);
+                        // two-sum: (uh + ul) += a exactly-rounded
+                        const float sum = uh[c][b] + a;
+                        const float bp = sum - uh[c][b];
+                        ul[c][b] += (uh[c][b] - (sum - bp)) + (a - bp);
+                        uh[c][b] = sum;
+                    }
+            }
+            named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
+            // every reader of sw and stage has passed the barrier: the next tile's weights go in
+            if (have_next) {
+                sw[tid] = wn0;
+                sw[tid + TC_EPI_THREADS] = wn1;
+            }
+            if (tile == ntl - 1 && hh == 0) {
                 // unit results of this angle block: lanes of the first size half
                 // hold the combined sums of (element kk, two columns)
-                if (hh == 0) {
-                    const double f2 = ldexp(1.0, 2 * (E - SHIFT_BITS));
+                const double f2 = ldexp(1.0, 2 * (cu.E - SHIFT_BITS));
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        const int col = blk * TC_NBLK + 32 * cg + 2 * cp + c;
-                        if (col < v.n_ang) {
+                for (int c = 0; c < 2; ++c) {
+                    const int col = blk * TC_NBLK + 32 * cg + 2 * cp + c;
+                    if (col < v.n_ang) {
 #pragma unroll
-                            for (int b = 0; b < NB; ++b) {
-                                if (b < v.n_bin) {
-                                    const double f = v.frac[(size_t)b * v.n_comp + comp];
-                                    atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
-                                              f * ((double)uh[c][b] + (double)ul[c][b]) * f2);
-                                }
+                        for (int b = 0; b < NB; ++b) {
+                            if (b < v.n_bin) {
+                                const double f = v.frac[(size_t)b * v.n_comp + comp];
+                                atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
+                                          f * ((double)uh[c][b] + (double)ul[c][b]) * f2);
                             }
                         }
                     }
                 }
             }
+            kq = nk;
+            blk = nb;
+            tile = nt;
+            cu = nu;
         }
         if (!ok && tid == 0) {
             *s_abort = 1;
@@ -795,7 +890,6 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     float4 *cf = (float4 *)(scr + p->o_cf);
     int *eexp = (int *)(scr + p->o_eexp);
     int *eunit = (int *)(scr + p->o_eunit);
-    __half *bt = (__half *)(scr + p->o_bt);
     ctx_pre_launch(ctx);
     k_f64x2_to_f32x2<<<(unsigned)ceil_div64(p->pc_total, 256), 256, 0, st>>>(p->pc_total, v.pc, v.pcf);
     GBMIE_TRY(ctx_check_launch(ctx, "k_f64x2_to_f32x2"));
@@ -803,13 +897,15 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     k_fill_int<<<(unsigned)ceil_div64(p->n_units, 256), 256, 0, st>>>((int)p->n_units, eunit, -100000);
     GBMIE_TRY(ctx_check_launch(ctx, "k_fill_int"));
     ctx_pre_launch(ctx);
-    k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, cf, eexp, eunit,
-                                                                            ctx->d_flags);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
-    ctx_pre_launch(ctx);
-    k_tab_bt_f16<<<(p->n_pad_total + 127) / 128, 128, 0, st>>>(d.n_ang, p->n_pad_total, p->k_pad, p->nmax_max,
-                                                                d.cos_theta, bt);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_bt_f16"));
+    if (d.m_core) {
+        k_tab_coeffs_mixed_coated<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, cf, eexp,
+                                                                                      eunit, ctx->d_flags);
+        GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed_coated"));
+    } else {
+        k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, cf, eexp, eunit,
+                                                                                ctx->d_flags);
+        GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
+    }
     uint8_t *asplit = (uint8_t *)(scr + p->o_asplit);
     ctx_pre_launch(ctx);
     k_tab_split_a<<<(unsigned)(p->n_units * p->ntiles), 128, 0, st>>>(v, p->ntiles, cf, eexp, p->tile_cbase,
@@ -820,7 +916,7 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     a.cf = cf;
     a.eexp = eexp;
     a.eunit = eunit;
-    a.bt = bt;
+    a.bt = p->bt;
     a.n_pad = p->n_pad_total;
     a.k_pad = p->k_pad;
     a.unit_order = p->unit_order;
@@ -851,3 +947,15 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
 }
 
 size_t table_mixed_smem_bytes() { return TC_SMEM_BYTES; }
+
+// The B operands depend only on the angles and the largest nmax: built once
+// per plan into plan-owned memory (plan creation synchronises afterwards).
+int build_table_bt(gbmie_ctx *ctx, gbmie_table_plan *p)
+{
+    const size_t bytes = 4 * 2 * (size_t)p->n_pad_total * p->k_pad;
+    GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&p->bt, bytes), "B operand tables"));
+    ctx_pre_launch(ctx);
+    k_tab_bt_f16<<<(p->n_pad_total + 127) / 128, 128, 0, ctx->stream>>>(p->d.n_ang, p->n_pad_total, p->k_pad,
+                                                                         p->nmax_max, p->d.cos_theta, p->bt);
+    return ctx_check_launch(ctx, "k_tab_bt_f16");
+}

@@ -4,6 +4,7 @@
 #include "common.cuh"
 #include "gsf.cuh"
 #include "mie_device.cuh"
+#include <cuda_fp16.h>
 
 #define TWO_PI 6.28318530717958647692
 #define PI_D 3.14159265358979323846
@@ -20,7 +21,8 @@ struct gbmie_table_plan {
     int nmax_max;
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
     // mixed precision (tensor-core) path
-    size_t o_cf, o_eexp, o_eunit, o_bt, o_wf, o_tw, o_rowc, o_hidx, o_pcf;
+    size_t o_cf, o_eexp, o_eunit, o_wf, o_tw, o_rowc, o_hidx, o_pcf, o_dscr;
+    __half *bt;          // B operands of the contraction (plan-owned, built once at plan time)
     int n_pad_total;     // angles padded to whole 64-column blocks
     int k_pad;           // orders padded to 32
     int *unit_order;     // [n_units] units by decreasing work (plan-owned)
@@ -77,6 +79,9 @@ struct TabView {
     const double *lambda, *grid, *dgrid, *psd_param, *gf_psd, *frac, *rhop, *rhop0, *gf, *rlow, *rup;
     const double *theta;
     const double2 *m;
+    const double2 *m_core;   // coated: core index per unit, or NULL
+    const double *core_ratio;
+    double2 *dscr;           // coated: 5 complex per order of every instance
     const double *xg;
     const int64_t *off, *unit_base;
     double2 *pc, *an, *bn;
@@ -104,3 +109,24 @@ struct TabView {
     }
 };
 
+// Coated units (pymiecoated Mie(m=core, m2=shell, x=core, y=outer)): the
+// reference's dispatch (mie_coeffs.py:62-71) and the FP64 coated recurrences
+// (:183-251), one thread per instance; the grid is the outer size.
+template <class Emit>
+__device__ __forceinline__ void coated_table_instance(const TabView &v, int64_t unit, int64_t c, int64_t o, int nmax,
+                                                      double x, Emit &emit, EffSums &es, int *flags)
+{
+    const int rh = (int)((unit / v.n_comp) % v.n_rh);
+    const cplx ms = cx(v.m[unit]), mc = cx(v.m_core[unit]);
+    const double ratio = v.core_ratio[rh];
+    if (!(ratio >= 0.0 && ratio <= 1.0) || !isfinite(mc.re) || !isfinite(mc.im)) atomicOr(flags, GBMIE_FLAG_INVALID);
+    const cplx e1 = mc * mc, e2 = ms * ms;
+    const double xc = ratio * x;
+    if (xc == x || (e1.re == e2.re && e1.im == e2.im)) homog_instance(x, e1, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
+    else if (xc == 0.0) homog_instance(x, e2, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
+    else coated_instance(xc, x, e1, e2, v.pc + o, nmax, v.dscr + 5 * c, emit, es);
+}
+
+// Mixed path (gbmie_table_tc.cu): the contraction's B operand tables, built
+// once per plan.
+int build_table_bt(gbmie_ctx *ctx, gbmie_table_plan *p);

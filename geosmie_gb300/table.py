@@ -43,7 +43,7 @@ class _Desc(ctypes.Structure):
                [(n, ctypes.c_void_p) for n in ["lambda_", "grid", "dgrid", "m", "psd_param", "gf_psd"]] + \
                [("rh0_index", ctypes.c_int32), ("n_gsf_nodes", ctypes.c_int32)] + \
                [(n, ctypes.c_void_p) for n in ["frac", "weights", "rhop", "rhop0", "gf", "rlow", "rup",
-                                                "cos_theta", "theta"]]
+                                                "cos_theta", "theta", "m_core", "core_ratio"]]
 
 
 class _Out(ctypes.Structure):
@@ -65,7 +65,10 @@ class TablePlan(object):
     complex, psd_kind, psd_param [nbin, ncomp, 4], gf_psd [nrh], rh0_index,
     frac [nbin, ncomp], weights [nl, nrh, nbin, ncomp, ns] (psd_kind
     PSD_WEIGHTS), rhop [nbin, nrh], rhop0 [nbin], gf [nrh], rlow [nbin],
-    rup [nbin], ang (degrees) [nang].  Inputs are copied to the device once;
+    rup [nbin], ang (degrees) [nang]; for coated spheres also m_core [nl,
+    nrh, ncomp] complex (the core index; m is then the shell index and the
+    grid the outer size) and core_ratio [nrh] (core / outer size parameter).
+    Inputs are copied to the device once;
     ``run()`` launches the whole pipeline on the current stream (no host
     synchronisation, capturable in a CUDA graph).
     """
@@ -92,6 +95,9 @@ class TablePlan(object):
             "rhop0": d(spec["rhop0"]), "gf": d(spec["gf"]), "rlow": d(spec["rlow"]), "rup": d(spec["rup"]),
             "cos_theta": d(np.cos(theta)), "theta": d(theta),
         }
+        if spec.get("m_core") is not None:   # coated spheres: core index per unit, core/outer size per RH
+            self.t["m_core"] = d(np.asarray(spec["m_core"], np.complex128).reshape(m.shape), torch.complex128)
+            self.t["core_ratio"] = d(np.asarray(spec["core_ratio"], np.float64))
         psd_kind = int(spec["psd_kind"])
         if psd_kind == PSD_WEIGHTS:
             self.t["weights"] = d(spec["weights"])
@@ -113,7 +119,7 @@ class TablePlan(object):
             return None if t is None else t.data_ptr()
         desc.lambda_ = p("lambda")
         for k in ["grid", "dgrid", "m", "psd_param", "gf_psd", "frac", "weights", "rhop", "rhop0", "gf",
-                  "rlow", "rup", "cos_theta", "theta"]:
+                  "rlow", "rup", "cos_theta", "theta", "m_core", "core_ratio"]:
             setattr(desc, k, p(k))
         self.desc = desc
         self.shape = (nbin, nl, nrh)

@@ -14,6 +14,9 @@ geosmie_gb300.table.TablePlan) plus a short description.
   sulfate_table        36 RH x 60 wavelengths x 5 bins x 2000 radii x 181
                        angles + 64 GSF moments, kappa growth (0.6), volume
                        mixed index of 1.43 + 1e-8i with water 1.333 + 1e-9i
+  coated_bc            core 1.95 + 0.79i in a humidified 1.53 + 0.01i shell,
+                       20 RH x 10 core fractions x 30 wavelengths x 2000
+                       outer radii x 181 angles
   seasalt_large        m = 1.50 + 1e-8i, 20 wavelengths 0.2-4 um, 4000 radii
                        0.03-20 um (x up to ~630), lognormal r_g = 1 um,
                        sigma_g = 2.0; angles at the 4000 Gauss-Legendre
@@ -114,6 +117,36 @@ def seasalt_large(n_lambda=20, n_radii=4000, n_nodes=4000, n_moments=1000):
     desc = ("sea-salt-like: %d wavelengths x %d radii x %d Gauss-node angles, %d GSF moments"
             % (n_lambda, n_radii, n_nodes, n_moments))
     return spec, desc, n_moments, n_nodes
+
+
+def coated_bc(n_lambda=30, n_radii=2000, n_rh=20, n_frac=10, nang=181):
+    """Black-carbon core in an organic shell swollen by humidity.
+
+    Core m = 1.95 + 0.79i; shell 1.53 + 0.01i volume-mixed with water
+    (1.333 + 1e-9i) by the kappa-growth factor (kappa = 0.6) at 20 RH (every
+    other value of the sulfate-table RH list, 18, plus 0.97 and 0.99); core
+    volume fractions f = 0.05 .. 0.5 (linear) of the
+    whole particle, x_core = y f^(1/3); 30 wavelengths 0.2-3 um; 2000 outer
+    radii 0.01-2 um; one lognormal bin (r_g = 0.1 um, sigma_g = 2.0) over the
+    grid.  The table's "RH" axis holds the n_rh x n_frac (RH, f) conditions,
+    RH-major.
+    """
+    rh = np.array(sorted(SU_RH[::2] + [0.97, 0.99])[:n_rh])
+    gf = (1.0 + 0.6 * rh / (1.0 - rh)) ** (1.0 / 3.0)
+    f = np.linspace(0.05, 0.5, n_frac)
+    lam = np.logspace(np.log10(0.2e-6), np.log10(3e-6), n_lambda)
+    r = np.logspace(np.log10(0.01e-6), np.log10(2e-6), n_radii)
+    shell0, nw, core = 1.53 + 0.01j, 1.333 + 1e-9j, 1.95 + 0.79j
+    shell = nw + (shell0 - nw) * gf ** -3.0                         # per RH
+    gfc = np.repeat(gf, n_frac)                                      # per condition
+    m = np.repeat(shell, n_frac)[None, :, None] * np.ones((n_lambda, 1, 1))
+    spec = _lognormal_spec(lam, r, m, gfc, [0.1e-6], 2.0, 1500.0, np.linspace(0.0, 180.0, nang))
+    spec["gf_psd"] = np.ones(gfc.size)          # the lognormal is over the outer (wet) grid as given
+    spec["m_core"] = np.full(m.shape, core)
+    spec["core_ratio"] = np.tile(np.cbrt(f), n_rh)
+    desc = ("coated black carbon: %d RH x %d core fractions x %d wavelengths x %d outer radii x %d angles"
+            % (n_rh, n_frac, n_lambda, n_radii, nang))
+    return spec, desc
 
 
 def nmax_of(x):

@@ -203,6 +203,14 @@ typedef struct {
     const double *rup;          /* [n_bin] */
     const double *cos_theta;    /* [n_ang] */
     const double *theta;        /* [n_ang] radians, ascending */
+    /* Coated spheres (pymiecoated Mie(m=core, m2=shell, x, y),
+     * mie_coeffs.py:183-251), or NULL for homogeneous spheres: the grid is
+     * the outer size, m the shell index and m_core the core index per
+     * (lambda, rh, comp); the core size parameter is core_ratio[rh] times the
+     * outer one (0 <= core_ratio <= 1; 0 gives the shell alone, 1 or equal
+     * indices the homogeneous core sphere, mie_coeffs.py:62-71). */
+    const gbmie_complex *m_core;  /* [n_lambda][n_rh][n_comp] or NULL */
+    const double *core_ratio;     /* [n_rh], with m_core */
 } gbmie_table_desc;
 
 typedef struct {

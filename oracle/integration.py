@@ -191,15 +191,30 @@ def calculate_psd(params, radind, onerh, rh, xxarr, drarr, rrat, lam):
     return psd, ref, rlow, rup
 
 
-def raw_mie(x_arr, costarr, lam, mr, mi, batch=True):
+def raw_mie(x_arr, costarr, lam, mr, mi, batch=True, m_core=None, core_ratio=None):
     """Per-size Mie results of one (lambda, component), dointegration.py:1211-1254.
 
     Returns the dict rawMie builds: the six Mueller arrays [nx, nang] and the
-    per-size qext, qsca, qabs, qb, g, csca, cext.
+    per-size qext, qsca, qabs, qb, g, csca, cext.  With m_core: coated
+    spheres of outer size x_arr, shell index mr + i mi, core index m_core and
+    core size core_ratio * x (pymiecoated Mie(m=m_core, m2=shell, x, y)).
     """
     x_arr = np.asarray(x_arr, dtype=np.float64)
     rr = x_arr * lam / (2.0 * np.pi)
-    if batch:
+    if m_core is not None:
+        eps_s = complex(mr, mi) ** 2
+        eps_c = complex(m_core) ** 2
+        ans, bns, nmax = [], [], []
+        for xx in x_arr:
+            a, b, nm = pymie.mie_coeffs(eps_c, float(core_ratio) * xx, y=xx, eps2=eps_s)
+            ans.append(a)
+            bns.append(b)
+            nmax.append(nm)
+        nmax = np.array(nmax)
+        pr = pymie.batch_props(ans, bns, nmax, x_arr)
+        s1, s2 = pymie.batch_s12(ans, bns, nmax, costarr)
+        vals = {"qext": pr[:, 0], "qsca": pr[:, 1], "qabs": pr[:, 2], "qb": pr[:, 3], "asy": pr[:, 4]}
+    elif batch:
         eps = complex(mr, mi) ** 2
         ans, bns, nmax = pymie.batch_coeffs_homog(x_arr, eps)
         pr = pymie.batch_props(ans, bns, nmax, x_arr)
@@ -435,7 +450,13 @@ def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
                   for c in range(ncomp)] for b in range(nbin)]
         mass0 = [None] * nbin
         for ri in range(nrh):
-            raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag) for c in range(ncomp)]
+            if spec.get("m_core") is not None:
+                mcore = np.asarray(spec["m_core"], np.complex128)
+                cr = float(np.asarray(spec["core_ratio"])[ri])
+                raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag, m_core=mcore[li, ri, c],
+                                core_ratio=cr) for c in range(ncomp)]
+            else:
+                raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag) for c in range(ncomp)]
             for b in range(nbin):
                 psd = [weights(li, ri, b, c, x) for c in range(ncomp)]
                 rhop = float(np.asarray(spec["rhop"])[b, ri])

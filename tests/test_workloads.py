@@ -1,5 +1,6 @@
 """The benchmark workloads (homogeneous single wavelength, dust-like bins,
-sea-salt-like large sizes on Gauss nodes) through the table pipeline.
+sea-salt-like large sizes on Gauss nodes, coated black carbon) through the
+table pipeline.
 
 Parity: the GPU FP64 table against the oracle's restatement on the same
 seeded inputs (reduced sizes where the oracle would take minutes), and the
@@ -107,3 +108,30 @@ def test_seasalt_large_gauss_nodes_gpu():
     err = np.max(np.abs(b["p11"][..., fwd] - a["p11"][..., fwd]) / a["p11"][..., fwd])
     assert err < 1e-6, err
     assert np.allclose(a["pmom"][..., 0, 0], 1.0, atol=1e-12)
+
+
+def test_coated_workload_spec_cpu():
+    spec, _ = workloads.coated_bc()
+    assert spec["m"].shape == (30, 200, 1) and spec["m_core"].shape == (30, 200, 1)
+    assert spec["core_ratio"].shape == (200,) and np.all((spec["core_ratio"] > 0) & (spec["core_ratio"] < 1))
+    f = spec["core_ratio"][:10] ** 3
+    assert np.allclose(f, np.linspace(0.05, 0.5, 10))
+
+
+@pytest.mark.gpu
+def test_coated_table_gpu():
+    """Coated black-carbon table: reduced (3 wavelengths x 3 RH x 2 core
+    fractions x 200 outer radii) FP64 against the oracle's per-size coated
+    coefficients (the reference's own ratio chain); the full 30 x 200 x 2000
+    workload mixed (FP64 coated recurrences, FP32 coefficients into the tensor
+    cores) against FP64."""
+    from oracle import integration
+    spec, _ = workloads.coated_bc(n_lambda=3, n_radii=200, n_rh=3, n_frac=2)
+    a, b = _mixed_plain(spec, n_gsf=16)
+    ref = integration.run_spec(spec, n_gsf=16)
+    _check_table(a, ref)
+    assert np.max(np.abs(a["pmom"] - ref["pmom"])) < 1e-9
+    _check_mixed(a, b, 16)
+    spec, _ = workloads.coated_bc()
+    a, b = _mixed_plain(spec)
+    _check_mixed(a, b, 0)
