@@ -298,10 +298,10 @@ def main():
         "k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * counts["instances"]) * nang,
         # D_n steps (12 flop), a_n/b_n and efficiency sums (89 flop per order)
         "k_tab_coeffs": coef_flop,
-        # FP64 part of the mixed recurrences: 19 flop per warm-up D_n step, 36 per
-        # order (D_n, its Newton reciprocal, Re of the a_n/b_n numerators and
-        # denominators); the ratio and the efficiency sums are FP32
-        "k_tab_coeffs_mixed": 19.0 * counts["sum_warm"] + 36.0 * counts["sum_nmax"],
+        # FP64 part of the mixed recurrences: 15 flop per warm-up D_n step, 32 per
+        # order (D_n, its one-step Newton reciprocal, Re of the a_n/b_n
+        # numerators and denominators); the ratio and the efficiency sums are FP32
+        "k_tab_coeffs_mixed": 15.0 * counts["sum_warm"] + 32.0 * counts["sum_nmax"],
     }
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))

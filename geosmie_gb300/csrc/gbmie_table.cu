@@ -362,14 +362,29 @@ __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
                 }
             }
         }
-        // block reduction of the NB x 9 sums: warp shuffles, then one thread
-        // per sum over the warps
+        // block reduction of the NB x 9 sums: warp shuffles (FP64 for the FP64
+        // sums; for the FP32 sums unevaluated FP32 pairs hi + lo combined by
+        // two-sum, which keeps FP64 work off the reduction), then one thread
+        // per sum over the warps in FP64
 #pragma unroll
         for (int b = 0; b < NB; ++b)
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
-                double t = acc[b][j].val();
-                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                double t;
+                if (sizeof(T) == 8) {
+                    t = acc[b][j].val();
+                    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                } else {
+                    float hi = (float)acc[b][j].s, lo = -(float)acc[b][j].c;
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+                        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+                        const float sm = hi + oh, bp = sm - hi;
+                        lo += ol + ((hi - (sm - bp)) + (oh - bp));
+                        hi = sm;
+                    }
+                    t = (double)hi + (double)lo;
+                }
                 if ((threadIdx.x & 31) == 0) sRed[threadIdx.x >> 5][b * 9 + j] = t;
             }
         __syncthreads();

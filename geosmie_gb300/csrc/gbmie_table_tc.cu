@@ -35,18 +35,17 @@
 // ---------------------------------------------------------------------------
 // Mixed-precision coefficients: FP32 (c, d) + exponent
 // ---------------------------------------------------------------------------
-// 1/c (c > 0) in FP64 from an FP32 seed and two Newton steps for the
-// reciprocal (e = 1 - c y, y <- y + y e; the error squares at each step, so
-// 2^-24 becomes ~1 ulp); values outside the FP32 normal range take the
-// IEEE division.
+// 1/c (c > 0) in FP64 from an FP32 seed and one Newton step for the
+// reciprocal (e = 1 - c y, y <- y + y e: the relative error squares, 2^-23
+// becomes ~2^-46, far below the FP32 coefficients this path emits; emulated
+// for x up to 650: coefficients within 2.2e-7 of the instance maximum, the
+// same as with the exact reciprocal, while the bare seed gives 1.3e-4);
+// values outside the FP32 normal range take the IEEE division.
 __device__ __forceinline__ double rcp_newton(double c)
 {
     if (!(c > 1e-30 && c < 1e30)) return 1.0 / c;
-    double y = (double)__frcp_rn((float)c);
-    double e = fma(-c, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-c, y, 1.0);
-    return fma(y, e, y);
+    const double y = (double)__frcp_rn((float)c);
+    return fma(y, fma(-c, y, 1.0), y);
 }
 
 // N / (N - i M) in FP32 for N = (nr, ni), M = (mr, mi), with both scaled by
@@ -100,28 +99,30 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
         if (need < warm) warm = need;
     }
     cplx D = cx(0.0, 0.0);
+    // r_k = (k+1)/z and k/x step down by 1/z and 1/x (no integer conversion
+    // per order; the accumulated rounding stays near 1e-13)
+    cplx r = zinv * (double)(nmax + warm + 1);
     for (int k = nmax + warm; k > nmax; --k) {
-        const cplx r = zinv * (double)(k + 1);
         const cplx w = D + r;
         const double iw = rcp_newton(abs2(w));
         D = cx(fma(-w.re, iw, r.re), fma(w.im, iw, r.im));   // r - 1/w
+        r = r - zinv;
     }
-    cplx rk = zinv * (double)(nmax + 1);   // r_nmax = (nmax+1)/z
+    cplx rk = r;                            // r_nmax = (nmax+1)/z
     cplx w = D + rk;                        // D_{nmax+1} + r_nmax
     double iw = rcp_newton(abs2(w));
     double2 pn = row1[nmax - 1];
     float2 pnf = rowf[nmax - 1];
+    double nx = (double)nmax * xinv;        // k/x
     for (int k = nmax; k >= 1; --k) {
         D = cx(fma(-w.re, iw, rk.re), fma(w.im, iw, rk.im));   // D_k
-        const double dk = (double)k;
-        rk = zinv * dk;                                          // r_{k-1} = k/z
+        rk = rk - zinv;                                          // r_{k-1} = k/z
         if (k > 1) {
             w = D + rk;
             iw = rcp_newton(abs2(w));
         }
         const double2 pm = (k > 1) ? row1[k - 2] : make_double2(sx, cxv);
         const float2 pmf = (k > 1) ? rowf[k - 2] : make_float2((float)sx, (float)cxv);
-        const double nx = dk * xinv;
         const double dar = fma(D.re, minv.re, fma(-D.im, minv.im, nx));   // Re(D/m) + k/x
         const double dbr = fma(D.re, m.re, fma(-D.im, m.im, nx));         // Re(D m) + k/x
         const float nar = (float)fma(dar, pn.x, -pm.x), nbr = (float)fma(dbr, pn.x, -pm.x);
@@ -133,6 +134,7 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
         emit(k, a, b);
         pn = pm;
         pnf = pmf;
+        nx -= xinv;
     }
 }
 
@@ -440,6 +442,7 @@ struct TcArgs {
 #define TC_SMEM_BYTES                                                                                  \
     (TC_B0_SLOTS * TC_B16_BYTES + TC_NS * TC_STAGE_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
 #define TC_BAR_EPI 1                                   // named barrier id of the epilogue warps
+#define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
 
 static_assert(TC_WIN <= TC_NS, "a window's chunks must fit the ring");
 static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
@@ -519,7 +522,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
             int prev_blk = -1;
             bool ok = true;
             if (!reload) {   // every block's resident chunk, loaded once
-                ok = mbar_wait_or_abort(b0_full, 0, s_abort);
+                ok = mbar_wait_or_abort(b0_full, 0, s_abort, TC_SLEEP_NS);
                 b0_loads = 1;
             }
             for (int k = 0; ok; ++k) {
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 for (int blk = 0; blk < nblocks && ok; ++blk) {
                     if (reload && blk != prev_blk) {   // the producers reload the resident slot
                         if (prev_blk >= 0) mma_commit(b0_empty);
-                        if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort)) {
+                        if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort, TC_SLEEP_NS)) {
                             ok = false;
                             break;
                         }
@@ -546,13 +549,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         for (int w0 = 0; w0 < nc && ok; w0 += TC_WIN) {
                             const int nj = min(TC_WIN, nc - w0);
                             const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
-                            if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort)) {
+                            if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, TC_SLEEP_NS)) {
                                 ok = false;
                                 break;
                             }
                             for (int j = 0; j < nj && ok; ++j) {
                                 const uint32_t c = it + j;
-                                ok = mbar_wait_or_abort(full + c % TC_NS, (c / TC_NS) & 1u, s_abort);
+                                ok = mbar_wait_or_abort(full + c % TC_NS, (c / TC_NS) & 1u, s_abort, TC_SLEEP_NS);
                             }
                             if (!ok) break;
                             tc_fence_after();
@@ -624,7 +627,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * TC_A16_BYTES;
                 for (int blk = 0; blk < nblocks && ok; ++blk) {
                     if (reload && blk != prev_blk) {
-                        if (prev_blk >= 0 && !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort)) {
+                        if (prev_blk >= 0 && !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort, TC_SLEEP_NS)) {
                             ok = false;
                             break;
                         }
@@ -641,7 +644,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                             const uint32_t c = it++;
                             const int st = (int)(c % TC_NS);
                             uint8_t *sA = sStage + st * TC_STAGE_BYTES;
-                            if (c >= TC_NS && !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort)) {
+                            if (c >= TC_NS && !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort, TC_SLEEP_NS)) {
                                 ok = false;
                                 break;
                             }

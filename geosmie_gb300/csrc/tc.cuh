@@ -40,8 +40,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
 
 // The same wait, giving up early when *abort becomes nonzero (checked every
 // 256 tries), so that one role's failure ends the waits of the others.
+// sleep_ns > 0 backs off between tries (roles whose waits are long and whose
+// warps should not take issue slots from the compute warps).
 __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, uint32_t parity, const volatile int *abort,
-                                                   uint32_t limit = 1u << 26)
+                                                   uint32_t sleep_ns = 0, uint32_t limit = 1u << 26)
 {
     const uint32_t a = smem_u32(bar);
     for (uint32_t it = 0; it < limit; ++it) {
@@ -55,6 +57,7 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, uint32_t parit
             : "memory");
         if (done) return true;
         if ((it & 255u) == 255u && *abort) return false;
+        if (sleep_ns) __nanosleep(sleep_ns);
     }
     return false;
 }
