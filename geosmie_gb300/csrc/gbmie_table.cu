@@ -370,10 +370,10 @@ __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
         for (int b = 0; b < NB; ++b)
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
-                double t;
                 if (sizeof(T) == 8) {
-                    t = acc[b][j].val();
+                    double t = acc[b][j].val();
                     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                    if ((threadIdx.x & 31) == 0) sRed[threadIdx.x >> 5][b * 9 + j] = t;
                 } else {
                     float hi = (float)acc[b][j].s, lo = -(float)acc[b][j].c;
                     for (int o = 16; o > 0; o >>= 1) {
@@ -383,9 +383,8 @@ __global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
                         lo += ol + ((hi - (sm - bp)) + (oh - bp));
                         hi = sm;
                     }
-                    t = (double)hi + (double)lo;
+                    if ((threadIdx.x & 31) == 0) sRed[threadIdx.x >> 5][b * 9 + j] = (double)hi + (double)lo;
                 }
-                if ((threadIdx.x & 31) == 0) sRed[threadIdx.x >> 5][b * 9 + j] = t;
             }
         __syncthreads();
         if (threadIdx.x < NB * 9) {

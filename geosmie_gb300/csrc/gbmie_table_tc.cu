@@ -35,16 +35,18 @@
 // ---------------------------------------------------------------------------
 // Mixed-precision coefficients: FP32 (c, d) + exponent
 // ---------------------------------------------------------------------------
-// 1/c (c > 0) in FP64 from an FP32 seed and one Newton step for the
-// reciprocal (e = 1 - c y, y <- y + y e: the relative error squares, 2^-23
-// becomes ~2^-46, far below the FP32 coefficients this path emits; emulated
-// for x up to 650: coefficients within 2.2e-7 of the instance maximum, the
-// same as with the exact reciprocal, while the bare seed gives 1.3e-4);
-// values outside the FP32 normal range take the IEEE division.
+// 1/c (c > 0) in FP64: the PTX approximate reciprocal (rcp.approx.ftz.f64)
+// as the seed and one Newton-Raphson step (e = 1 - c y, y <- y + y e: the
+// relative error squares), far below the FP32 coefficients this path emits.
+// Emulated for x up to 650 with a 2^-23 seed: coefficients within 2.2e-7 of
+// the instance maximum, the same as with the exact reciprocal, while the
+// bare seed gives 1.3e-4.  Values outside [1e-30, 1e30] take the IEEE
+// division.
 __device__ __forceinline__ double rcp_newton(double c)
 {
     if (!(c > 1e-30 && c < 1e30)) return 1.0 / c;
-    const double y = (double)__frcp_rn((float)c);
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(c));
     return fma(y, fma(-c, y, 1.0), y);
 }
 
