@@ -53,6 +53,8 @@ SIGNATURES = {
     "gbmie_table_plan_destroy": (ctypes.c_int, [_P]),
     "gbmie_table_run": (ctypes.c_int, [_P, _P, _P]),
     "gbmie_table_run_graph": (ctypes.c_int, [_P, _P, _P]),
+    "gbmie_table_plan_autotune": (ctypes.c_int, [_P, _P, _P]),
+    "gbmie_table_plan_tuning": (ctypes.c_int, [_P, _P]),
     "gbmie_gsf": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32, _P, _P, _I32]),
     "gbmie_measure_fp64_peak": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
 }

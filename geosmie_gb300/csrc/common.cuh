@@ -104,6 +104,12 @@ struct gbmie_ctx {
     int64_t *h_pinned;        // pinned scratch for small host results
     int64_t launches;
     char err[512];
+    // autotuned launch parameters of table plans, keyed by the table's shape
+    struct TuneEntry {
+        int64_t key[10];
+        int32_t params[13];
+    } tune_cache[16];
+    int n_tune;
 };
 
 int ctx_fail(gbmie_ctx *ctx, int status, const char *fmt, ...);

@@ -24,6 +24,8 @@
 
 #include "table_internal.cuh"
 
+#include <string.h>
+
 // ---------------------------------------------------------------------------
 // plan kernels
 // ---------------------------------------------------------------------------
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_coated(TabView v, int64_t n_
 // streamed through shared memory as (a+b, a-b).
 #define TAB_CAP 2048
 template <int NB>
-__global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int nchunk)
+__global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int nchunk, const int2 *__restrict__ brange)
 {
     __shared__ double2 cd[TAB_CAP][2];
     const int64_t unit = blockIdx.x / nchunk;
@@ -215,7 +217,8 @@ __global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int
     const int64_t lr = unit / v.n_comp;   // lam * n_rh + rh
     const int lam = (int)(lr / v.n_rh);
     const int le = v.le(lam);
-    const int i0 = ch * chunk, i1 = min(v.n_size, i0 + chunk);
+    const int2 rg = brange[le];           // this launch's nmax bucket on this x grid
+    const int i0 = rg.x + ch * chunk, i1 = min(rg.y, i0 + chunk);
     if (i0 >= i1) return;
     const int64_t *off = v.off + (int64_t)le * v.n_size;   // off[i] for this x grid
     const int64_t cbase = v.unit_base[unit] - off[0];
@@ -580,6 +583,7 @@ static void plan_free(gbmie_table_plan *p)
     if (p->unit_order) cudaFree(p->unit_order);
     if (p->tile_cbase) cudaFree(p->tile_cbase);
     if (p->bt) cudaFree(p->bt);
+    if (p->brange) cudaFree(p->brange);
     if (p->unit_cbase) cudaFree(p->unit_cbase);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
@@ -749,6 +753,46 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
             free(ub);
         }
     }
+    // nmax buckets of the plain angular kernel: per x grid, the size range
+    // whose nmax falls in each bucket (nmax grows with the size index)
+    if (st == GBMIE_OK) {
+        const int lim[GBMIE_TUNE_BUCKETS - 1] = {16, 64, 256};
+        const int nb1 = GBMIE_TUNE_BUCKETS + 1;
+        int2 *hb = (int2 *)malloc(sizeof(int2) * nb1 * (size_t)p->n_le);
+        if (!hb) st = GBMIE_ERR_NOMEM;
+        for (int b = 0; b < nb1; ++b) p->bmaxlen[b] = 0;
+        for (int le = 0; hb && le < p->n_le; ++le) {
+            int i = 0;
+            for (int b = 0; b < GBMIE_TUNE_BUCKETS; ++b) {
+                const int i0 = i;
+                if (b == GBMIE_TUNE_BUCKETS - 1) i = d.n_size;
+                else
+                    while (i < d.n_size) {
+                        const int64_t r = (int64_t)le * d.n_size + i;
+                        if (hoff[r + 1] - hoff[r] > lim[b]) break;
+                        ++i;
+                    }
+                hb[b * p->n_le + le] = make_int2(i0, i);
+                if (i - i0 > p->bmaxlen[b]) p->bmaxlen[b] = i - i0;
+            }
+            hb[GBMIE_TUNE_BUCKETS * p->n_le + le] = make_int2(0, d.n_size);
+        }
+        p->bmaxlen[GBMIE_TUNE_BUCKETS] = d.n_size;
+        if (st == GBMIE_OK)
+            st = ctx_cuda(ctx, cudaMalloc(&p->brange, sizeof(int2) * nb1 * (size_t)p->n_le), "bucket ranges");
+        if (st == GBMIE_OK)
+            st = ctx_cuda(ctx, cudaMemcpy(p->brange, hb, sizeof(int2) * nb1 * (size_t)p->n_le, cudaMemcpyHostToDevice),
+                          "bucket ranges copy");
+        free(hb);
+        const int thr = d.n_ang >= 256 ? 256 : ((d.n_ang + 31) / 32) * 32;
+        for (int b = 0; b < nb1; ++b) {
+            p->plain_chunk[b] = 256;
+            p->plain_threads[b] = thr;
+        }
+        p->plain_split = 0;   // one launch over the whole grid until tuned
+        p->coef_block = 128;
+        p->tc_win = 3;
+    }
     free(hoff);
     if (st == GBMIE_OK) {
         size_t o = 0;
@@ -785,6 +829,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         st = ctx_scratch(ctx, p->bytes, &scr);
     }
     if (st == GBMIE_OK && d.precision == GBMIE_MIXED) st = build_table_bt(ctx, p);
+    if (st == GBMIE_OK) table_tune_lookup(ctx, p);
     if (st == GBMIE_OK && d.n_gsf > 0) {
         st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf);
         p->has_gsf = 1;
@@ -835,6 +880,24 @@ static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, co
 
 int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr);
 
+// The plain angular kernel over one nmax bucket (sizes of every unit whose
+// nmax falls in it; bucket GBMIE_TUNE_BUCKETS = the whole grid), `chunk`
+// sizes per block, `threads` angles per pass.
+static int launch_s12_plain(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, int b, int chunk, int threads)
+{
+    if (p->bmaxlen[b] == 0) return GBMIE_OK;
+    const int nchunk = (p->bmaxlen[b] + chunk - 1) / chunk;
+    const unsigned grid = (unsigned)(p->n_units * nchunk);
+    const int2 *br = p->brange + (size_t)b * p->n_le;
+    cudaStream_t st = ctx->stream;
+    ctx_pre_launch(ctx);
+    if (p->d.n_bin <= 1) k_tab_s12_plain<1><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
+    else if (p->d.n_bin <= 2) k_tab_s12_plain<2><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
+    else if (p->d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
+    else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
+    return ctx_check_launch(ctx, "k_tab_s12_plain");
+}
+
 extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_table_out *out)
 {
     if (!ctx || !p || !out || p->ctx != ctx) return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_run: bad plan");
@@ -875,16 +938,13 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
     GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
                        "pacc clear"));
-    const int chunk = 256;
-    const int nchunk = (d.n_size + chunk - 1) / chunk;
-    const int threads = d.n_ang >= 256 ? 256 : ((d.n_ang + 31) / 32) * 32;
-    const unsigned grid = (unsigned)(p->n_units * nchunk);
-    ctx_pre_launch(ctx);
-    if (d.n_bin <= 1) k_tab_s12_plain<1><<<grid, threads, 0, st>>>(v, chunk, nchunk);
-    else if (d.n_bin <= 2) k_tab_s12_plain<2><<<grid, threads, 0, st>>>(v, chunk, nchunk);
-    else if (d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk);
-    else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_s12_plain"));
+    if (p->plain_split) {
+        for (int b = 0; b < GBMIE_TUNE_BUCKETS; ++b)
+            GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b]));
+    } else {
+        const int b = GBMIE_TUNE_BUCKETS;
+        GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b]));
+    }
     return launch_table_tail(ctx, p, v, out);
 }
 
@@ -953,3 +1013,161 @@ extern "C" int gbmie_table_run_graph(gbmie_ctx *ctx, gbmie_table_plan *p, const 
     ctx->launches += p->glaunches - 1;   // the graph's kernels, not the graph launch itself
     return st;
 }
+
+// ---------------------------------------------------------------------------
+// Autotuning
+// ---------------------------------------------------------------------------
+static void tune_key(const gbmie_table_plan *p, int64_t *k)
+{
+    const gbmie_table_desc &d = p->d;
+    k[0] = d.precision;
+    k[1] = d.n_ang;
+    k[2] = d.n_size;
+    k[3] = p->n_le;
+    k[4] = p->n_units;
+    k[5] = d.n_bin;
+    k[6] = d.n_comp;
+    k[7] = p->nmax_max;
+    k[8] = p->pc_total;
+    k[9] = d.m_core ? 1 : 0;
+}
+
+// parameter vector: split, chunk [5], threads [5], coefficient block, window
+static void tune_save(const gbmie_table_plan *p, int32_t *q)
+{
+    q[0] = p->plain_split;
+    for (int b = 0; b <= GBMIE_TUNE_BUCKETS; ++b) {
+        q[1 + b] = p->plain_chunk[b];
+        q[1 + GBMIE_TUNE_BUCKETS + 1 + b] = p->plain_threads[b];
+    }
+    q[11] = p->coef_block;
+    q[12] = p->tc_win;
+}
+
+static void tune_load(gbmie_table_plan *p, const int32_t *q)
+{
+    p->plain_split = q[0];
+    for (int b = 0; b <= GBMIE_TUNE_BUCKETS; ++b) {
+        p->plain_chunk[b] = q[1 + b];
+        p->plain_threads[b] = q[1 + GBMIE_TUNE_BUCKETS + 1 + b];
+    }
+    p->coef_block = q[11];
+    p->tc_win = q[12];
+}
+
+// A plan whose table shape was tuned before in this context takes those
+// parameters (called at plan creation).
+int table_tune_lookup(gbmie_ctx *ctx, gbmie_table_plan *p)
+{
+    int64_t k[10];
+    tune_key(p, k);
+    for (int i = 0; i < ctx->n_tune; ++i)
+        if (memcmp(ctx->tune_cache[i].key, k, sizeof(k)) == 0) {
+            tune_load(p, ctx->tune_cache[i].params);
+            p->tuned = 1;
+            return 1;
+        }
+    return 0;
+}
+
+extern "C" int gbmie_table_plan_autotune(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_table_out *out)
+{
+    if (!ctx || !p || !out || p->ctx != ctx) return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_autotune: bad plan");
+    cudaSetDevice(ctx->device);
+    if (p->tuned || table_tune_lookup(ctx, p)) return GBMIE_OK;
+    const int save_timing = ctx->timing;
+    const int64_t save_launches = ctx->launches;
+    ctx->timing = 0;
+    int st = gbmie_table_run(ctx, p, out);   // fills coefficients, weights, B tables
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaEventCreate(&e0), "tune events");
+    if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaEventCreate(&e1), "tune events");
+    void *s = nullptr;
+    if (st == GBMIE_OK) st = ctx_scratch(ctx, p->bytes, &s);
+    if (st == GBMIE_OK) {
+        char *scr = (char *)s;
+        TabView v = make_view(p, scr);
+        if (p->d.precision == GBMIE_MIXED) {
+            st = tune_table_mixed(ctx, p, v, scr, e0, e1);
+        } else {
+            // per nmax bucket, and for one launch over the whole grid: sizes per
+            // block x angles per pass of the plain kernel; then the bucketed
+            // launches against the single one
+            const int chunks[4] = {64, 128, 256, 512};
+            const int thr_cap = p->d.n_ang >= 256 ? 256 : ((p->d.n_ang + 31) / 32) * 32;
+            int thrs[4], nthr = 0;
+            for (int t = 64; t <= 256; t *= 2)
+                if (t < thr_cap) thrs[nthr++] = t;
+            thrs[nthr++] = thr_cap;
+            auto timed = [&](auto launch, float &ms_out) -> int {
+                float best = 3.4e38f;
+                for (int rep = 0; rep < 2; ++rep) {
+                    cudaEventRecord(e0, ctx->stream);
+                    GBMIE_TRY(launch());
+                    cudaEventRecord(e1, ctx->stream);
+                    GBMIE_TRY(ctx_cuda(ctx, cudaEventSynchronize(e1), "tune angular sums"));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best) best = ms;
+                }
+                ms_out = best;
+                return GBMIE_OK;
+            };
+            for (int b = 0; st == GBMIE_OK && b <= GBMIE_TUNE_BUCKETS; ++b) {
+                if (p->bmaxlen[b] == 0) continue;
+                float best = 3.4e38f;
+                for (int ci = 0; st == GBMIE_OK && ci < 4; ++ci)
+                    for (int ti = 0; st == GBMIE_OK && ti < nthr; ++ti) {
+                        float ms = 0.f;
+                        st = timed([&] { return launch_s12_plain(ctx, p, v, b, chunks[ci], thrs[ti]); }, ms);
+                        if (st == GBMIE_OK && ms < best) {
+                            best = ms;
+                            p->plain_chunk[b] = chunks[ci];
+                            p->plain_threads[b] = thrs[ti];
+                        }
+                    }
+            }
+            float t_split = 0.f, t_single = 0.f;
+            if (st == GBMIE_OK)
+                st = timed([&] {
+                    for (int b = 0; b < GBMIE_TUNE_BUCKETS; ++b)
+                        GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b]));
+                    return (int)GBMIE_OK;
+                }, t_split);
+            const int bw = GBMIE_TUNE_BUCKETS;
+            if (st == GBMIE_OK)
+                st = timed([&] { return launch_s12_plain(ctx, p, v, bw, p->plain_chunk[bw], p->plain_threads[bw]); },
+                           t_single);
+            p->plain_split = t_split < t_single ? 1 : 0;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st == GBMIE_OK) {
+        p->tuned = 1;
+        int64_t k[10];
+        tune_key(p, k);
+        const int slot = ctx->n_tune < 16 ? ctx->n_tune++ : 15;
+        memcpy(ctx->tune_cache[slot].key, k, sizeof(k));
+        tune_save(p, ctx->tune_cache[slot].params);
+        if (p->gexec) {   // a captured graph holds the old launch parameters
+            cudaGraphExecDestroy(p->gexec);
+            p->gexec = nullptr;
+        }
+        st = gbmie_table_run(ctx, p, out);   // the outputs of the tuned table
+    }
+    if (st == GBMIE_OK) st = gbmie_ctx_synchronize(ctx);
+    ctx->timing = save_timing;
+    ctx->launches = save_launches;
+    return st;
+}
+
+extern "C" int gbmie_table_plan_tuning(const gbmie_table_plan *p, int32_t *params)
+{
+    if (!p || !params) return GBMIE_ERR_INVALID;
+    params[0] = p->tuned;
+    tune_save(p, params + 1);
+    params[14] = params[15] = 0;
+    return GBMIE_OK;
+}
+

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int6
     atomicMax(eunit + unit, ex);
 }
 
-__global__ void __launch_bounds__(128) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
+__global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
                                                           int *__restrict__ eexp, int *__restrict__ eunit,
                                                           int *flags)
 {
@@ -388,7 +388,7 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 // of MMAs into one accumulator therefore loses a fraction of an ulp per
 // product, always in the same direction: at forward angles, where all terms
 // of S+ add coherently, x = 628 gave 1.4e-6 of P11.  Here every tile's
-// orders are split into windows of TC_WIN 16-order chunks; each window
+// orders are split into windows of g.win (<= TC_NS) 16-order chunks; each window
 // starts a fresh accumulator, adds the two cross products of its orders
 // (C_hi P_lo, C_lo P_hi, 2^-11 of the result) while the accumulator is small
 // and then the C_hi P_hi products, and the epilogue adds the windows in FP32
@@ -424,12 +424,13 @@ struct TcArgs {
     const int *tile_cbase;       // [n_le][ntiles + 1]
     const int64_t *unit_cbase;   // [n_units]
     int ntiles;
+    int win;                     // accumulation window (16-order chunks, <= TC_NS)
     int *flags;
 };
 
 #define TC_KC16 16                                     // orders per chunk (one MMA K step)
 #define TC_NS 4                                        // ring stages
-#define TC_WIN 3                                       // chunks per accumulation window (<= TC_NS)
+#define TC_WIN_MAX TC_NS                               // longest accumulation window (chunks)
 #define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
 #define TC_B0_SLOTS 4                                  // resident B chunks (angle blocks)
 #define TC_A16_MAT (TC_KC16 * 128 * 2)                 // one A matrix of a chunk: 4 KB
@@ -446,7 +447,6 @@ struct TcArgs {
 #define TC_BAR_EPI 1                                   // named barrier id of the epilogue warps
 #define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
 
-static_assert(TC_WIN <= TC_NS, "a window's chunks must fit the ring");
 static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
 
 // k-th unit of CTA `cta` among G CTAs: units in decreasing-work order,
@@ -548,8 +548,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         const int ntile = min(TC_INST, v.n_size - t0);
                         const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
                         const int nc = (kt + TC_KC16 - 1) / TC_KC16;
-                        for (int w0 = 0; w0 < nc && ok; w0 += TC_WIN) {
-                            const int nj = min(TC_WIN, nc - w0);
+                        for (int w0 = 0; w0 < nc && ok; w0 += g.win) {
+                            const int nj = min(g.win, nc - w0);
                             const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
                             if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, TC_SLEEP_NS)) {
                                 ok = false;
@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
             const int64_t *off = cu.off;
             const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
             const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
-            const int nwin = ((kt + TC_KC16 - 1) / TC_KC16 + TC_WIN - 1) / TC_WIN;
+            const int nwin = ((kt + TC_KC16 - 1) / TC_KC16 + g.win - 1) / g.win;
             if (tile == 0) {
 #pragma unroll
                 for (int c = 0; c < 2; ++c)
@@ -907,8 +907,8 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
                                                                                       eunit, ctx->d_flags);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed_coated"));
     } else {
-        k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, cf, eexp, eunit,
-                                                                                ctx->d_flags);
+        k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, p->coef_block), p->coef_block, 0, st>>>(
+            v, p->n_inst, cf, eexp, eunit, ctx->d_flags);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
     }
     uint8_t *asplit = (uint8_t *)(scr + p->o_asplit);
@@ -929,6 +929,7 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     a.tile_cbase = p->tile_cbase;
     a.unit_cbase = p->unit_cbase;
     a.ntiles = p->ntiles;
+    a.win = p->tc_win < 1 ? 1 : (p->tc_win > TC_WIN_MAX ? TC_WIN_MAX : p->tc_win);
     a.flags = ctx->d_flags;
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -964,3 +965,61 @@ int build_table_bt(gbmie_ctx *ctx, gbmie_table_plan *p)
                                                                          p->nmax_max, p->d.cos_theta, p->bt);
     return ctx_check_launch(ctx, "k_tab_bt_f16");
 }
+
+// Autotuning of the mixed path on the plan's own data (after one full run
+// has filled its buffers): the block size of k_tab_coeffs_mixed (64, 128,
+// 256) and the contraction's accumulation window (2, 3 or 4 chunks of 16
+// orders; every window keeps the measured accumulation error near 2e-7 of
+// P11), each the fastest of two timed launches.  Leaves pacc holding
+// partial sums: the caller runs the table again.
+int tune_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr, cudaEvent_t e0, cudaEvent_t e1)
+{
+    cudaStream_t st = ctx->stream;
+    float4 *cf = (float4 *)(scr + p->o_cf);
+    int *eexp = (int *)(scr + p->o_eexp);
+    int *eunit = (int *)(scr + p->o_eunit);
+    float best = 3.4e38f;
+    int pick = p->coef_block;
+    if (!p->d.m_core) {
+        const int blocks[3] = {64, 128, 256};
+        for (int c = 0; c < 3; ++c)
+            for (int rep = 0; rep < 2; ++rep) {
+                const int bs = blocks[c];
+                cudaEventRecord(e0, st);
+                k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, bs), bs, 0, st>>>(v, p->n_inst, cf, eexp, eunit,
+                                                                                      ctx->d_flags);
+                cudaEventRecord(e1, st);
+                GBMIE_TRY(ctx_cuda(ctx, cudaEventSynchronize(e1), "tune coefficients"));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) {
+                    best = ms;
+                    pick = bs;
+                }
+            }
+        p->coef_block = pick;
+    }
+    best = 3.4e38f;
+    int wpick = p->tc_win;
+    for (int w = 2; w <= TC_WIN_MAX; ++w)
+        for (int rep = 0; rep < 2; ++rep) {
+            p->tc_win = w;
+            const int save = ctx->timing;
+            ctx->timing = 0;
+            cudaEventRecord(e0, st);
+            const int rc = launch_table_mixed(ctx, p, v, scr);
+            cudaEventRecord(e1, st);
+            ctx->timing = save;
+            GBMIE_TRY(rc);
+            GBMIE_TRY(ctx_cuda(ctx, cudaEventSynchronize(e1), "tune contraction"));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                wpick = w;
+            }
+        }
+    p->tc_win = wpick;
+    return GBMIE_OK;
+}
+

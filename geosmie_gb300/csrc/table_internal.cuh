@@ -6,6 +6,9 @@
 #include "mie_device.cuh"
 #include <cuda_fp16.h>
 
+// nmax buckets of the plain angular kernel: nmax <= 16, <= 64, <= 256, more
+#define GBMIE_TUNE_BUCKETS 4
+
 #define TWO_PI 6.28318530717958647692
 #define PI_D 3.14159265358979323846
 
@@ -42,6 +45,17 @@ struct gbmie_table_plan {
     gbmie_table_out gout;   // output pointers the graph was captured with
     void *gscratch;         // context scratch block the graph was captured with
     int64_t glaunches;      // kernel launches in one replay
+    // launch parameters, defaults until gbmie_table_plan_autotune (or a
+    // context cache hit) sets them
+    // [GBMIE_TUNE_BUCKETS + 1][n_le] size range [begin, end) of each nmax
+    // bucket, then the whole grid (plan-owned)
+    int2 *brange;
+    int bmaxlen[GBMIE_TUNE_BUCKETS + 1];   // longest range of a bucket over the x grids
+    int plain_chunk[GBMIE_TUNE_BUCKETS + 1], plain_threads[GBMIE_TUNE_BUCKETS + 1];
+    int plain_split;        // 1: one launch per nmax bucket, 0: one launch over the whole grid
+    int coef_block;         // block size of k_tab_coeffs_mixed
+    int tc_win;             // accumulation window of k_tab_s12_tc (16-order chunks)
+    int tuned;
 };
 
 // ---------------------------------------------------------------------------
@@ -130,3 +144,6 @@ __device__ __forceinline__ void coated_table_instance(const TabView &v, int64_t 
 // Mixed path (gbmie_table_tc.cu): the contraction's B operand tables, built
 // once per plan.
 int build_table_bt(gbmie_ctx *ctx, gbmie_table_plan *p);
+int tune_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr, cudaEvent_t e0, cudaEvent_t e1);
+// gbmie_table.cu: launch parameters tuned before for this table shape, if any
+int table_tune_lookup(gbmie_ctx *ctx, gbmie_table_plan *p);

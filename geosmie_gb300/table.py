@@ -153,6 +153,21 @@ class TablePlan(object):
         gbmie_table_run_graph)."""
         self.ctx.call("gbmie_table_run_graph" if graph else "gbmie_table_run", self.h, ctypes.byref(self.out))
 
+    def autotune(self):
+        """Tune the launch parameters on this plan's data (synchronous; ends
+        with a run of the tuned table) and return them (see tuning())."""
+        self.ctx.call("gbmie_table_plan_autotune", self.h, ctypes.byref(self.out))
+        return self.tuning()
+
+    def tuning(self):
+        """{'tuned', 'plain_per_bucket', 'plain_chunk' [5], 'plain_threads'
+        [5], 'coef_block', 'tc_window'}: the plan's launch parameters (nmax
+        buckets <= 16, <= 64, <= 256, more, then the whole-grid launch)."""
+        q = (ctypes.c_int32 * 16)()
+        self.ctx.check(self.ctx.lib.gbmie_table_plan_tuning(self.h, q), "gbmie_table_plan_tuning")
+        return {"tuned": bool(q[0]), "plain_per_bucket": bool(q[1]), "plain_chunk": list(q[2:7]),
+                "plain_threads": list(q[7:12]), "coef_block": int(q[12]), "tc_window": int(q[13])}
+
     def sync(self):
         self.ctx.sync()
 

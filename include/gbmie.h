@@ -248,6 +248,22 @@ int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_ou
  * counterpart in the reference (its table loop is Python,
  * geosmie/dointegration.py:786-1031). */
 int gbmie_table_run_graph(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_out *out);
+/* Autotuning (synchronous): times launch parameters on the plan's own data
+ * and keeps the fastest; the plain FP64 path tunes sizes per block and
+ * angles per pass of its angular kernel for each nmax bucket (nmax <= 16,
+ * <= 64, <= 256, more) and for one launch over the whole grid, then keeps
+ * the faster of the two layouts; the mixed path the block size of its coefficient
+ * kernel and the accumulation window of its tensor-core contraction.  The
+ * choice is cached in the context by table shape: later plans of the same
+ * shape take it at creation.  Ends with a run of the tuned table into out.
+ * No counterpart in the reference (its loops run in Python). */
+int gbmie_table_plan_autotune(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_out *out);
+/* params[16]: [0] 1 when tuned (or taken from the cache); [1] 1 = the plain
+ * angular kernel runs one launch per nmax bucket, 0 = one launch over the
+ * whole grid; [2..6] sizes per block and [7..11] angles per pass of the four
+ * buckets and of the whole-grid launch; [12] coefficient block size of the
+ * mixed path; [13] its accumulation window. */
+int gbmie_table_plan_tuning(const gbmie_table_plan *plan, int32_t *params);
 
 /* ---- GSF expansion ------------------------------------------------------ */
 /* Expansion coefficients of ntab scattering matrices given on one angle grid:

@@ -200,3 +200,39 @@ def test_table_as_cuda_graph_gpu(precision):
     assert np.max(np.abs(c["p11"] - a["p11"]) / p11) < 1e-12
     assert not np.isnan(old["phase"].cpu().numpy()).any()   # the old buffers kept their values
     plan.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_gpu(precision):
+    """gbmie_table_plan_autotune: the tuned table equals the default one
+    (FP64: 1e-12 of P11, the order of the atomic sums aside; mixed: both
+    within 1e-6 of the FP64 table), the parameters are in range, and a new
+    plan of the same shape takes them from the context cache."""
+    from geosmie_gb300.table import TablePlan
+    spec = synthetic_spec(nl=2, nrh=3, ns=700, nbin=3, nang=181)
+    ref = TablePlan(spec, precision=0)
+    ref.run()
+    a = ref.results()
+    plan = TablePlan(spec, precision=precision)
+    before = plan.tuning()
+    tun = plan.autotune()
+    b = plan.results()
+    assert tun["tuned"]
+    assert all(c in (64, 128, 256, 512) for c in tun["plain_chunk"])
+    assert all(t in (64, 128, 192, 256) for t in tun["plain_threads"])   # 192: one pass over 181 angles
+    assert tun["coef_block"] in (64, 128, 256) and tun["tc_window"] in (2, 3, 4)
+    tol = 1e-12 if precision == 0 else 1e-6
+    p11 = np.abs(a["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(b[k] - a[k]) / p11) < tol, k
+    for k in TIGHT:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < (1e-12 if precision == 0 else 1e-6), k
+    plan.run(graph=True)   # a graph captured after tuning uses the tuned launches
+    c = plan.results()
+    assert np.max(np.abs(c["p11"] - b["p11"]) / p11) < 1e-12
+    again = TablePlan(spec, precision=precision)
+    assert again.tuning() == tun   # taken from the context cache at creation
+    again.run()
+    d = again.results()
+    assert np.max(np.abs(d["p11"] - b["p11"]) / p11) < 1e-12
