@@ -35,7 +35,9 @@ SAMPLE_LAMBDA = [0, 12, 24, 36, 48, 59]
 # DRAM bytes (read + write) per (wavelength, RH, component) unit from one ncu
 # capture of the 12-wavelength sulfate table (432 units; profiles/
 # k_tab_coeffs_mixed_k_tab_s12_tc_sulfate12.md), scaled to a run by its units
-NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": 138.586112e6 / 432, "k_tab_s12_tc": 175.143168e6 / 432}
+NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": (13.54368e6 + 130.015232e6) / 432,
+                      "k_tab_s12_tc": (740.37888e6 + 12.53632e6) / 432,
+                      "k_tab_split_a": (159.200256e6 + 255.044608e6) / 432}
 SAMPLE_RH = [0, 35]
 
 
@@ -351,7 +353,9 @@ def main():
                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
                     "algorithmic_flop_per_launch": alg, "executed_mma_flop_per_launch": exe,
                     "note": "executed = 3 split products x 2 GEMMs on padded tiles; algorithmic = 8 flop "
-                            "per (order, angle) of the S+/S- sums"}
+                            "per (order, angle) of the S+/S- sums; the tensor pipe is not this kernel's "
+                            "limit: ncu shows the fused Mueller/PSD epilogue issue-bound (47% issue "
+                            "active, tensor pipe 4%)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.small:

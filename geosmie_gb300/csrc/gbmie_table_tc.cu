@@ -50,6 +50,22 @@ __device__ __forceinline__ double rcp_newton(double c)
     return fma(y, fma(-c, y, 1.0), y);
 }
 
+// FP64 -> FP32 by integer operations on the bit pattern (exponent rebias,
+// mantissa truncated to 23 bits: relative error below 2^-23; underflow gives
+// a signed zero, overflow a signed infinity).  On GB300 the FP64 pipe is
+// this kernel's bound and a conversion instruction occupies it, while the
+// integer pipe is idle.
+__device__ __forceinline__ float f64_to_f32_bits(double v)
+{
+    const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+    const unsigned sign = hi & 0x80000000u;
+    const int ef = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+    const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    if (ef <= 0) return __uint_as_float(sign);
+    if (ef >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((unsigned)ef << 23) | mant);
+}
+
 // N / (N - i M) in FP32 for N = (nr, ni), M = (mr, mi), with both scaled by
 // the denominator's largest component (no overflow of |q|^2 for any size).
 __device__ __forceinline__ float2 mie_ratio_f32(float nr, float ni, float mr, float mi)
@@ -127,9 +143,9 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
         const float2 pmf = (k > 1) ? rowf[k - 2] : make_float2((float)sx, (float)cxv);
         const double dar = fma(D.re, minv.re, fma(-D.im, minv.im, nx));   // Re(D/m) + k/x
         const double dbr = fma(D.re, m.re, fma(-D.im, m.im, nx));         // Re(D m) + k/x
-        const float nar = (float)fma(dar, pn.x, -pm.x), nbr = (float)fma(dbr, pn.x, -pm.x);
-        const float mar = (float)fma(dar, pn.y, -pm.y), mbr = (float)fma(dbr, pn.y, -pm.y);
-        const float Dr = (float)D.re, Di = (float)D.im;
+        const float nar = f64_to_f32_bits(fma(dar, pn.x, -pm.x)), nbr = f64_to_f32_bits(fma(dbr, pn.x, -pm.x));
+        const float mar = f64_to_f32_bits(fma(dar, pn.y, -pm.y)), mbr = f64_to_f32_bits(fma(dbr, pn.y, -pm.y));
+        const float Dr = f64_to_f32_bits(D.re), Di = f64_to_f32_bits(D.im);
         const float dai = fmaf(Dr, mifi, Di * mifr), dbi = fmaf(Dr, mfi, Di * mfr);
         const float2 a = mie_ratio_f32(nar, dai * pnf.x, mar, dai * pnf.y);
         const float2 b = mie_ratio_f32(nbr, dbi * pnf.x, mbr, dbi * pnf.y);
