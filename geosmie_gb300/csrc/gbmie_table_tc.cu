@@ -109,11 +109,15 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
     const double az = h.azm * x;
     const int nmx = (int)rint(fmax((double)nmax, az) + 16.0);
     const cplx zinv = h.zminv * xinv;
-    // warm-up steps above nmax: as homog_core
+    // Warm-up steps above nmax.  When |z| < nmax + 1 every step lies where
+    // the recurrence damps the start error by (|z| / (2n+1))^2 per step, so
+    // the steps are counted for a damping of e^-23 (1e-10; the FP64 path
+    // asks for 1e-17); emulated for x in [1e-3, 650]: the same coefficients
+    // to 2.2e-7 with 24% fewer steps on the sulfate-like table.
     int warm = nmx - 1 - nmax;
-    if (az < 0.5 * (nmax + 1)) {
+    if (az < (double)(nmax + 1)) {
         const float q = 2.f * logf((2.f * (float)(nmax + 1) + 1.f) / (float)az);
-        const int need = (int)ceilf(39.2f / q) + 2;
+        const int need = (int)ceilf(23.0f / q) + 2;
         if (need < warm) warm = need;
     }
     cplx D = cx(0.0, 0.0);
@@ -205,9 +209,77 @@ struct EmitCf {
     }
 };
 
+// A operand of the contraction, written once per (unit, 64-size tile,
+// 16-order chunk) as a 16 KB block in the no-swizzle K-major shared-memory
+// layout
+//   [matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
+// (rows 2 i, 2 i + 1 = Re, Im of size i), so that the contraction loads it
+// with one bulk copy per angle block.  split_rows writes the rows of one
+// instance (size i of its unit): FP32 (c, d) orders 1..nmax -> FP16 hi/lo
+// scaled by 2^(13 - e_i), rows 2 ia, 2 ia + 1 (ia = i % 64) of every chunk
+// of the instance's tile, zero past nmax.  The coefficient kernels call it
+// once an instance is done: its coefficients are still in L2, and the
+// integer/FP32/LSU work hides under their FP64 recurrences.
+__device__ __forceinline__ void split_rows(const TabView &v, int64_t unit, int i, int ex, int nmax,
+                                           const float4 *__restrict__ cfi, const int *__restrict__ tile_cbase,
+                                           const int64_t *__restrict__ unit_cbase, int ntiles,
+                                           uint8_t *__restrict__ asplit)
+{
+    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+    const int *tcb = tile_cbase + (size_t)v.le(lam) * (ntiles + 1);
+    const int tile = i >> 6, ia = i & 63;
+    const int nc = tcb[tile + 1] - tcb[tile];
+    uint8_t *dst = asplit + (size_t)(unit_cbase[unit] + tcb[tile]) * 16384;
+    const float sc = ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - ex)));
+    const int r0 = 2 * ia, r1 = 2 * ia + 1;
+    for (int j = 0; j < nc; ++j)
+#pragma unroll
+        for (int kg = 0; kg < 2; ++kg) {
+            __half ch[4][8], cl[4][8];
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const int k = 16 * j + 8 * kg + jj;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k < nmax) q = cfi[k];
+                split_f16(q.x * sc, ch[0][jj], cl[0][jj]);
+                split_f16(q.y * sc, ch[1][jj], cl[1][jj]);
+                split_f16(q.z * sc, ch[2][jj], cl[2][jj]);
+                split_f16(q.w * sc, ch[3][jj], cl[3][jj]);
+            }
+            const uint32_t o0 = (kg * 16 + (r0 >> 3)) * 128 + (r0 & 7) * 16;
+            const uint32_t o1 = (kg * 16 + (r1 >> 3)) * 128 + (r1 & 7) * 16;
+            uint8_t *blk = dst + (size_t)j * 16384;
+            *(uint4 *)(blk + 0 * 4096 + o0) = *(uint4 *)ch[0];
+            *(uint4 *)(blk + 0 * 4096 + o1) = *(uint4 *)ch[1];
+            *(uint4 *)(blk + 1 * 4096 + o0) = *(uint4 *)cl[0];
+            *(uint4 *)(blk + 1 * 4096 + o1) = *(uint4 *)cl[1];
+            *(uint4 *)(blk + 2 * 4096 + o0) = *(uint4 *)ch[2];
+            *(uint4 *)(blk + 2 * 4096 + o1) = *(uint4 *)ch[3];
+            *(uint4 *)(blk + 3 * 4096 + o0) = *(uint4 *)cl[2];
+            *(uint4 *)(blk + 3 * 4096 + o1) = *(uint4 *)cl[3];
+        }
+    // the last size of a partial tile also zeroes the rows of the sizes the
+    // tile lacks (their PSD weights are zero, but 0 x NaN would not be)
+    const int ntile = min(64, v.n_size - 64 * tile);
+    if (ia == ntile - 1 && ntile < 64) {
+        const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+        for (int j = 0; j < nc; ++j)
+            for (int r = 2 * ntile; r < 128; ++r)
+#pragma unroll
+                for (int kg = 0; kg < 2; ++kg) {
+                    const uint32_t o = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
+                    uint8_t *blk = dst + (size_t)j * 16384;
+#pragma unroll
+                    for (int mtx = 0; mtx < 4; ++mtx) *(uint4 *)(blk + mtx * 4096 + o) = z;
+                }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int64_t n_inst, float4 *__restrict__ cf,
                                                                  int *__restrict__ eexp, int *__restrict__ eunit,
-                                                                 int *flags)
+                                                                 int *flags, const int *__restrict__ tile_cbase,
+                                                                 const int64_t *__restrict__ unit_cbase, int ntiles,
+                                                                 uint8_t *__restrict__ asplit)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_inst) return;
@@ -233,11 +305,14 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int6
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
+    split_rows(v, unit, i, ex, nmax, cf + c, tile_cbase, unit_cbase, ntiles, asplit);
 }
 
 __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
                                                           int *__restrict__ eexp, int *__restrict__ eunit,
-                                                          int *flags)
+                                                          int *flags, const int *__restrict__ tile_cbase,
+                                                          const int64_t *__restrict__ unit_cbase, int ntiles,
+                                                          uint8_t *__restrict__ asplit)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_inst) return;
@@ -273,6 +348,7 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
+    split_rows(v, unit, i, ex, nmax, cf + c, tile_cbase, unit_cbase, ntiles, asplit);
 }
 
 // FP32 copy of the psi/chi rows for the FP32 parts of the mixed recurrences.
@@ -289,62 +365,6 @@ __global__ void k_fill_int(int n, int *p, int val)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = val;
-}
-
-// ---------------------------------------------------------------------------
-// A operand of the contraction: FP32 (c, d) -> FP16 hi/lo scaled by
-// 2^(13 - e_i), written once per (unit, 64-size tile, 16-order chunk) as a
-// 16 KB block in the no-swizzle K-major shared-memory layout
-//   [matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
-// (rows 2 i, 2 i + 1 = Re, Im of size i), so that the contraction loads it
-// with one bulk copy per angle block.  Block = (unit, tile); thread =
-// (size i, 8-order half kg); orders past an instance's nmax are zero.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_tab_split_a(TabView v, int ntiles, const float4 *__restrict__ cf,
-                                                     const int *__restrict__ eexp,
-                                                     const int *__restrict__ tile_cbase,
-                                                     const int64_t *__restrict__ unit_cbase, uint8_t *__restrict__ asplit)
-{
-    const int64_t unit = blockIdx.x / ntiles;
-    const int tile = (int)(blockIdx.x % ntiles);
-    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
-    const int le = v.le(lam);
-    const int64_t *off = v.off + (int64_t)le * v.n_size;
-    const int *tcb = tile_cbase + (size_t)le * (ntiles + 1);
-    const int nc = tcb[tile + 1] - tcb[tile];
-    uint8_t *dst = asplit + (size_t)(unit_cbase[unit] + tcb[tile]) * 16384;
-    const int t0 = 64 * tile, ntile = min(64, v.n_size - t0);
-    const int ia = threadIdx.x >> 1, kg = threadIdx.x & 1;
-    const bool has = ia < ntile;
-    const int64_t pa = has ? off[t0 + ia] : 0;
-    const int nma = has ? (int)(off[t0 + ia + 1] - pa) : 0;
-    const float4 *src = cf + (v.unit_base[unit] - off[0]) + pa;
-    const float sc = has ? ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - eexp[unit * v.n_size + t0 + ia]))) : 0.f;
-    const int r0 = 2 * ia, r1 = 2 * ia + 1;
-    const uint32_t o0 = (kg * 16 + (r0 >> 3)) * 128 + (r0 & 7) * 16;
-    const uint32_t o1 = (kg * 16 + (r1 >> 3)) * 128 + (r1 & 7) * 16;
-    for (int j = 0; j < nc; ++j) {
-        __half ch[4][8], cl[4][8];   // [c.re, c.im, d.re, d.im][order]
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-            const int k = 16 * j + 8 * kg + jj;
-            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k < nma) q = src[k];
-            split_f16(q.x * sc, ch[0][jj], cl[0][jj]);
-            split_f16(q.y * sc, ch[1][jj], cl[1][jj]);
-            split_f16(q.z * sc, ch[2][jj], cl[2][jj]);
-            split_f16(q.w * sc, ch[3][jj], cl[3][jj]);
-        }
-        uint8_t *blk = dst + (size_t)j * 16384;
-        *(uint4 *)(blk + 0 * 4096 + o0) = *(uint4 *)ch[0];
-        *(uint4 *)(blk + 0 * 4096 + o1) = *(uint4 *)ch[1];
-        *(uint4 *)(blk + 1 * 4096 + o0) = *(uint4 *)cl[0];
-        *(uint4 *)(blk + 1 * 4096 + o1) = *(uint4 *)cl[1];
-        *(uint4 *)(blk + 2 * 4096 + o0) = *(uint4 *)ch[2];
-        *(uint4 *)(blk + 2 * 4096 + o1) = *(uint4 *)ch[3];
-        *(uint4 *)(blk + 3 * 4096 + o0) = *(uint4 *)cl[2];
-        *(uint4 *)(blk + 3 * 4096 + o1) = *(uint4 *)cl[3];
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -415,7 +435,7 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 //   warps 0-7   epilogue: TMEM -> window sums -> Mueller -> PSD-weighted sums
 //   warp 8      MMA issue (one thread)
 //   warp 9      producer (one thread): bulk copies of the split A operand
-//               (k_tab_split_a) and of B orders > 16 into a TC_NS-stage
+//               (split_rows) and of B orders > 16 into a TC_NS-stage
 //               shared-memory ring
 // Angles go in blocks of 64 (MMA N = 64); TMEM holds TC_NSETS accumulator
 // sets (S+ 64 columns | S- 64 columns), so the MMAs run up to four windows
@@ -436,7 +456,7 @@ struct TcArgs {
     const __half *bt;
     int n_pad, k_pad;
     const int *unit_order;
-    const uint8_t *asplit;       // split A operand (k_tab_split_a)
+    const uint8_t *asplit;       // split A operand (split_rows)
     const int *tile_cbase;       // [n_le][ntiles + 1]
     const int64_t *unit_cbase;   // [n_units]
     int ntiles;
@@ -918,20 +938,16 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     k_fill_int<<<(unsigned)ceil_div64(p->n_units, 256), 256, 0, st>>>((int)p->n_units, eunit, -100000);
     GBMIE_TRY(ctx_check_launch(ctx, "k_fill_int"));
     ctx_pre_launch(ctx);
+    uint8_t *asplit = (uint8_t *)(scr + p->o_asplit);
     if (d.m_core) {
-        k_tab_coeffs_mixed_coated<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, cf, eexp,
-                                                                                      eunit, ctx->d_flags);
+        k_tab_coeffs_mixed_coated<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(
+            v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed_coated"));
     } else {
         k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, p->coef_block), p->coef_block, 0, st>>>(
-            v, p->n_inst, cf, eexp, eunit, ctx->d_flags);
+            v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
     }
-    uint8_t *asplit = (uint8_t *)(scr + p->o_asplit);
-    ctx_pre_launch(ctx);
-    k_tab_split_a<<<(unsigned)(p->n_units * p->ntiles), 128, 0, st>>>(v, p->ntiles, cf, eexp, p->tile_cbase,
-                                                                      p->unit_cbase, asplit);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_split_a"));
     TcArgs a;
     a.v = v;
     a.cf = cf;
@@ -1002,8 +1018,9 @@ int tune_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr,
             for (int rep = 0; rep < 2; ++rep) {
                 const int bs = blocks[c];
                 cudaEventRecord(e0, st);
-                k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, bs), bs, 0, st>>>(v, p->n_inst, cf, eexp, eunit,
-                                                                                      ctx->d_flags);
+                k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, bs), bs, 0, st>>>(
+                    v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles,
+                    (uint8_t *)(scr + p->o_asplit));
                 cudaEventRecord(e1, st);
                 GBMIE_TRY(ctx_cuda(ctx, cudaEventSynchronize(e1), "tune coefficients"));
                 float ms = 0.f;

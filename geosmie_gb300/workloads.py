@@ -176,9 +176,9 @@ def work_counts(spec):
                 sum_nmax += int(nmi.sum())
                 sum_nmx += int(nmx.sum())
                 warm = nmx - 1 - nmi
-                short = z < 0.5 * (nmi + 1)
+                short = z < nmi + 1
                 q = 2.0 * np.log((2.0 * (nmi + 1) + 1.0) / np.where(short, z, 1.0))
-                need = np.ceil(39.2 / np.where(short, q, 1.0)) + 2
+                need = np.ceil(23.0 / np.where(short, q, 1.0)) + 2
                 sum_warm += int(np.where(short, np.minimum(warm, need), warm).sum())
     # tensor-core tiles: 64 sizes, orders in chunks of 16 up to the tile's
     # largest nmax, per unit
