@@ -190,118 +190,19 @@ __global__ void k_gsf_expand(int ntab, int nang, int ng, int L, const double *__
     }
 }
 
-// The same expansion with FP32 arithmetic for the mixed-precision table.
-// Node values F w and the functions P are split into FP32 hi + lo parts;
-// each product f p is formed as hi*hi (rounded) + its exact FMA residual +
-// the two cross terms, so a term carries ~2^-48 relative error, and the
-// rounded parts are summed with Kahan compensation (sum error ~2^-24 of the
-// coefficient whatever the node count).
-__global__ void k_gsf_expand_f32(int ntab, int nang, int ng, int L, const double *__restrict__ F,
-                                 int64_t entry_stride, int64_t row_stride, GsfMap map, const double *__restrict__ w,
-                                 const float *__restrict__ Ph, const float *__restrict__ Pl,
-                                 const int *__restrict__ base, const double *__restrict__ frac,
-                                 double *__restrict__ coef, int64_t out_stride, int64_t out_row_stride,
-                                 double *__restrict__ cnorm)
-{
-    // per node: f11 f44 f22+f33 f22-f33 f12 f34, hi and lo
-    __shared__ float2 Fs[GSF_NODE_CHUNK][6];
-    __shared__ double s_norm;
-    const size_t plane = (size_t)ng * L;
-    for (int e = blockIdx.x; e < ntab; e += gridDim.x) {
-        const double *Fe = F + (size_t)e * entry_stride;
-        for (int l0 = 0; l0 < L; l0 += blockDim.x) {
-            const int l = l0 + threadIdx.x;
-            float sm[6], cm[6], lo[6];
-#pragma unroll
-            for (int r = 0; r < 6; ++r) sm[r] = cm[r] = lo[r] = 0.f;
-            for (int g0 = 0; g0 < ng; g0 += GSF_NODE_CHUNK) {
-                const int gn = min(GSF_NODE_CHUNK, ng - g0);
-                __syncthreads();
-                for (int gg = threadIdx.x; gg < gn; gg += blockDim.x) {
-                    const int g = g0 + gg;
-                    const int b = base[g];
-                    const double fr = frac[g], wg = w[g];
-                    double f[6];
-#pragma unroll
-                    for (int el = 0; el < 6; ++el) {
-                        const double *row = Fe + (size_t)map.f[el] * row_stride;
-                        const double y0 = row[b], y1 = row[b + 1];
-                        f[el] = (y0 + (y1 - y0) * fr) * wg;
-                    }
-                    const double c[6] = {f[0], f[3], f[1] + f[2], f[1] - f[2], f[4], f[5]};
-#pragma unroll
-                    for (int r = 0; r < 6; ++r) {
-                        const float h = (float)c[r];
-                        Fs[gg][r] = make_float2(h, (float)(c[r] - (double)h));
-                    }
-                }
-                __syncthreads();
-                if (l < L) {
-                    for (int gg = 0; gg < gn; ++gg) {
-                        const size_t pi = (size_t)(g0 + gg) * L + l;
-                        const float ph[4] = {Ph[pi], Ph[pi + plane], Ph[pi + 2 * plane], Ph[pi + 3 * plane]};
-                        const float pl[4] = {Pl[pi], Pl[pi + plane], Pl[pi + 2 * plane], Pl[pi + 3 * plane]};
-                        const int which[6] = {0, 0, 1, 2, 3, 3};   // P1 P1 P2 P3 P4 P4
-#pragma unroll
-                        for (int r = 0; r < 6; ++r) {
-                            const float2 fv = Fs[gg][r];
-                            const float a = ph[which[r]], b = pl[which[r]];
-                            const float p = fv.x * a;
-                            const float res = fmaf(fv.x, a, -p);
-                            lo[r] += fmaf(fv.x, b, fmaf(fv.y, a, res));
-                            const float y = p - cm[r];
-                            const float t = sm[r] + y;
-                            cm[r] = (t - sm[r]) - y;
-                            sm[r] = t;
-                        }
-                    }
-                }
-            }
-            double al[6];
-#pragma unroll
-            for (int r = 0; r < 6; ++r) al[r] = (double)sm[r] - (double)cm[r] + (double)lo[r];
-            const double cl = (double)l + 0.5;
-            const double a2 = al[2] * cl * 0.5, a3 = al[3] * cl * 0.5;
-            double v[6] = {al[0] * cl, a2 + a3, a2 - a3, al[1] * cl, al[4] * cl, al[5] * cl};
-            if (l0 == 0) {
-                __syncthreads();
-                if (threadIdx.x == 0) s_norm = 1.0 / v[0];
-                __syncthreads();
-            }
-            if (l < L) {
-                const double cn = s_norm;
-                double *out = coef + (size_t)e * out_stride + l;
-                for (int r = 0; r < 6; ++r) out[(size_t)map.o[r] * out_row_stride] = v[r] * cn;
-                if (l == 0 && cnorm) cnorm[e] = cn;
-            }
-        }
-    }
-}
-
-__global__ void k_gsf_split(size_t n, const double *__restrict__ P, float *__restrict__ Ph, float *__restrict__ Pl)
-{
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float h = (float)P[i];
-    Ph[i] = h;
-    Pl[i] = (float)(P[i] - (double)h);
-}
-
-int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, GsfTables *t)
+int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, GsfTables *t, int ntab_max,
+                int precision)
 {
     t->ng = ng;
     t->L = L;
     t->nang = nang;
-    const size_t bytes = sizeof(double) * (2 * (size_t)ng + 4 * (size_t)ng * L + ng) +
-                         sizeof(float) * 8 * (size_t)ng * L + sizeof(int) * ng;
+    const size_t bytes = sizeof(double) * (2 * (size_t)ng + 4 * (size_t)ng * L + ng) + sizeof(int) * ng;
     GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&t->mem, bytes), "gsf tables"));
     char *p = (char *)t->mem;
     t->z = (double *)p; p += sizeof(double) * ng;
     t->w = (double *)p; p += sizeof(double) * ng;
     t->P = (double *)p; p += sizeof(double) * 4 * (size_t)ng * L;
     t->frac = (double *)p; p += sizeof(double) * ng;
-    t->Ph = (float *)p; p += sizeof(float) * 4 * (size_t)ng * L;
-    t->Pl = (float *)p; p += sizeof(float) * 4 * (size_t)ng * L;
     t->base = (int *)p;
     const int tb = 128, nb = (ng + tb - 1) / tb;
     ctx_pre_launch(ctx);
@@ -310,19 +211,19 @@ int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, Gs
     ctx_pre_launch(ctx);
     k_gsf_gener<<<nb, tb, 0, ctx->stream>>>(ng, t->L, t->z, t->P);
     GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_gener"));
-    const size_t np = 4 * (size_t)ng * L;
-    ctx_pre_launch(ctx);
-    k_gsf_split<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(np, t->P, t->Ph, t->Pl);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_split"));
     ctx_pre_launch(ctx);
     k_gsf_interp<<<nb, tb, 0, ctx->stream>>>(ng, nang, t->z, theta, t->base, t->frac);
-    return ctx_check_launch(ctx, "k_gsf_interp");
+    GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_interp"));
+    if (precision == GBMIE_MIXED) GBMIE_TRY(gsf_tc_prepare(ctx, t, ntab_max));
+    return GBMIE_OK;
 }
 
 void gsf_release(GsfTables *t)
 {
     if (t->mem) cudaFree(t->mem);
     t->mem = nullptr;
+    if (t->tc.mem) cudaFree(t->tc.mem);
+    t->tc.mem = nullptr;
 }
 
 int launch_gsf_expand(gbmie_ctx *ctx, const GsfTables *t, int ntab, const double *F, int64_t entry_stride,
@@ -333,13 +234,10 @@ int launch_gsf_expand(gbmie_ctx *ctx, const GsfTables *t, int ntab, const double
     int threads = ((t->L + 31) / 32) * 32;
     if (threads > 256) threads = 256;
     const int grid = ntab < 152 * 16 ? ntab : 152 * 16;
+    if (precision == GBMIE_MIXED)
+        return launch_gsf_expand_tc(ctx, t, ntab, F, entry_stride, row_stride, map, coef, out_stride, out_row_stride,
+                                    cnorm);
     ctx_pre_launch(ctx);
-    if (precision == GBMIE_MIXED) {
-        k_gsf_expand_f32<<<grid, threads, 0, ctx->stream>>>(ntab, t->nang, t->ng, t->L, F, entry_stride, row_stride,
-                                                            map, t->w, t->Ph, t->Pl, t->base, t->frac, coef,
-                                                            out_stride, out_row_stride, cnorm);
-        return ctx_check_launch(ctx, "k_gsf_expand_f32");
-    }
     k_gsf_expand<<<grid, threads, 0, ctx->stream>>>(ntab, t->nang, t->ng, t->L, F, entry_stride, row_stride, map,
                                                     t->w, t->P, t->base, t->frac, coef, out_stride, out_row_stride,
                                                     cnorm);
@@ -372,7 +270,7 @@ extern "C" int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const doubl
     k_deg2rad<<<(nang + 127) / 128, 128, 0, ctx->stream>>>(nang, ang_deg, theta, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_deg2rad"));
     GsfTables t{};
-    GBMIE_TRY(gsf_prepare(ctx, nnodes, nnodes, nang, theta, &t));
+    GBMIE_TRY(gsf_prepare(ctx, nnodes, nnodes, nang, theta, &t, ntab, precision));
     GsfMap map;
     for (int i = 0; i < 6; ++i) map.f[i] = i, map.o[i] = i;
     int st = launch_gsf_expand(ctx, &t, ntab, F, (int64_t)6 * nang, nang, map, coef, (int64_t)6 * nnodes, nnodes,

@@ -327,8 +327,10 @@ struct KSum {
     __device__ __forceinline__ double val() const { return (double)s - (double)c; }
 };
 
+// (FP32 sums: at most 128 registers, two blocks per SM; the FP64 form keeps
+// its registers)
 template <int NB, typename T>
-__global__ void __launch_bounds__(256) k_tab_scalars(TabView v)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_tab_scalars(TabView v)
 {
     __shared__ double sR[NB][15];
     __shared__ double sRed[8][NB * 9];
@@ -831,7 +833,8 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     if (st == GBMIE_OK && d.precision == GBMIE_MIXED) st = build_table_bt(ctx, p);
     if (st == GBMIE_OK) table_tune_lookup(ctx, p);
     if (st == GBMIE_OK && d.n_gsf > 0) {
-        st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf);
+        st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf,
+                         (int)p->n_entries, d.precision);
         p->has_gsf = 1;
     }
     if (st == GBMIE_OK) st = gbmie_ctx_synchronize(ctx);

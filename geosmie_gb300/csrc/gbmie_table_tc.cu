@@ -40,11 +40,12 @@
 // relative error squares), far below the FP32 coefficients this path emits.
 // Emulated for x up to 650 with a 2^-23 seed: coefficients within 2.2e-7 of
 // the instance maximum, the same as with the exact reciprocal, while the
-// bare seed gives 1.3e-4.  Values outside [1e-30, 1e30] take the IEEE
-// division.
+// bare seed gives 1.3e-4.  No range test: the approximate reciprocal covers
+// the normal FP64 range, and c = |D + r|^2 > 0 here (a zero would be a
+// breakdown of the recurrence itself); FP64 comparisons would occupy the
+// FP64 pipe this kernel is bound by.
 __device__ __forceinline__ double rcp_newton(double c)
 {
-    if (!(c > 1e-30 && c < 1e30)) return 1.0 / c;
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(c));
     return fma(y, fma(-c, y, 1.0), y);

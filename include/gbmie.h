@@ -272,8 +272,9 @@ int gbmie_table_plan_tuning(const gbmie_table_plan *plan, int32_t *params);
  * beta2 (l = 0..nnodes-1) normalised so alpha1(0) = 1; cnorm [ntab] or NULL
  * receives 1/alpha1(0).  Replaces gsf/spher_expan.f:93-107,120-180,269-407,
  * 520-623 (one program run per matrix in the reference).  precision
- * GBMIE_PLAIN_FP64: FP64 sums; GBMIE_MIXED: split-FP32 products with
- * Kahan-compensated FP32 sums (coefficients within ~1e-7 of alpha1(0)). */
+ * GBMIE_PLAIN_FP64: FP64 sums; GBMIE_MIXED: tensor-core GEMMs on
+ * fixed-point digits (exact integer sums; coefficients within ~1e-7 of
+ * alpha1(0)). */
 int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const double *ang_deg,
               const double *F, int32_t nnodes, double *coef, double *cnorm,
               int32_t precision);

@@ -111,7 +111,7 @@ def test_gsf_api_gpu():
         ref, rcn = ogsf.expand(ang, F, ng)
         assert np.max(np.abs(got - ref)) < 1e-10, ng
         assert np.max(np.abs(cn - rcn) / rcn) < 1e-12
-        # split-FP32 products, Kahan FP32 sums: within 1e-6 of alpha1(0) = 1
+        # tensor-core GEMMs on fixed-point digits: within 1e-6 of alpha1(0) = 1
         mixed, mcn = gsf.expand(ang, F, ng, precision=1)
         assert np.max(np.abs(mixed - ref)) < 1e-6, ng
         assert np.max(np.abs(mcn - rcn) / rcn) < 1e-6
