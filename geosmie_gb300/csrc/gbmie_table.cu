@@ -678,7 +678,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         }
         p->ab_total = acc;
         // mixed path: units in decreasing order of work (sum of nmax of their size row)
-        p->n_pad_total = (d.n_ang + 63) / 64 * 64;
+        p->n_pad_total = (d.n_ang + 127) / 128 * 128;
         p->k_pad = (p->nmax_max + 31) / 32 * 32;
         if (ub && d.precision == GBMIE_MIXED && st == GBMIE_OK) {
             int64_t *cost = (int64_t *)malloc(sizeof(int64_t) * p->n_units);

@@ -10,26 +10,28 @@
 // with a per-instance exponent e_i = floor(log2 max |c|, |d|).  The two
 // contractions
 //   S+ = S1 + S2 = sum_n c_n (pi~_n + tau~_n),   S- = S1 - S2 = sum_n d_n (pi~_n - tau~_n)
-// are GEMMs [instances x orders] x [orders x angles]: rows are (instance,
-// Re/Im) pairs, 64 instances = M 128 per tile; columns are angles in blocks of
-// 64 (N).  Each operand is split into FP16 hi + lo halves (values
-// scaled by 2^(13 - e_i) so the row maximum sits just below 2^14), and
-//   C P ~ C_hi P_hi + C_hi P_lo + C_lo P_hi
+// are GEMMs [angles x orders] x [orders x instances]: rows (MMA M) are
+// angles in blocks of 128, columns (N) the (instance, Re/Im) pairs of half a
+// 64-size tile.  Each operand is split into FP16 hi + lo halves (coefficients
+// scaled by 2^(13 - e_i) so the instance's maximum sits just below 2^14), and
+//   P C ~ P_hi C_hi + P_hi C_lo + P_lo C_hi
 // is accumulated in FP32 in tensor memory: three tcgen05.mma per product and
-// K step of 16 orders, six per step for S+ and S- (in windows of 48 orders,
-// cross products first, see below).  The epilogue reads S+/S-
-// rows from TMEM (tcgen05.ld), pairs Re/Im lanes, forms s11, s12, s33, s34
-// and reduces them over the tile's 64 sizes with the PSD weights of every
-// bin (the weights absorb 2^(2(e_i - E)) with E the unit's largest
-// exponent), accumulating per unit in FP64.  Per-size phase matrices never
-// reach global memory.
+// K step of 16 orders, six per step for S+ and S- (in windows of up to 64
+// orders, cross products first, see below).  The epilogue reads S+/S- from
+// TMEM (tcgen05.ld; one angle per thread), forms s11, s12, s33, s34 and sums
+// them over the tile's sizes with the PSD weights of every bin (the weights
+// absorb 2^(2(e_i - E)) with E the unit's largest exponent), accumulating
+// per unit in FP64.  Per-size phase matrices never reach global memory.
 #include "common.cuh"
 #include "mie_device.cuh"
 #include "table_internal.cuh"
 #include "tc.cuh"
 
-#define TC_INST 64        // sizes per tile (M = 128 rows: Re, Im)
-#define TC_NBLK 64        // angles per column block (N)
+#define TC_INST 64                      // sizes per tile
+#define TC_HALF 32                      // sizes per half tile (MMA N = 64: Re, Im)
+#define TC_ABLK 128                     // angles per block (MMA M)
+#define TC_MAT_A (16 * TC_ABLK * 2)     // one angle-function matrix of a 16-order chunk: 4 KB
+#define TC_MAT_B (16 * 2 * TC_HALF * 2) // one coefficient matrix of a half-tile chunk: 2 KB
 #define SHIFT_BITS 13
 
 // ---------------------------------------------------------------------------
@@ -210,15 +212,15 @@ struct EmitCf {
     }
 };
 
-// A operand of the contraction, written once per (unit, 64-size tile,
-// 16-order chunk) as a 16 KB block in the no-swizzle K-major shared-memory
-// layout
-//   [matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
-// (rows 2 i, 2 i + 1 = Re, Im of size i), so that the contraction loads it
-// with one bulk copy per angle block.  split_rows writes the rows of one
-// instance (size i of its unit): FP32 (c, d) orders 1..nmax -> FP16 hi/lo
-// scaled by 2^(13 - e_i), rows 2 ia, 2 ia + 1 (ia = i % 64) of every chunk
-// of the instance's tile, zero past nmax.  The coefficient kernels call it
+// Coefficient operand of the contraction (MMA B), written once per (unit,
+// 64-size tile, 16-order chunk) as a 16 KB block in the no-swizzle K-major
+// shared-memory layout
+//   [half h][matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
+// (rows 2 i', 2 i' + 1 = Re, Im of size 32 h + i'), so that the contraction
+// loads a half tile with one 8 KB bulk copy.  split_rows writes the rows of
+// one instance (size i of its unit): FP32 (c, d) orders 1..nmax -> FP16
+// hi/lo scaled by 2^(13 - e_i), in every chunk of the instance's tile, zero
+// past nmax.  The coefficient kernels call it
 // once an instance is done: its coefficients are still in L2, and the
 // integer/FP32/LSU work hides under their FP64 recurrences.
 __device__ __forceinline__ void split_rows(const TabView &v, int64_t unit, int i, int ex, int nmax,
@@ -232,7 +234,7 @@ __device__ __forceinline__ void split_rows(const TabView &v, int64_t unit, int i
     const int nc = tcb[tile + 1] - tcb[tile];
     uint8_t *dst = asplit + (size_t)(unit_cbase[unit] + tcb[tile]) * 16384;
     const float sc = ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - ex)));
-    const int r0 = 2 * ia, r1 = 2 * ia + 1;
+    const int hh = ia >> 5, r0 = 2 * (ia & 31), r1 = r0 + 1;
     for (int j = 0; j < nc; ++j)
 #pragma unroll
         for (int kg = 0; kg < 2; ++kg) {
@@ -247,31 +249,34 @@ __device__ __forceinline__ void split_rows(const TabView &v, int64_t unit, int i
                 split_f16(q.z * sc, ch[2][jj], cl[2][jj]);
                 split_f16(q.w * sc, ch[3][jj], cl[3][jj]);
             }
-            const uint32_t o0 = (kg * 16 + (r0 >> 3)) * 128 + (r0 & 7) * 16;
-            const uint32_t o1 = (kg * 16 + (r1 >> 3)) * 128 + (r1 & 7) * 16;
+            const uint32_t o0 = hh * 8192 + kg * 1024 + (r0 >> 3) * 128 + (r0 & 7) * 16;
+            const uint32_t o1 = hh * 8192 + kg * 1024 + (r1 >> 3) * 128 + (r1 & 7) * 16;
             uint8_t *blk = dst + (size_t)j * 16384;
-            *(uint4 *)(blk + 0 * 4096 + o0) = *(uint4 *)ch[0];
-            *(uint4 *)(blk + 0 * 4096 + o1) = *(uint4 *)ch[1];
-            *(uint4 *)(blk + 1 * 4096 + o0) = *(uint4 *)cl[0];
-            *(uint4 *)(blk + 1 * 4096 + o1) = *(uint4 *)cl[1];
-            *(uint4 *)(blk + 2 * 4096 + o0) = *(uint4 *)ch[2];
-            *(uint4 *)(blk + 2 * 4096 + o1) = *(uint4 *)ch[3];
-            *(uint4 *)(blk + 3 * 4096 + o0) = *(uint4 *)cl[2];
-            *(uint4 *)(blk + 3 * 4096 + o1) = *(uint4 *)cl[3];
+            *(uint4 *)(blk + 0 * 2048 + o0) = *(uint4 *)ch[0];
+            *(uint4 *)(blk + 0 * 2048 + o1) = *(uint4 *)ch[1];
+            *(uint4 *)(blk + 1 * 2048 + o0) = *(uint4 *)cl[0];
+            *(uint4 *)(blk + 1 * 2048 + o1) = *(uint4 *)cl[1];
+            *(uint4 *)(blk + 2 * 2048 + o0) = *(uint4 *)ch[2];
+            *(uint4 *)(blk + 2 * 2048 + o1) = *(uint4 *)ch[3];
+            *(uint4 *)(blk + 3 * 2048 + o0) = *(uint4 *)cl[2];
+            *(uint4 *)(blk + 3 * 2048 + o1) = *(uint4 *)cl[3];
         }
     // the last size of a partial tile also zeroes the rows of the sizes the
-    // tile lacks (their PSD weights are zero, but 0 x NaN would not be)
+    // tile lacks (their PSD weights are zero, but 0 x NaN would not be); a
+    // half tile without sizes is never read
     const int ntile = min(64, v.n_size - 64 * tile);
     if (ia == ntile - 1 && ntile < 64) {
         const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+        const int rend = ntile <= 32 ? 64 : 128;
         for (int j = 0; j < nc; ++j)
-            for (int r = 2 * ntile; r < 128; ++r)
+            for (int r = 2 * ntile; r < rend; ++r)
 #pragma unroll
                 for (int kg = 0; kg < 2; ++kg) {
-                    const uint32_t o = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
+                    const int rr = r & 63;
+                    const uint32_t o = (r >> 6) * 8192 + kg * 1024 + (rr >> 3) * 128 + (rr & 7) * 16;
                     uint8_t *blk = dst + (size_t)j * 16384;
 #pragma unroll
-                    for (int mtx = 0; mtx < 4; ++mtx) *(uint4 *)(blk + mtx * 4096 + o) = z;
+                    for (int mtx = 0; mtx < 4; ++mtx) *(uint4 *)(blk + mtx * 2048 + o) = z;
                 }
     }
 }
@@ -369,16 +374,18 @@ __global__ void k_fill_int(int n, int *p, int val)
 }
 
 // ---------------------------------------------------------------------------
-// B operands: (p, q) = (pi~ + tau~, pi~ - tau~) split into FP16 hi/lo, in the
-// no-swizzle K-major canonical layout [k/8][angle/8][8 angles][8 orders].
-// Matrices 0..3: P_hi, P_lo, Q_hi, Q_lo, each n_pad x k_pad halves.
+// Angle-function operand (MMA A): (p, q) = (pi~ + tau~, pi~ - tau~) split
+// into FP16 hi/lo, one 16 KB block per (128-angle block, 16-order chunk) in
+// the no-swizzle K-major shared-memory layout
+//   [matrix P_hi P_lo Q_hi Q_lo][kg = order / 8 % 2][angle / 8 (16)][angle % 8][8 orders]
 // ---------------------------------------------------------------------------
 __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const double *__restrict__ cost,
                              __half *__restrict__ bt)
 {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n_pad) return;
-    const size_t mat = (size_t)n_pad * k_pad;
+    const int nkc = k_pad / 16;
+    const int ab = a / TC_ABLK, ag = (a % TC_ABLK) >> 3, a8 = a & 7;
     const double u = a < nang ? cost[a] : 0.0;
     double pm2 = 0.0, pm1 = 0.0;
     for (int n = 1; n <= k_pad; ++n) {
@@ -403,7 +410,8 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
             q = (float)(pv * s - tv * s);
         }
         const int k = n - 1;
-        const size_t off = ((size_t)(k >> 3) * (n_pad >> 3) + (a >> 3)) * 64 + (a & 7) * 8 + (k & 7);
+        const size_t mat = TC_MAT_A / 2;   // halves per matrix
+        const size_t off = (size_t)(ab * nkc + (k >> 4)) * 4 * mat + (((k >> 3) & 1) * 16 + ag) * 64 + a8 * 8 + (k & 7);
         __half h, l;
         split_f16(p, h, l);
         bt[off] = h;
@@ -427,27 +435,36 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 // of S+ add coherently, x = 628 gave 1.4e-6 of P11.  Here every tile's
 // orders are split into windows of g.win (<= TC_NS) 16-order chunks; each window
 // starts a fresh accumulator, adds the two cross products of its orders
-// (C_hi P_lo, C_lo P_hi, 2^-11 of the result) while the accumulator is small
-// and then the C_hi P_hi products, and the epilogue adds the windows in FP32
+// (P_hi C_lo, P_lo C_hi, 2^-11 of the result) while the accumulator is small
+// and then the P_hi C_hi products, and the epilogue adds the windows in FP32
 // registers with round-to-nearest.  Emulating the measured rule puts the
 // bulk P11 error at x = 628 near 2.6e-7 this way.
 //
+// Orientation: angles are the MMA's M (128 per block, TMEM lanes), the
+// (size, Re/Im) rows of half a tile its N (64 columns = 32 sizes).  Each
+// epilogue thread owns one angle and 16 sizes, so the Mueller elements and
+// their PSD-weighted sums over sizes stay in its registers: no shared-memory
+// staging, no shuffles and no barrier among the epilogue warps.
+//
 // Pipeline (one CTA per SM, persistent, 10 warps):
-//   warps 0-7   epilogue: TMEM -> window sums -> Mueller -> PSD-weighted sums
+//   warps 0-7   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
+//               angles) and columns of sizes 16 (w / 4) .. + 15 of the half
+//               tile; window sums -> Mueller -> PSD-weighted sums
 //   warp 8      MMA issue (one thread)
-//   warp 9      producer (one thread): bulk copies of the split A operand
-//               (split_rows) and of B orders > 16 into a TC_NS-stage
-//               shared-memory ring
-// Angles go in blocks of 64 (MMA N = 64); TMEM holds TC_NSETS accumulator
-// sets (S+ 64 columns | S- 64 columns), so the MMAs run up to four windows
-// ahead of the epilogue.  The B chunk of orders 1..16 stays resident for up
-// to TC_B0_SLOTS angle blocks (loaded once: it is the same for every unit;
-// 84% of the sulfate-like table's 64-size tiles need no other order); with
-// more blocks one slot is reloaded at every block change.  mbarriers: stage
-// full/empty, resident-B full/empty, accumulator-set full/empty.  Every wait
-// is bounded and also ends when another role has raised the block's abort
-// flag; role-wide decisions are taken by one thread and shared through a
-// named barrier, so each role leaves its loops uniformly.
+//   warp 9      producer (one thread): bulk copies of the coefficient half
+//               tiles (split_rows) and of the angle functions of orders > 16
+//               into a TC_NS-stage shared-memory ring
+// Work items are (unit, angle block, 64-size tile, half tile); a half tile
+// without sizes (the last tile of a grid) is skipped by every role.  TMEM
+// holds TC_NSETS accumulator sets (S+ 64 columns | S- 64 columns), so the
+// MMAs run up to four windows ahead of the epilogue.  The angle-function
+// chunk of orders 1..16 stays resident for up to TC_B0_SLOTS angle blocks
+// (loaded once: it is the same for every unit; 84% of the sulfate-like
+// table's tiles need no other order); with more blocks one slot is reloaded
+// at every (unit, block) change.  mbarriers: stage full/empty, resident
+// full/empty, accumulator-set full/empty.  Every wait is bounded and also
+// ends when another role has raised the block's abort flag; the epilogue
+// warps decide per warp (lane 0 waits, the warp follows its answer).
 // ---------------------------------------------------------------------------
 struct TcArgs {
     TabView v;
@@ -457,7 +474,7 @@ struct TcArgs {
     const __half *bt;
     int n_pad, k_pad;
     const int *unit_order;
-    const uint8_t *asplit;       // split A operand (split_rows)
+    const uint8_t *asplit;       // coefficient operand (split_rows)
     const int *tile_cbase;       // [n_le][ntiles + 1]
     const int64_t *unit_cbase;   // [n_units]
     int ntiles;
@@ -469,22 +486,24 @@ struct TcArgs {
 #define TC_NS 4                                        // ring stages
 #define TC_WIN_MAX TC_NS                               // longest accumulation window (chunks)
 #define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
-#define TC_B0_SLOTS 4                                  // resident B chunks (angle blocks)
-#define TC_A16_MAT (TC_KC16 * 128 * 2)                 // one A matrix of a chunk: 4 KB
-#define TC_A16_BYTES (4 * TC_A16_MAT)                  // C_hi C_lo D_hi D_lo: 16 KB
-#define TC_B16_MAT (TC_KC16 * TC_NBLK * 2)             // one B matrix of a chunk: 2 KB
-#define TC_B16_BYTES (4 * TC_B16_MAT)                  // P_hi P_lo Q_hi Q_lo: 8 KB
-#define TC_STAGE_BYTES (TC_A16_BYTES + TC_B16_BYTES)   // 24 KB
-#define TC_STAGE_PITCH 66                              // 64 columns + 2: conflict-free pair writes
-#define TC_STAGE_FLOATS (4 * TC_INST * TC_STAGE_PITCH) // Mueller staging [k][size][col]: 66 KB
-#define TC_EPI_THREADS 256
-#define TC_THREADS (TC_EPI_THREADS + 64)             // + the MMA warp and the producer warp
-#define TC_SMEM_BYTES                                                                                  \
-    (TC_B0_SLOTS * TC_B16_BYTES + TC_NS * TC_STAGE_BYTES + TC_STAGE_FLOATS * 4 + 8 * TC_INST * 4 + 256)
-#define TC_BAR_EPI 1                                   // named barrier id of the epilogue warps
+// resident angle-function chunks (angle blocks): 3 leave room for the running
+// sums of 6-8 bins
+#define TC_B0_SLOTS(NB) ((NB) > 5 ? 3 : 4)
+#define TC_A_BYTES (4 * TC_MAT_A)                      // P_hi P_lo Q_hi Q_lo of a chunk: 16 KB
+#define TC_B_BYTES (4 * TC_MAT_B)                      // C_hi C_lo D_hi D_lo of a half chunk: 8 KB
+#define TC_STAGE_BYTES (TC_B_BYTES + TC_A_BYTES)       // 24 KB
+#define TC_EPI_WARPS 8
+#define TC_EPI_THREADS (32 * TC_EPI_WARPS)
+#define TC_THREADS (TC_EPI_THREADS + 64)               // + the MMA warp and the producer warp
+#define TC_WBUF_FLOATS (2 * 16 * 16)                   // per epilogue warp: 2 items x 16 sizes x 8 bins x 2
+#define TC_SUM_FLOATS(NB) (2 * 4 * (NB) * TC_EPI_THREADS) // running sums (hi, lo) [2][4 NB][thread]
+#define TC_SMEM_BYTES(NB)                                                                                  \
+    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS * TC_STAGE_BYTES + TC_EPI_WARPS * TC_WBUF_FLOATS * 4 +               \
+     TC_SUM_FLOATS(NB) * 4 + 256)
 #define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
 
 static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
+static_assert(TC_SMEM_BYTES(5) <= 227 * 1024 && TC_SMEM_BYTES(8) <= 227 * 1024, "shared memory");
 
 // k-th unit of CTA `cta` among G CTAs: units in decreasing-work order,
 // dealt in a snake (c, then G-1-c) so that every CTA gets a similar mix.
@@ -493,43 +512,27 @@ __device__ __forceinline__ int64_t tc_unit_index(int k, int cta, int G)
     return (int64_t)k * G + ((k & 1) ? (G - 1 - cta) : cta);
 }
 
-// Chunk j (orders 16 j + 1 .. 16 j + 16) of angle block blk of the four B
-// matrices, global [m][k/8][angle/8][8][8] -> shared [m][kg][ng][8][8]: per
-// (m, kg) one contiguous run of 8 core matrices (1 KB).  One thread; the
-// caller has armed `bar` with the bytes (mbar_arrive_expect_tx).
-__device__ __forceinline__ void tc_copy_b16(const TcArgs &g, uint8_t *dst, int j, int blk, uint64_t *bar)
-{
-    const int ngt = g.n_pad / 8, nng = TC_NBLK / 8;
-    const size_t mat = (size_t)g.n_pad * g.k_pad;
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int kg = 0; kg < 2; ++kg) {
-            const __half *src = g.bt + m * mat + ((size_t)(2 * j + kg) * ngt + (size_t)blk * nng) * 64;
-            bulk_g2s(dst + m * TC_B16_MAT + kg * nng * 128, src, nng * 128, bar);
-        }
-}
-
 template <int NB>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sB0 = smem;                                            // resident B chunks, orders 1..16
-    uint8_t *sStage = sB0 + TC_B0_SLOTS * TC_B16_BYTES;             // TC_NS x (A 16 KB | B 8 KB)
-    float *stage = (float *)(sStage + TC_NS * TC_STAGE_BYTES);     // Mueller staging [4][64][66]
-    float *sw = stage + TC_STAGE_FLOATS;                            // [64 sizes][8 bins]
-    uint64_t *bars = (uint64_t *)(sw + 8 * TC_INST);
+    uint8_t *sB0 = smem;                                            // resident angle chunks, orders 1..16
+    uint8_t *sStage = sB0 + TC_B0_SLOTS(NB) * TC_A_BYTES;           // TC_NS x (coeff 8 KB | angles 16 KB)
+    float *sW = (float *)(sStage + TC_NS * TC_STAGE_BYTES);         // per epilogue warp [2][16 sizes][8 bins]
+    float *sSum = sW + TC_EPI_WARPS * TC_WBUF_FLOATS;               // per-(unit, block) sums [2][4 NB][thread]
+    uint64_t *bars = (uint64_t *)(sSum + TC_SUM_FLOATS(NB));
     uint64_t *full = bars, *empty = bars + TC_NS;
     uint64_t *b0_full = bars + 2 * TC_NS, *b0_empty = b0_full + 1;
     uint64_t *acc_full = b0_full + 2, *acc_empty = acc_full + TC_NSETS, *drain = acc_empty + TC_NSETS;
     uint32_t *s_tmem = (uint32_t *)(drain + 1);
     volatile int *s_abort = (volatile int *)(s_tmem + 1);
-    volatile int *s_epi_go = s_abort + 1;    // [2] epilogue: 1 = accumulator set ready, 0 = stop
 
     const TabView &v = g.v;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nblocks = g.n_pad / TC_NBLK;
-    const bool reload = nblocks > TC_B0_SLOTS;   // one resident slot, reloaded per block
+    const int nblocks = g.n_pad / TC_ABLK;
+    const int nkc = g.k_pad / TC_KC16;
+    const int ntl = g.ntiles;
+    const bool reload = nblocks > TC_B0_SLOTS(NB);   // one resident slot, reloaded per (unit, block)
     if (warp == 0) tmem_alloc(s_tmem, 512);
     if (tid == 0) {
         for (int i = 0; i < TC_NS; ++i) {
@@ -540,7 +543,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         mbar_init(b0_empty, 1);
         for (int i = 0; i < TC_NSETS; ++i) {
             mbar_init(acc_full + i, 1);
-            mbar_init(acc_empty + i, TC_EPI_THREADS / 32);
+            mbar_init(acc_empty + i, TC_EPI_WARPS);
         }
         mbar_init(drain, 1);
         fence_mbar_init();
@@ -556,10 +559,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
     if (warp == 8) {
         // ================= MMA issue =================
         if (lane == 0) {
-            const uint32_t idesc = idesc_f16_f32(128, TC_NBLK);
+            const uint32_t idesc = idesc_f16_f32(TC_ABLK, 2 * TC_HALF);
             uint32_t it = 0, item = 0, b0_loads = 0;
-            int prev_blk = -1;
-            bool ok = true;
+            bool ok = true, have_b0 = false;
             if (!reload) {   // every block's resident chunk, loaded once
                 ok = mbar_wait_or_abort(b0_full, 0, s_abort, TC_SLEEP_NS);
                 b0_loads = 1;
@@ -570,66 +572,67 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 const int64_t unit = g.unit_order[uidx];
                 const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
                 const int64_t *off = v.off + (int64_t)v.le(lam) * v.n_size;
-                for (int blk = 0; blk < nblocks && ok; ++blk) {
-                    if (reload && blk != prev_blk) {   // the producers reload the resident slot
-                        if (prev_blk >= 0) mma_commit(b0_empty);
+                for (int ab = 0; ab < nblocks && ok; ++ab) {
+                    if (reload) {   // the producer reloads the resident slot
+                        if (have_b0) mma_commit(b0_empty);
                         if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort, TC_SLEEP_NS)) {
                             ok = false;
                             break;
                         }
                         ++b0_loads;
-                        prev_blk = blk;
+                        have_b0 = true;
                     }
-                    const uint32_t aB0 = smem_u32(sB0 + (reload ? 0 : blk) * TC_B16_BYTES);
-                    for (int t0 = 0; t0 < v.n_size && ok; t0 += TC_INST) {
-                        const int ntile = min(TC_INST, v.n_size - t0);
+                    const uint32_t aB0 = smem_u32(sB0 + (reload ? 0 : ab) * TC_A_BYTES);
+                    for (int tile = 0; tile < ntl && ok; ++tile) {
+                        const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
                         const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
                         const int nc = (kt + TC_KC16 - 1) / TC_KC16;
-                        for (int w0 = 0; w0 < nc && ok; w0 += g.win) {
-                            const int nj = min(g.win, nc - w0);
-                            const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
-                            if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, TC_SLEEP_NS)) {
-                                ok = false;
-                                break;
-                            }
-                            for (int j = 0; j < nj && ok; ++j) {
-                                const uint32_t c = it + j;
-                                ok = mbar_wait_or_abort(full + c % TC_NS, (c / TC_NS) & 1u, s_abort, TC_SLEEP_NS);
-                            }
-                            if (!ok) break;
-                            tc_fence_after();
-                            const uint32_t d = tmem + set * 128;   // S+ at d, S- at d + 64
-                            for (int pass = 0; pass < 2; ++pass) {
-                                for (int j = 0; j < nj; ++j) {
+                        for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h) {
+                            for (int w0 = 0; w0 < nc && ok; w0 += g.win) {
+                                const int nj = min(g.win, nc - w0);
+                                const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
+                                if (use > 0 &&
+                                    !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, TC_SLEEP_NS)) {
+                                    ok = false;
+                                    break;
+                                }
+                                for (int j = 0; j < nj && ok; ++j) {
                                     const uint32_t c = it + j;
-                                    const uint32_t aA = smem_u32(sStage + (c % TC_NS) * TC_STAGE_BYTES);
-                                    const uint32_t aB = (w0 + j) == 0 ? aB0 : aA + TC_A16_BYTES;
-                                    // A: LBO (K step of 8 orders) = 16 core matrices; B: 8
-                                    const uint64_t a_chi = smem_desc(aA + 0 * TC_A16_MAT, 16 * 128, 128);
-                                    const uint64_t a_dhi = smem_desc(aA + 2 * TC_A16_MAT, 16 * 128, 128);
-                                    const uint64_t b_phi = smem_desc(aB + 0 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
-                                    const uint64_t b_qhi = smem_desc(aB + 2 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
-                                    if (pass == 0) {   // cross products: small accumulator
-                                        const uint64_t a_clo = smem_desc(aA + 1 * TC_A16_MAT, 16 * 128, 128);
-                                        const uint64_t a_dlo = smem_desc(aA + 3 * TC_A16_MAT, 16 * 128, 128);
-                                        const uint64_t b_plo =
-                                            smem_desc(aB + 1 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
-                                        const uint64_t b_qlo =
-                                            smem_desc(aB + 3 * TC_B16_MAT, (TC_NBLK / 8) * 128, 128);
-                                        mma_f16(d, a_chi, b_plo, idesc, j == 0 ? 0u : 1u);
-                                        mma_f16(d, a_clo, b_phi, idesc, 1u);
-                                        mma_f16(d + 64, a_dhi, b_qlo, idesc, j == 0 ? 0u : 1u);
-                                        mma_f16(d + 64, a_dlo, b_qhi, idesc, 1u);
-                                    } else {
-                                        mma_f16(d, a_chi, b_phi, idesc, 1u);
-                                        mma_f16(d + 64, a_dhi, b_qhi, idesc, 1u);
-                                        mma_commit(empty + c % TC_NS);   // stage free when its MMAs are done
+                                    ok = mbar_wait_or_abort(full + c % TC_NS, (c / TC_NS) & 1u, s_abort, TC_SLEEP_NS);
+                                }
+                                if (!ok) break;
+                                tc_fence_after();
+                                const uint32_t d = tmem + set * 128;   // S+ at d, S- at d + 64
+                                for (int pass = 0; pass < 2; ++pass) {
+                                    for (int j = 0; j < nj; ++j) {
+                                        const uint32_t c = it + j;
+                                        const uint32_t sB = smem_u32(sStage + (c % TC_NS) * TC_STAGE_BYTES);
+                                        const uint32_t sA = (w0 + j) == 0 ? aB0 : sB + TC_B_BYTES;
+                                        // A (angles): LBO = 16 core matrices (K step of 8 orders); B: 8
+                                        const uint64_t p_hi = smem_desc(sA + 0 * TC_MAT_A, 16 * 128, 128);
+                                        const uint64_t q_hi = smem_desc(sA + 2 * TC_MAT_A, 16 * 128, 128);
+                                        const uint64_t c_hi = smem_desc(sB + 0 * TC_MAT_B, 8 * 128, 128);
+                                        const uint64_t d_hi = smem_desc(sB + 2 * TC_MAT_B, 8 * 128, 128);
+                                        if (pass == 0) {   // cross products: small accumulator
+                                            const uint64_t p_lo = smem_desc(sA + 1 * TC_MAT_A, 16 * 128, 128);
+                                            const uint64_t q_lo = smem_desc(sA + 3 * TC_MAT_A, 16 * 128, 128);
+                                            const uint64_t c_lo = smem_desc(sB + 1 * TC_MAT_B, 8 * 128, 128);
+                                            const uint64_t d_lo = smem_desc(sB + 3 * TC_MAT_B, 8 * 128, 128);
+                                            mma_f16(d, p_hi, c_lo, idesc, j == 0 ? 0u : 1u);
+                                            mma_f16(d, p_lo, c_hi, idesc, 1u);
+                                            mma_f16(d + 64, q_hi, d_lo, idesc, j == 0 ? 0u : 1u);
+                                            mma_f16(d + 64, q_lo, d_hi, idesc, 1u);
+                                        } else {
+                                            mma_f16(d, p_hi, c_hi, idesc, 1u);
+                                            mma_f16(d + 64, q_hi, d_hi, idesc, 1u);
+                                            mma_commit(empty + c % TC_NS);   // stage free when its MMAs are done
+                                        }
                                     }
                                 }
+                                it += nj;
+                                mma_commit(acc_full + set);
+                                ++item;
                             }
-                            it += nj;
-                            mma_commit(acc_full + set);
-                            ++item;
                         }
                     }
                 }
@@ -647,13 +650,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         // ================= producer: bulk copies (one thread) =================
         if (lane == 0) {
             uint32_t it = 0, b0_loads = 0;
-            int prev_blk = -1;
             uint64_t *last_tx = nullptr;   // barrier of the last bulk copy, and its phase
             uint32_t last_tx_phase = 0;
             bool ok = true;
             if (!reload) {
-                mbar_arrive_expect_tx(b0_full, (uint32_t)(nblocks * TC_B16_BYTES));
-                for (int b = 0; b < nblocks; ++b) tc_copy_b16(g, sB0 + b * TC_B16_BYTES, 0, b, b0_full);
+                mbar_arrive_expect_tx(b0_full, (uint32_t)(nblocks * TC_A_BYTES));
+                for (int b = 0; b < nblocks; ++b)
+                    bulk_g2s(sB0 + b * TC_A_BYTES, (const uint8_t *)g.bt + (size_t)b * nkc * TC_A_BYTES, TC_A_BYTES,
+                             b0_full);
                 last_tx = b0_full;
                 last_tx_phase = 0;
             }
@@ -662,36 +666,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 if (uidx >= n_units) break;
                 const int64_t unit = g.unit_order[uidx];
                 const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
-                const int *tcb = g.tile_cbase + (size_t)v.le(lam) * (g.ntiles + 1);
-                const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * TC_A16_BYTES;
-                for (int blk = 0; blk < nblocks && ok; ++blk) {
-                    if (reload && blk != prev_blk) {
-                        if (prev_blk >= 0 && !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort, TC_SLEEP_NS)) {
+                const int *tcb = g.tile_cbase + (size_t)v.le(lam) * (ntl + 1);
+                const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * (2 * TC_B_BYTES);
+                for (int ab = 0; ab < nblocks && ok; ++ab) {
+                    const uint8_t *gA = (const uint8_t *)g.bt + (size_t)ab * nkc * TC_A_BYTES;
+                    if (reload) {
+                        if (b0_loads > 0 &&
+                            !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort, TC_SLEEP_NS)) {
                             ok = false;
                             break;
                         }
-                        mbar_arrive_expect_tx(b0_full, TC_B16_BYTES);
-                        tc_copy_b16(g, sB0, 0, blk, b0_full);
+                        mbar_arrive_expect_tx(b0_full, TC_A_BYTES);
+                        bulk_g2s(sB0, gA, TC_A_BYTES, b0_full);
                         last_tx = b0_full;
                         last_tx_phase = b0_loads & 1u;
                         ++b0_loads;
-                        prev_blk = blk;
                     }
-                    for (int tile = 0; tile < g.ntiles && ok; ++tile) {
+                    for (int tile = 0; tile < ntl && ok; ++tile) {
+                        const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
                         const int nc = tcb[tile + 1] - tcb[tile];
-                        for (int j = 0; j < nc; ++j) {
-                            const uint32_t c = it++;
-                            const int st = (int)(c % TC_NS);
-                            uint8_t *sA = sStage + st * TC_STAGE_BYTES;
-                            if (c >= TC_NS && !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort, TC_SLEEP_NS)) {
-                                ok = false;
-                                break;
+                        for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h) {
+                            for (int j = 0; j < nc; ++j) {
+                                const uint32_t c = it++;
+                                const int st = (int)(c % TC_NS);
+                                uint8_t *sS = sStage + st * TC_STAGE_BYTES;
+                                if (c >= TC_NS &&
+                                    !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort, TC_SLEEP_NS)) {
+                                    ok = false;
+                                    break;
+                                }
+                                mbar_arrive_expect_tx(full + st, TC_B_BYTES + (j > 0 ? TC_A_BYTES : 0));
+                                bulk_g2s(sS, ua + ((size_t)(tcb[tile] + j) * 2 + h) * TC_B_BYTES, TC_B_BYTES, full + st);
+                                if (j > 0) bulk_g2s(sS + TC_B_BYTES, gA + (size_t)j * TC_A_BYTES, TC_A_BYTES, full + st);
+                                last_tx = full + st;
+                                last_tx_phase = (c / TC_NS) & 1u;
                             }
-                            mbar_arrive_expect_tx(full + st, TC_A16_BYTES + (j > 0 ? TC_B16_BYTES : 0));
-                            bulk_g2s(sA, ua + (size_t)(tcb[tile] + j) * TC_A16_BYTES, TC_A16_BYTES, full + st);
-                            if (j > 0) tc_copy_b16(g, sA + TC_A16_BYTES, j, blk, full + st);
-                            last_tx = full + st;
-                            last_tx_phase = (c / TC_NS) & 1u;
                         }
                     }
                 }
@@ -706,20 +715,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         __syncwarp();
     } else {
         // ================= epilogue (warps 0-7) =================
-        // One flat sequence of tiles s = (unit k, angle block, 64-size tile);
-        // the PSD weights of tile s + 1 are fetched into registers while tile
-        // s is processed and land in shared memory after its last barrier.
-        uint32_t item = 0;
-        bool ok = true;
-        const int q = warp & 3, half = warp >> 2;
-        const int il = 16 * q + (lane >> 1);
-        const bool odd = lane & 1;
-        const int kk = warp >> 1, cg = warp & 1, hh = lane >> 4, cp = lane & 15;
-        const int ntl = g.ntiles;
+        // Items in the MMA's order.  The PSD weights and the order count of
+        // item i + 1 are loaded while item i is processed; the weights go into
+        // this warp's other weight buffer at the start of item i + 1.
+        // Per size the thread forms E0 = (|S+|^2, |S-|^2) and
+        // E1 = (Re S+ S-*, Im S- S+*) and adds w_b E0, w_b E1 with packed FP32
+        // pair FMAs; the constant factors of the Mueller elements
+        //   s11 = (|S+|^2 + |S-|^2)/4, s12 = -Re(S+ S-*)/2,
+        //   s33 = (|S+|^2 - |S-|^2)/4, s34 = -Im(S- S+*)/2
+        // are applied to the unit's sums.
+        const int q = warp & 3, wh = warp >> 2;
+        float *wbuf = sW + warp * TC_WBUF_FLOATS;   // [2 items][16 sizes][8 bins][w, w]
         // per-unit constants of this CTA's kq-th unit (valid = false past its last unit)
         struct UnitC {
             bool valid;
-            int comp, lr, lam, E;
+            int comp, lr, E;
             const float *Wb;
             const int *ex;
             const int64_t *off;
@@ -732,88 +742,115 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
             const int unit = g.unit_order[uidx];
             u.comp = unit % v.n_comp;
             u.lr = unit / v.n_comp;
-            u.lam = u.lr / v.n_rh;
-            const int rhi = u.lr - u.lam * v.n_rh;
-            u.Wb = v.Wf + v.wlam(u.lam) + ((size_t)rhi * v.n_bin * v.n_comp + u.comp) * v.n_size;
+            const int lam = u.lr / v.n_rh;
+            const int rhi = u.lr - lam * v.n_rh;
+            u.Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + u.comp) * v.n_size;
             u.ex = g.eexp + (size_t)unit * v.n_size;
             u.E = g.eunit[unit];
-            u.off = v.off + (int64_t)v.le(u.lam) * v.n_size;
+            u.off = v.off + (int64_t)v.le(lam) * v.n_size;
             return u;
         };
-        // PSD weights of a tile scaled by 2^(2 (e_i - E)) (E is the unit's largest
-        // exponent, so the power is <= 1; below 2^-126 the weight is dropped) for
-        // this thread's two entries idx = tid, tid + 256 of [64 sizes][8 bins]
-        auto fetch_w = [&](const UnitC &u, int tile, float &w0, float &w1) {
-            const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
-            float w[2];
+        // PSD weights scaled by 2^(2 (e_i - E)) (E is the unit's largest
+        // exponent, so the power is <= 1; below 2^-126 the weight is dropped)
+        // of this warp's 16 sizes of half tile h: lane l holds size l / 2,
+        // bins 4 (l % 2) .. + 3
+        auto fetch_w = [&](const UnitC &u, int tile, int h, float4 &wv) {
+            const int si = tile * TC_INST + TC_HALF * h + 16 * wh + (lane >> 1);
+            const int b0 = 4 * (lane & 1);
+            float w[4] = {0.f, 0.f, 0.f, 0.f};
+            if (si < v.n_size && b0 < NB) {
+                const int e = 2 * (u.ex[si] - u.E);
+                const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
 #pragma unroll
-            for (int h2 = 0; h2 < 2; ++h2) {
-                const int idx = tid + h2 * TC_EPI_THREADS, b = idx & 7, i = idx >> 3;
-                w[h2] = 0.f;
-                if (i < ntile && b < v.n_bin && b < NB) {
-                    const int e = 2 * (u.ex[t0 + i] - u.E);
-                    const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
-                    w[h2] = u.Wb[(size_t)b * v.n_comp * v.n_size + t0 + i] * p2;
+                for (int bb = 0; bb < 4; ++bb) {
+                    const int b = b0 + bb;
+                    if (b < v.n_bin && b < NB) w[bb] = u.Wb[(size_t)b * v.n_comp * v.n_size + si] * p2;
                 }
             }
-            w0 = w[0];
-            w1 = w[1];
+            wv = make_float4(w[0], w[1], w[2], w[3]);
         };
-        float wn0 = 0.f, wn1 = 0.f;
-        UnitC cu = unit_c(0);
-        if (cu.valid) {
-            fetch_w(cu, 0, wn0, wn1);
-            sw[tid] = wn0;
-            sw[tid + TC_EPI_THREADS] = wn1;
-        }
-        float uh[2][NB], ul[2][NB];   // per-(unit, block) sums, unevaluated FP32 pairs (two-sum)
-        int kq = 0, blk = 0, tile = 0;   // the tile sequence: units, angle blocks, 64-size tiles
-        while (ok && cu.valid) {
-            const int comp = cu.comp, lr = cu.lr;
-            const int64_t *off = cu.off;
+        // 16-order chunks of a tile (its last size has the largest nmax)
+        auto tile_chunks = [&](const UnitC &u, int tile) -> int {
             const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
-            const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
-            const int nwin = ((kt + TC_KC16 - 1) / TC_KC16 + g.win - 1) / g.win;
-            if (tile == 0) {
+            return (int)((u.off[t0 + ntile] - u.off[t0 + ntile - 1] + TC_KC16 - 1) / TC_KC16);
+        };
+        constexpr int NP = (NB + 1) / 2;   // 16-byte weight loads per size: two bins each
+        bool ok = true;
+        uint32_t item = 0, ie = 0;
+        int kq = 0, ab = 0, tile = 0, h = 0;
+        UnitC cu = unit_c(0);
+        float4 wn = make_float4(0.f, 0.f, 0.f, 0.f);
+        int nc = 0;
+        if (cu.valid) {
+            nc = tile_chunks(cu, 0);
+            if (32 * q < v.n_ang) fetch_w(cu, 0, 0, wn);
+        }
+        // tile sums in registers; per-(unit, block) sums as unevaluated pairs
+        // (hi + lo) in this thread's column of sSum: [hi, lo][2 NB pairs][thread]
+        f32x2 acc[2][NB];
+        f32x2 *suh = (f32x2 *)sSum + tid, *sul = suh + 2 * NB * TC_EPI_THREADS;
 #pragma unroll
-                for (int c = 0; c < 2; ++c)
+        for (int e = 0; e < 2; ++e)
 #pragma unroll
-                    for (int b = 0; b < NB; ++b) uh[c][b] = ul[c][b] = 0.f;
+            for (int b = 0; b < NB; ++b) {
+                acc[e][b] = 0ull;
+                suh[(e * NB + b) * TC_EPI_THREADS] = 0ull;
+                sul[(e * NB + b) * TC_EPI_THREADS] = 0ull;
             }
-            int nk = kq, nb = blk, nt = tile + 1;   // the next tile
-            if (nt == ntl) {
-                nt = 0;
-                if (++nb == nblocks) {
-                    nb = 0;
-                    ++nk;
+        while (ok && cu.valid) {
+            const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
+            const int nwin = (nc + g.win - 1) / g.win;
+            const bool active = TC_ABLK * ab + 32 * q < v.n_ang;   // this warp has angles in the block
+            // the next item
+            int nk = kq, nab = ab, nt = tile, nh = h + 1;
+            if (nh == 2 || TC_HALF * nh >= ntile) {
+                nh = 0;
+                if (++nt == ntl) {
+                    nt = 0;
+                    if (++nab == nblocks) {
+                        nab = 0;
+                        ++nk;
+                    }
                 }
             }
             const UnitC nu = nk == kq ? cu : unit_c(nk);
-            const bool have_next = nu.valid;
-            if (have_next) fetch_w(nu, nt, wn0, wn1);   // in flight during this tile
-            // window sums of S+ and S- (Re/Im of this lane's row, 32 columns)
+            float *wb = wbuf + (ie & 1) * (TC_WBUF_FLOATS / 2);
+            if (active) {   // duplicated pairs (w_b, w_b) for the packed FMAs
+                *(float4 *)(wb + 8 * lane) = make_float4(wn.x, wn.x, wn.y, wn.y);
+                *(float4 *)(wb + 8 * lane + 4) = make_float4(wn.z, wn.z, wn.w, wn.w);
+            }
+            __syncwarp();
+            int nc_next = 0;
+            if (nu.valid) {   // in flight during this item
+                nc_next = nh == 0 ? tile_chunks(nu, nt) : nc;
+                if (TC_ABLK * nab + 32 * q < v.n_ang) fetch_w(nu, nt, nh, wn);
+            }
+            // window sums of S+ and S- (this lane's angle, 16 sizes x Re/Im)
             float rp[32], rm[32];
             for (int w = 0; w < nwin; ++w) {
                 const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
-                if (tid == 0) s_epi_go[item & 1] = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
-                named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
-                if (!s_epi_go[item & 1]) {
+                int go = 1;
+                if (lane == 0) go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
+                go = __shfl_sync(0xffffffffu, go, 0);
+                if (!go) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * half;
-                if (w == 0) {
-                    tmem_ld32(ta, rp);
-                    tmem_ld32(ta + 64, rm);
-                } else {
-                    float t[32];
-                    tmem_ld32(ta, t);
+                if (active) {
+                    const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * wh;
+                    if (w == 0) {
+                        tmem_ld32(ta, rp);
+                        tmem_ld32(ta + 64, rm);
+                    } else {
+                        float t[32];
+                        tmem_ld32(ta, t);
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) rp[i] += t[i];
-                    tmem_ld32(ta + 64, t);
+                        for (int i = 0; i < 32; ++i) rp[i] += t[i];
+                        tmem_ld32(ta + 64, t);
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) rm[i] += t[i];
+                        for (int i = 0; i < 32; ++i) rm[i] += t[i];
+                    }
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -821,97 +858,85 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 ++item;
             }
             if (!ok) break;
-            // Mueller phase: warp (q = TMEM lane quarter, half = warp / 4) holds
-            // rows 32 q .. + 31 (sizes 16 q .. + 15, Re/Im lane pairs) for 32
-            // columns; the even lane forms column 2p and the odd lane 2p + 1.
-            float *strow = stage + il * TC_STAGE_PITCH + 32 * half + (odd ? 1 : 0);
+            if (active) {
 #pragma unroll
-            for (int pj = 0; pj < 16; ++pj) {
-                const int j0 = 2 * pj, j1 = 2 * pj + 1;
-                const float xp = __shfl_xor_sync(0xffffffffu, odd ? rp[j0] : rp[j1], 1);
-                const float xm = __shfl_xor_sync(0xffffffffu, odd ? rm[j0] : rm[j1], 1);
-                const float pr = odd ? xp : rp[j0], pi = odd ? rp[j1] : xp;
-                const float mr = odd ? xm : rm[j0], mi = odd ? rm[j1] : xm;
-                const float A2 = pr * pr + pi * pi, B2 = mr * mr + mi * mi;
-                float *st = strow + j0;
-                st[0 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 + B2);
-                st[1 * TC_INST * TC_STAGE_PITCH] = -0.5f * (pr * mr + pi * mi);
-                st[2 * TC_INST * TC_STAGE_PITCH] = 0.25f * (A2 - B2);
-                st[3 * TC_INST * TC_STAGE_PITCH] = -0.5f * (mr * pi - mi * pr);
-            }
-            named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
-            // Reduction phase: warp w sums element kk = w / 2 over columns
-            // 32 (w % 2) + 2 cp + {0, 1} (cp = lane % 16) and sizes 32 h .. + 31
-            // (h = lane / 16) for every bin; the two halves meet by a shuffle.
-            {
-                float acc[2][NB];
+                for (int s = 0; s < 16; ++s) {
+                    const float pr = rp[2 * s], pi = rp[2 * s + 1], mr = rm[2 * s], mi = rm[2 * s + 1];
+                    const f32x2 e0 = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
+                    const f32x2 e1 = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
+                    const ulonglong2 *wp = (const ulonglong2 *)(wb + 16 * s);
 #pragma unroll
-                for (int c = 0; c < 2; ++c)
-#pragma unroll
-                    for (int b = 0; b < NB; ++b) acc[c][b] = 0.f;
-                const float *src = stage + (kk * TC_INST + 32 * hh) * TC_STAGE_PITCH + 32 * cg + 2 * cp;
-                const float *wsrc = sw + 32 * hh * 8;
-#pragma unroll 4
-                for (int i = 0; i < 32; ++i) {
-                    const float2 sv = *(const float2 *)(src + i * TC_STAGE_PITCH);
-                    const float4 w0 = *(const float4 *)(wsrc + 8 * i);
-                    float wv[8] = {w0.x, w0.y, w0.z, w0.w, 0.f, 0.f, 0.f, 0.f};
-                    if (NB > 4) {
-                        const float4 w1 = *(const float4 *)(wsrc + 8 * i + 4);
-                        wv[4] = w1.x;
-                        wv[5] = w1.y;
-                        wv[6] = w1.z;
-                        wv[7] = w1.w;
-                    }
-#pragma unroll
-                    for (int b = 0; b < NB; ++b) {
-                        acc[0][b] = fmaf(wv[b], sv.x, acc[0][b]);
-                        acc[1][b] = fmaf(wv[b], sv.y, acc[1][b]);
-                    }
-                }
-#pragma unroll
-                for (int c = 0; c < 2; ++c)
-#pragma unroll
-                    for (int b = 0; b < NB; ++b) {
-                        const float a = acc[c][b] + __shfl_xor_sync(0xffffffffu, acc[c][b], 16);
-                        // two-sum: (uh + ul) += a exactly-rounded
-                        const float sum = uh[c][b] + a;
-                        const float bp = sum - uh[c][b];
-                        ul[c][b] += (uh[c][b] - (sum - bp)) + (a - bp);
-                        uh[c][b] = sum;
-                    }
-            }
-            named_bar_sync(TC_BAR_EPI, TC_EPI_THREADS);
-            // every reader of sw and stage has passed the barrier: the next tile's weights go in
-            if (have_next) {
-                sw[tid] = wn0;
-                sw[tid + TC_EPI_THREADS] = wn1;
-            }
-            if (tile == ntl - 1 && hh == 0) {
-                // unit results of this angle block: lanes of the first size half
-                // hold the combined sums of (element kk, two columns)
-                const double f2 = ldexp(1.0, 2 * (cu.E - SHIFT_BITS));
-#pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    const int col = blk * TC_NBLK + 32 * cg + 2 * cp + c;
-                    if (col < v.n_ang) {
-#pragma unroll
-                        for (int b = 0; b < NB; ++b) {
-                            if (b < v.n_bin) {
-                                const double f = v.frac[(size_t)b * v.n_comp + comp];
-                                atomicAdd(v.pacc + (((size_t)lr * v.n_bin + b) * 4 + kk) * v.n_ang + col,
-                                          f * ((double)uh[c][b] + (double)ul[c][b]) * f2);
-                            }
+                    for (int p = 0; p < NP; ++p) {
+                        const ulonglong2 w2 = wp[p];   // (w_2p, w_2p), (w_2p+1, w_2p+1)
+                        acc[0][2 * p] = f2_fma(w2.x, e0, acc[0][2 * p]);
+                        acc[1][2 * p] = f2_fma(w2.x, e1, acc[1][2 * p]);
+                        if (2 * p + 1 < NB) {
+                            acc[0][2 * p + 1] = f2_fma(w2.y, e0, acc[0][2 * p + 1]);
+                            acc[1][2 * p + 1] = f2_fma(w2.y, e1, acc[1][2 * p + 1]);
                         }
                     }
                 }
             }
+            if (nh == 0) {
+                // end of a tile: two-sum (hi + lo) += acc, exactly rounded
+#pragma unroll
+                for (int e = 0; e < 2; ++e)
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) {
+                        const int o = (e * NB + b) * TC_EPI_THREADS;
+                        const f32x2 a = acc[e][b], hi = suh[o];
+                        const f32x2 sum = f2_add(hi, a);
+                        const f32x2 bp = f2_sub(sum, hi);
+                        sul[o] = f2_add(sul[o], f2_add(f2_sub(hi, f2_sub(sum, bp)), f2_sub(a, bp)));
+                        suh[o] = sum;
+                        acc[e][b] = 0ull;
+                    }
+                if (nt == 0) {
+                    // end of the (unit, angle block): this thread's share of the unit's sums
+                    const int ang = TC_ABLK * ab + 32 * q + lane;
+                    if (ang < v.n_ang) {
+                        const double f2 = ldexp(1.0, 2 * (cu.E - SHIFT_BITS));
+#pragma unroll
+                        for (int b = 0; b < NB; ++b) {
+                            if (b < v.n_bin) {
+                                const double f = v.frac[(size_t)b * v.n_comp + cu.comp] * f2;
+                                double e[4];
+#pragma unroll
+                                for (int ee = 0; ee < 2; ++ee) {
+                                    const int o = (ee * NB + b) * TC_EPI_THREADS;
+                                    float h0, h1, l0, l1;
+                                    f2_unpack(suh[o], h0, h1);
+                                    f2_unpack(sul[o], l0, l1);
+                                    e[2 * ee] = (double)h0 + (double)l0;
+                                    e[2 * ee + 1] = (double)h1 + (double)l1;
+                                }
+                                const double m[4] = {0.25 * (e[0] + e[1]), -0.5 * e[2], 0.25 * (e[0] - e[1]),
+                                                     -0.5 * e[3]};
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+                                    atomicAdd(v.pacc + (((size_t)cu.lr * v.n_bin + b) * 4 + k) * v.n_ang + ang,
+                                              f * m[k]);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < 2; ++e)
+#pragma unroll
+                        for (int b = 0; b < NB; ++b) {
+                            suh[(e * NB + b) * TC_EPI_THREADS] = 0ull;
+                            sul[(e * NB + b) * TC_EPI_THREADS] = 0ull;
+                        }
+                }
+            }
             kq = nk;
-            blk = nb;
+            ab = nab;
             tile = nt;
+            h = nh;
             cu = nu;
+            nc = nc_next;
+            ++ie;
         }
-        if (!ok && tid == 0) {
+        if (!ok && lane == 0) {
             *s_abort = 1;
             atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
         }
@@ -967,13 +992,13 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
     const int grid = (int)(p->n_units < nsm ? p->n_units : nsm);
-    const size_t smem = TC_SMEM_BYTES;
     cudaError_t e = cudaSuccess;
     ctx_pre_launch(ctx);
 #define TC_LAUNCH(NBV)                                                                                   \
     case NBV:                                                                                            \
-        e = cudaFuncSetAttribute(k_tab_s12_tc<NBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        k_tab_s12_tc<NBV><<<grid, TC_THREADS, smem, st>>>(a);                                            \
+        e = cudaFuncSetAttribute(k_tab_s12_tc<NBV>, cudaFuncAttributeMaxDynamicSharedMemorySize,              \
+                                 (int)TC_SMEM_BYTES(NBV));                                               \
+        k_tab_s12_tc<NBV><<<grid, TC_THREADS, TC_SMEM_BYTES(NBV), st>>>(a);                              \
         break;
     switch (d.n_bin) {
         TC_LAUNCH(1) TC_LAUNCH(2) TC_LAUNCH(3) TC_LAUNCH(4) TC_LAUNCH(5) TC_LAUNCH(6) TC_LAUNCH(7)
@@ -985,7 +1010,7 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     return ctx_check_launch(ctx, "k_tab_s12_tc");
 }
 
-size_t table_mixed_smem_bytes() { return TC_SMEM_BYTES; }
+size_t table_mixed_smem_bytes() { return TC_SMEM_BYTES(8); }
 
 // The B operands depend only on the angles and the largest nmax: built once
 // per plan into plan-owned memory (plan creation synchronises afterwards).

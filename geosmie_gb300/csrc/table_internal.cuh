@@ -26,7 +26,7 @@ struct gbmie_table_plan {
     // mixed precision (tensor-core) path
     size_t o_cf, o_eexp, o_eunit, o_wf, o_tw, o_rowc, o_hidx, o_pcf, o_dscr;
     __half *bt;          // B operands of the contraction (plan-owned, built once at plan time)
-    int n_pad_total;     // angles padded to whole 64-column blocks
+    int n_pad_total;     // angles padded to whole 128-angle blocks (mixed path)
     int k_pad;           // orders padded to 32
     int *unit_order;     // [n_units] units by decreasing work (plan-owned)
     // split A operand of the tensor-core contraction: per unit, per 64-size
