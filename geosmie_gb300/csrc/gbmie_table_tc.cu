@@ -494,7 +494,10 @@ struct TcArgs {
 #define TC_STAGE_BYTES (TC_B_BYTES + TC_A_BYTES)       // 24 KB
 #define TC_EPI_WARPS 8
 #define TC_EPI_THREADS (32 * TC_EPI_WARPS)
-#define TC_THREADS (TC_EPI_THREADS + 64)               // + the MMA warp and the producer warp
+#define TC_THREADS (TC_EPI_THREADS + 96)               // + two MMA warps and the producer warp
+// register bound of 12 warps: three warps on an SM sub-partition fit its
+// 16K registers at 168 each
+#define TC_REG_BOUND_THREADS 384
 #define TC_WBUF_FLOATS (2 * 16 * 16)                   // per epilogue warp: 2 items x 16 sizes x 8 bins x 2
 #define TC_SUM_FLOATS(NB) (2 * 4 * (NB) * TC_EPI_THREADS) // running sums (hi, lo) [2][4 NB][thread]
 #define TC_SMEM_BYTES(NB)                                                                                  \
@@ -513,7 +516,7 @@ __device__ __forceinline__ int64_t tc_unit_index(int k, int cta, int G)
 }
 
 template <int NB>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
+__global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sB0 = smem;                                            // resident angle chunks, orders 1..16
@@ -526,6 +529,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
     uint64_t *acc_full = b0_full + 2, *acc_empty = acc_full + TC_NSETS, *drain = acc_empty + TC_NSETS;
     uint32_t *s_tmem = (uint32_t *)(drain + 1);
     volatile int *s_abort = (volatile int *)(s_tmem + 1);
+    // s_chunk[st]: the chunk the producer is loading into stage st.  An issuer
+    // skips the other issuer's chunks, so it can wait on a stage two phases
+    // ahead of the producer, where the barrier's parity alone would also match
+    // the older phase; it trusts the parity only once s_chunk holds its chunk
+    // (the producer writes it after the stage's previous chunk was consumed,
+    // so the stage's pending phase is then exactly that chunk's).
+    volatile int *s_chunk = s_abort + 2;
 
     const TabView &v = g.v;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -540,14 +550,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
             mbar_init(empty + i, 1);   // tcgen05.commit
         }
         mbar_init(b0_full, 1);
-        mbar_init(b0_empty, 1);
+        mbar_init(b0_empty, 2);   // both issuers leave the block
         for (int i = 0; i < TC_NSETS; ++i) {
             mbar_init(acc_full + i, 1);
             mbar_init(acc_empty + i, TC_EPI_WARPS);
         }
-        mbar_init(drain, 1);
+        mbar_init(drain, 2);
         fence_mbar_init();
         *s_abort = 0;
+        for (int i = 0; i < TC_NS; ++i) s_chunk[i] = -1;
     }
     tc_fence_before();
     __syncthreads();
@@ -556,14 +567,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
     const int64_t n_units = (int64_t)v.n_lambda * v.n_rh * v.n_comp;
     const int G = gridDim.x, cta = blockIdx.x;
 
-    if (warp == 8) {
-        // ================= MMA issue =================
+    if (warp == 8 || warp == 10) {
+        // ================= MMA issue: two issuers, alternate items =================
+        // Issuer p (warp 8: p = 0, warp 10: p = 1) takes the items of parity p
+        // and the accumulator sets 2p, 2p + 1; both walk every item to keep
+        // the ring's chunk count.  One issuing thread alone could not keep up:
+        // the issue of one small MMA and its bookkeeping took several times
+        // the tensor core's time for it.
+        const uint32_t p = warp == 10 ? 1u : 0u;
         if (lane == 0) {
             const uint32_t idesc = idesc_f16_f32(TC_ABLK, 2 * TC_HALF);
-            uint32_t it = 0, item = 0, b0_loads = 0;
+            // no-swizzle K-major descriptors without the start address: A (angles)
+            // LBO = 16 core matrices (K step of 8 orders), B (coefficients) 8; SBO 128 B
+            constexpr uint64_t DESC_A = ((uint64_t)((16 * 128) >> 4) << 16) | ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
+            constexpr uint64_t DESC_B = ((uint64_t)((8 * 128) >> 4) << 16) | ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
+            const uint32_t sStage0 = smem_u32(sStage);
+            uint32_t it = 0, ii = 0, wc = 0, b0_loads = 0;   // chunks, items, own windows
             bool ok = true, have_b0 = false;
             if (!reload) {   // every block's resident chunk, loaded once
-                ok = mbar_wait_or_abort(b0_full, 0, s_abort, TC_SLEEP_NS);
+                ok = mbar_wait_or_abort(b0_full, 0, s_abort);
                 b0_loads = 1;
             }
             for (int k = 0; ok; ++k) {
@@ -583,22 +605,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         have_b0 = true;
                     }
                     const uint32_t aB0 = smem_u32(sB0 + (reload ? 0 : ab) * TC_A_BYTES);
+                    // nmax of a tile's last size, loaded one tile ahead
+                    auto last_of = [&](int t) { return min(TC_INST * (t + 1), v.n_size); };
+                    long long o1 = ldg_pin_s64(off + last_of(0)), o0 = ldg_pin_s64(off + last_of(0) - 1);
                     for (int tile = 0; tile < ntl && ok; ++tile) {
                         const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
-                        const int kt = (int)(off[t0 + ntile] - off[t0 + ntile - 1]);
+                        const int kt = (int)(o1 - o0);
+                        if (tile + 1 < ntl) {
+                            o1 = ldg_pin_s64(off + last_of(tile + 1));
+                            o0 = ldg_pin_s64(off + last_of(tile + 1) - 1);
+                        }
                         const int nc = (kt + TC_KC16 - 1) / TC_KC16;
-                        for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h) {
+                        for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h, ++ii) {
+                            if ((ii & 1u) != p) {   // the other issuer's item
+                                it += nc;
+                                continue;
+                            }
                             for (int w0 = 0; w0 < nc && ok; w0 += g.win) {
                                 const int nj = min(g.win, nc - w0);
-                                const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
-                                if (use > 0 &&
-                                    !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, TC_SLEEP_NS)) {
+                                const uint32_t set = 2 * p + (wc & 1u), use = wc >> 1;
+                                if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort)) {
                                     ok = false;
                                     break;
                                 }
                                 for (int j = 0; j < nj && ok; ++j) {
-                                    const uint32_t c = it + j;
-                                    ok = mbar_wait_or_abort(full + c % TC_NS, (c / TC_NS) & 1u, s_abort, TC_SLEEP_NS);
+                                    const uint32_t c = it + j, st = c % TC_NS, par = (c / TC_NS) & 1u;
+                                    ok = false;
+                                    for (uint32_t tr = 0; tr < (1u << 26); ++tr) {
+                                        if (s_chunk[st] == (int)c && mbar_try(full + st, par)) {
+                                            ok = true;
+                                            break;
+                                        }
+                                        if ((tr & 255u) == 255u && *s_abort) break;
+                                    }
                                 }
                                 if (!ok) break;
                                 tc_fence_after();
@@ -606,32 +645,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                                 for (int pass = 0; pass < 2; ++pass) {
                                     for (int j = 0; j < nj; ++j) {
                                         const uint32_t c = it + j;
-                                        const uint32_t sB = smem_u32(sStage + (c % TC_NS) * TC_STAGE_BYTES);
+                                        const uint32_t sB = sStage0 + (c % TC_NS) * TC_STAGE_BYTES;
                                         const uint32_t sA = (w0 + j) == 0 ? aB0 : sB + TC_B_BYTES;
-                                        // A (angles): LBO = 16 core matrices (K step of 8 orders); B: 8
-                                        const uint64_t p_hi = smem_desc(sA + 0 * TC_MAT_A, 16 * 128, 128);
-                                        const uint64_t q_hi = smem_desc(sA + 2 * TC_MAT_A, 16 * 128, 128);
-                                        const uint64_t c_hi = smem_desc(sB + 0 * TC_MAT_B, 8 * 128, 128);
-                                        const uint64_t d_hi = smem_desc(sB + 2 * TC_MAT_B, 8 * 128, 128);
+                                        // descriptors: constant LBO/SBO fields + start address / 16;
+                                        // matrix m of an operand starts m x its matrix size later
+                                        const uint64_t a0 = DESC_A | (sA >> 4), b0 = DESC_B | (sB >> 4);
+                                        constexpr uint64_t MA = TC_MAT_A >> 4, MB = TC_MAT_B >> 4;
                                         if (pass == 0) {   // cross products: small accumulator
-                                            const uint64_t p_lo = smem_desc(sA + 1 * TC_MAT_A, 16 * 128, 128);
-                                            const uint64_t q_lo = smem_desc(sA + 3 * TC_MAT_A, 16 * 128, 128);
-                                            const uint64_t c_lo = smem_desc(sB + 1 * TC_MAT_B, 8 * 128, 128);
-                                            const uint64_t d_lo = smem_desc(sB + 3 * TC_MAT_B, 8 * 128, 128);
-                                            mma_f16(d, p_hi, c_lo, idesc, j == 0 ? 0u : 1u);
-                                            mma_f16(d, p_lo, c_hi, idesc, 1u);
-                                            mma_f16(d + 64, q_hi, d_lo, idesc, j == 0 ? 0u : 1u);
-                                            mma_f16(d + 64, q_lo, d_hi, idesc, 1u);
+                                            mma_f16(d, a0, b0 + MB, idesc, j == 0 ? 0u : 1u);
+                                            mma_f16(d, a0 + MA, b0, idesc, 1u);
+                                            mma_f16(d + 64, a0 + 2 * MA, b0 + 3 * MB, idesc, j == 0 ? 0u : 1u);
+                                            mma_f16(d + 64, a0 + 3 * MA, b0 + 2 * MB, idesc, 1u);
                                         } else {
-                                            mma_f16(d, p_hi, c_hi, idesc, 1u);
-                                            mma_f16(d + 64, q_hi, d_hi, idesc, 1u);
+                                            mma_f16(d, a0, b0, idesc, 1u);
+                                            mma_f16(d + 64, a0 + 2 * MA, b0 + 2 * MB, idesc, 1u);
                                             mma_commit(empty + c % TC_NS);   // stage free when its MMAs are done
                                         }
                                     }
                                 }
                                 it += nj;
                                 mma_commit(acc_full + set);
-                                ++item;
+                                ++wc;
                             }
                         }
                     }
@@ -641,7 +675,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 *s_abort = 1;
                 atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
             }
-            // every issued MMA has finished before TMEM is released
+            // every issued MMA (both issuers) has finished before TMEM is released
             mma_commit(drain);
             if (!mbar_wait(drain, 0)) atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
         }
@@ -668,6 +702,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
                 const int *tcb = g.tile_cbase + (size_t)v.le(lam) * (ntl + 1);
                 const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * (2 * TC_B_BYTES);
+                const int comp = (int)(unit % v.n_comp), rhi = (int)((unit / v.n_comp) % v.n_rh);
+                const float *uW = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
+                const int *uex = g.eexp + (size_t)unit * v.n_size;
                 for (int ab = 0; ab < nblocks && ok; ++ab) {
                     const uint8_t *gA = (const uint8_t *)g.bt + (size_t)ab * nkc * TC_A_BYTES;
                     if (reload) {
@@ -682,9 +719,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         last_tx_phase = b0_loads & 1u;
                         ++b0_loads;
                     }
+                    // chunk bases tcb[tile], tcb[tile + 1], loaded one tile ahead
+                    int cb0 = ldg_pin_s32(tcb), cb1 = ldg_pin_s32(tcb + 1);
                     for (int tile = 0; tile < ntl && ok; ++tile) {
                         const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
-                        const int nc = tcb[tile + 1] - tcb[tile];
+                        const int base = cb0, nc = cb1 - cb0;
+                        if (tile + 1 < ntl) {
+                            cb0 = cb1;
+                            cb1 = ldg_pin_s32(tcb + tile + 2);
+                        }
+                        // the coefficient chunks of the next tile into L2, and the
+                        // PSD weights and exponents of the tile after it (the
+                        // epilogue reads them one item ahead; they were evicted by
+                        // the coefficient operand)
+                        if (ab == 0 && tile + 1 < ntl)
+                            bulk_prefetch_l2(ua + (size_t)cb0 * (2 * TC_B_BYTES), (uint32_t)(cb1 - cb0) * (2 * TC_B_BYTES));
+                        if (tile + 2 < ntl || (tile + 2 - ntl < ntl && ab + 1 < nblocks)) {
+                            const int tp = tile + 2 < ntl ? tile + 2 : tile + 2 - ntl;
+                            const int t0 = tp * TC_INST, nt = min(TC_INST, v.n_size - t0);
+                            auto pf = [&](const void *p, size_t bytes) {
+                                const uintptr_t a0 = (uintptr_t)p & ~(uintptr_t)15, a1 = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+                                if (a1 > a0) bulk_prefetch_l2((const void *)a0, (uint32_t)(a1 - a0));
+                            };
+                            pf(uex + t0, sizeof(int) * nt);
+                            for (int b = 0; b < v.n_bin && b < NB; ++b)
+                                pf(uW + (size_t)b * v.n_comp * v.n_size + t0, sizeof(float) * nt);
+                        }
                         for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h) {
                             for (int j = 0; j < nc; ++j) {
                                 const uint32_t c = it++;
@@ -695,8 +755,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                                     ok = false;
                                     break;
                                 }
+                                s_chunk[st] = (int)c;
                                 mbar_arrive_expect_tx(full + st, TC_B_BYTES + (j > 0 ? TC_A_BYTES : 0));
-                                bulk_g2s(sS, ua + ((size_t)(tcb[tile] + j) * 2 + h) * TC_B_BYTES, TC_B_BYTES, full + st);
+                                bulk_g2s(sS, ua + ((size_t)(base + j) * 2 + h) * TC_B_BYTES, TC_B_BYTES, full + st);
                                 if (j > 0) bulk_g2s(sS + TC_B_BYTES, gA + (size_t)j * TC_A_BYTES, TC_A_BYTES, full + st);
                                 last_tx = full + st;
                                 last_tx_phase = (c / TC_NS) & 1u;
@@ -754,17 +815,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         // exponent, so the power is <= 1; below 2^-126 the weight is dropped)
         // of this warp's 16 sizes of half tile h: lane l holds size l / 2,
         // bins 4 (l % 2) .. + 3
-        auto fetch_w = [&](const UnitC &u, int tile, int h, float4 &wv) {
+        // (loads only: the scaling waits for them at the next item's start)
+        auto fetch_w = [&](const UnitC &u, int tile, int h, float4 &wv, int &wex) {
             const int si = tile * TC_INST + TC_HALF * h + 16 * wh + (lane >> 1);
             const int b0 = 4 * (lane & 1);
             float w[4] = {0.f, 0.f, 0.f, 0.f};
+            wex = -100000;
             if (si < v.n_size && b0 < NB) {
-                const int e = 2 * (u.ex[si] - u.E);
-                const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
+                wex = ldg_pin_s32(u.ex + si) - u.E;
 #pragma unroll
                 for (int bb = 0; bb < 4; ++bb) {
                     const int b = b0 + bb;
-                    if (b < v.n_bin && b < NB) w[bb] = u.Wb[(size_t)b * v.n_comp * v.n_size + si] * p2;
+                    if (b < v.n_bin && b < NB) w[bb] = ldg_pin_f32(u.Wb + (size_t)b * v.n_comp * v.n_size + si);
                 }
             }
             wv = make_float4(w[0], w[1], w[2], w[3]);
@@ -772,31 +834,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
         // 16-order chunks of a tile (its last size has the largest nmax)
         auto tile_chunks = [&](const UnitC &u, int tile) -> int {
             const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
-            return (int)((u.off[t0 + ntile] - u.off[t0 + ntile - 1] + TC_KC16 - 1) / TC_KC16);
+            return (int)((ldg_pin_s64(u.off + t0 + ntile) - ldg_pin_s64(u.off + t0 + ntile - 1) + TC_KC16 - 1) /
+                         TC_KC16);
         };
         constexpr int NP = (NB + 1) / 2;   // 16-byte weight loads per size: two bins each
         bool ok = true;
-        uint32_t item = 0, ie = 0;
+        uint32_t wce[2] = {0u, 0u}, ie = 0;   // windows read per issuer; items
         int kq = 0, ab = 0, tile = 0, h = 0;
         UnitC cu = unit_c(0);
         float4 wn = make_float4(0.f, 0.f, 0.f, 0.f);
+        int wnex = -100000;
         int nc = 0;
         if (cu.valid) {
             nc = tile_chunks(cu, 0);
-            if (32 * q < v.n_ang) fetch_w(cu, 0, 0, wn);
+            if (32 * q < v.n_ang) fetch_w(cu, 0, 0, wn, wnex);
         }
         // tile sums in registers; per-(unit, block) sums as unevaluated pairs
-        // (hi + lo) in this thread's column of sSum: [hi, lo][2 NB pairs][thread]
+        // (hi + lo) in this thread's column of sSum: [hi, lo][bin][thread] of
+        // (E0 pair, E1 pair), 16 bytes per access
         f32x2 acc[2][NB];
-        f32x2 *suh = (f32x2 *)sSum + tid, *sul = suh + 2 * NB * TC_EPI_THREADS;
+        ulonglong2 *suh = (ulonglong2 *)sSum + tid, *sul = suh + NB * TC_EPI_THREADS;
 #pragma unroll
-        for (int e = 0; e < 2; ++e)
-#pragma unroll
-            for (int b = 0; b < NB; ++b) {
-                acc[e][b] = 0ull;
-                suh[(e * NB + b) * TC_EPI_THREADS] = 0ull;
-                sul[(e * NB + b) * TC_EPI_THREADS] = 0ull;
-            }
+        for (int b = 0; b < NB; ++b) {
+            acc[0][b] = acc[1][b] = 0ull;
+            suh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
+            sul[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
+        }
         while (ok && cu.valid) {
             const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
             const int nwin = (nc + g.win - 1) / g.win;
@@ -816,19 +879,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
             const UnitC nu = nk == kq ? cu : unit_c(nk);
             float *wb = wbuf + (ie & 1) * (TC_WBUF_FLOATS / 2);
             if (active) {   // duplicated pairs (w_b, w_b) for the packed FMAs
-                *(float4 *)(wb + 8 * lane) = make_float4(wn.x, wn.x, wn.y, wn.y);
-                *(float4 *)(wb + 8 * lane + 4) = make_float4(wn.z, wn.z, wn.w, wn.w);
+                const int e = 2 * wnex;
+                const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
+                const float4 w = make_float4(wn.x * p2, wn.y * p2, wn.z * p2, wn.w * p2);
+                *(float4 *)(wb + 8 * lane) = make_float4(w.x, w.x, w.y, w.y);
+                *(float4 *)(wb + 8 * lane + 4) = make_float4(w.z, w.z, w.w, w.w);
             }
             __syncwarp();
             int nc_next = 0;
             if (nu.valid) {   // in flight during this item
                 nc_next = nh == 0 ? tile_chunks(nu, nt) : nc;
-                if (TC_ABLK * nab + 32 * q < v.n_ang) fetch_w(nu, nt, nh, wn);
+                if (TC_ABLK * nab + 32 * q < v.n_ang) fetch_w(nu, nt, nh, wn, wnex);
             }
             // window sums of S+ and S- (this lane's angle, 16 sizes x Re/Im)
             float rp[32], rm[32];
+            const uint32_t ip = ie & 1u;   // the item's issuer
             for (int w = 0; w < nwin; ++w) {
-                const uint32_t set = item % TC_NSETS, use = item / TC_NSETS;
+                const uint32_t wi = ip ? wce[1] : wce[0];
+                const uint32_t set = 2 * ip + (wi & 1u), use = wi >> 1;
                 int go = 1;
                 if (lane == 0) go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
                 go = __shfl_sync(0xffffffffu, go, 0);
@@ -840,30 +908,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                 if (active) {
                     const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * wh;
                     if (w == 0) {
-                        tmem_ld32(ta, rp);
-                        tmem_ld32(ta + 64, rm);
+                        tmem_ld32x2(ta, ta + 64, rp, rm);
                     } else {
-                        float t[32];
-                        tmem_ld32(ta, t);
+                        float t[32], u[32];
+                        tmem_ld32x2(ta, ta + 64, t, u);
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) rp[i] += t[i];
-                        tmem_ld32(ta + 64, t);
-#pragma unroll
-                        for (int i = 0; i < 32; ++i) rm[i] += t[i];
+                        for (int i = 0; i < 32; ++i) {
+                            rp[i] += t[i];
+                            rm[i] += u[i];
+                        }
                     }
                 }
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(acc_empty + set);
-                ++item;
+                if (ip) ++wce[1];
+                else ++wce[0];
             }
             if (!ok) break;
             if (active) {
+                // all sizes' pairs first (independent work for the scheduler), then
+                // the weighted sums; rp/rm die as E0/E1 are formed
+                f32x2 E0[16], E1[16];
 #pragma unroll
                 for (int s = 0; s < 16; ++s) {
                     const float pr = rp[2 * s], pi = rp[2 * s + 1], mr = rm[2 * s], mi = rm[2 * s + 1];
-                    const f32x2 e0 = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
-                    const f32x2 e1 = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
+                    E0[s] = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
+                    E1[s] = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
+                }
+#pragma unroll
+                for (int s = 0; s < 16; ++s) {
+                    const f32x2 e0 = E0[s], e1 = E1[s];
                     const ulonglong2 *wp = (const ulonglong2 *)(wb + 16 * s);
 #pragma unroll
                     for (int p = 0; p < NP; ++p) {
@@ -879,18 +954,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
             }
             if (nh == 0) {
                 // end of a tile: two-sum (hi + lo) += acc, exactly rounded
+                ulonglong2 H[NB], Lo[NB];
 #pragma unroll
-                for (int e = 0; e < 2; ++e)
+                for (int b = 0; b < NB; ++b) {
+                    H[b] = suh[b * TC_EPI_THREADS];
+                    Lo[b] = sul[b * TC_EPI_THREADS];
+                }
+                auto two_sum = [](f32x2 &hi, f32x2 &lo, f32x2 a) {
+                    const f32x2 sum = f2_add(hi, a);
+                    const f32x2 bp = f2_sub(sum, hi);
+                    lo = f2_add(lo, f2_add(f2_sub(hi, f2_sub(sum, bp)), f2_sub(a, bp)));
+                    hi = sum;
+                };
 #pragma unroll
-                    for (int b = 0; b < NB; ++b) {
-                        const int o = (e * NB + b) * TC_EPI_THREADS;
-                        const f32x2 a = acc[e][b], hi = suh[o];
-                        const f32x2 sum = f2_add(hi, a);
-                        const f32x2 bp = f2_sub(sum, hi);
-                        sul[o] = f2_add(sul[o], f2_add(f2_sub(hi, f2_sub(sum, bp)), f2_sub(a, bp)));
-                        suh[o] = sum;
-                        acc[e][b] = 0ull;
-                    }
+                for (int b = 0; b < NB; ++b) {
+                    two_sum(H[b].x, Lo[b].x, acc[0][b]);
+                    two_sum(H[b].y, Lo[b].y, acc[1][b]);
+                    acc[0][b] = acc[1][b] = 0ull;
+                    suh[b * TC_EPI_THREADS] = H[b];
+                    sul[b * TC_EPI_THREADS] = Lo[b];
+                }
                 if (nt == 0) {
                     // end of the (unit, angle block): this thread's share of the unit's sums
                     const int ang = TC_ABLK * ab + 32 * q + lane;
@@ -901,12 +984,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                             if (b < v.n_bin) {
                                 const double f = v.frac[(size_t)b * v.n_comp + cu.comp] * f2;
                                 double e[4];
+                                const ulonglong2 hb = suh[b * TC_EPI_THREADS], lb = sul[b * TC_EPI_THREADS];
 #pragma unroll
                                 for (int ee = 0; ee < 2; ++ee) {
-                                    const int o = (ee * NB + b) * TC_EPI_THREADS;
                                     float h0, h1, l0, l1;
-                                    f2_unpack(suh[o], h0, h1);
-                                    f2_unpack(sul[o], l0, l1);
+                                    f2_unpack(ee ? hb.y : hb.x, h0, h1);
+                                    f2_unpack(ee ? lb.y : lb.x, l0, l1);
                                     e[2 * ee] = (double)h0 + (double)l0;
                                     e[2 * ee + 1] = (double)h1 + (double)l1;
                                 }
@@ -920,12 +1003,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tab_s12_tc(TcArgs g)
                         }
                     }
 #pragma unroll
-                    for (int e = 0; e < 2; ++e)
-#pragma unroll
-                        for (int b = 0; b < NB; ++b) {
-                            suh[(e * NB + b) * TC_EPI_THREADS] = 0ull;
-                            sul[(e * NB + b) * TC_EPI_THREADS] = 0ull;
-                        }
+                    for (int b = 0; b < NB; ++b) {
+                        suh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
+                        sul[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
+                    }
                 }
             }
             kq = nk;
