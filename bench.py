@@ -34,10 +34,10 @@ UNIT = "instance-evals/s"
 SAMPLE_LAMBDA = [0, 12, 24, 36, 48, 59]
 # DRAM bytes (read + write) per (wavelength, RH, component) unit from one ncu
 # capture of the 12-wavelength sulfate table (432 units; profiles/
-# k_tab_coeffs_mixed_k_tab_s12_tc_sulfate12.md), scaled to a run by its units
-NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": (13.54368e6 + 130.015232e6) / 432,
-                      "k_tab_s12_tc": (740.37888e6 + 12.53632e6) / 432,
-                      "k_tab_split_a": (159.200256e6 + 255.044608e6) / 432}
+# k_tab_s12_tc_k_tab_coeffs_mixed_k_gsf_tc_gemm_sulfate12.md), scaled to a run
+# by its units
+NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": (44.090112e6 + 433.773056e6) / 432,
+                      "k_tab_s12_tc": (532.276736e6 + 10.899456e6) / 432}
 SAMPLE_RH = [0, 35]
 
 
@@ -340,8 +340,9 @@ def main():
         nl_, tms = ktimes["k_tab_s12_tc"]
         sec = tms / nl_ * 1e-3
         alg = 8.0 * counts["sum_nmax"] * nang
-        # 6 MMAs (M 128 x N 64 x K 16) per 16-order chunk of a tile, per 64-angle block
-        exe = counts["sum_kc16"] * 6 * 2 * 128 * 64 * 16 * (-(-nang // 64))
+        # 6 MMAs (M 128 angles x N 64 (32 sizes, Re/Im) x K 16) per 16-order chunk
+        # of a half tile, per 128-angle block
+        exe = counts["sum_kc16_half"] * 6 * 2 * 128 * 64 * 16 * (-(-nang // 128))
         kernels["k_tab_s12_tc"]["algorithmic_tflops"] = alg / sec / 1e12
         kernels["k_tab_s12_tc"]["executed_mma_tflops"] = exe / sec / 1e12
         kernels["k_tab_s12_tc"]["tensor_peak_tflops"] = peaks.get("bf16_tflops")
@@ -354,8 +355,8 @@ def main():
                     "algorithmic_flop_per_launch": alg, "executed_mma_flop_per_launch": exe,
                     "note": "executed = 3 split products x 2 GEMMs on padded tiles; algorithmic = 8 flop "
                             "per (order, angle) of the S+/S- sums; the tensor pipe is not this kernel's "
-                            "limit: ncu shows the fused Mueller/PSD epilogue issue-bound (47% issue "
-                            "active, tensor pipe 4%)"}
+                            "limit: the fused Mueller/PSD epilogue is (latency-bound FP32 work of 8 "
+                            "warps; the MMA/copy pipeline alone runs in 0.4 of the kernel's time)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.small:

@@ -183,12 +183,16 @@ def work_counts(spec):
     # tensor-core tiles: 64 sizes, orders in chunks of 16 up to the tile's
     # largest nmax, per unit
     sum_kc16 = 0
+    sum_kc16_half = 0   # the same per half tile of 32 sizes (the contraction's MMA N = 64)
+    tsize = np.minimum(64, grid.size - np.arange(0, grid.size, 64))
+    halves = np.where(tsize > 32, 2, 1)
     for li in range(nl):
         nmi = nm[le[li]]
         last = nmi[np.minimum(np.arange(63, grid.size + 63, 64), grid.size - 1)]
         sum_kc16 += int(np.sum((last + 15) // 16)) * nrh * ncomp
+        sum_kc16_half += int(np.sum((last + 15) // 16 * halves)) * nrh * ncomp
     return {"instances": int(nl * nrh * ncomp * grid.size), "units": int(nl * nrh * ncomp),
             "sum_nmax": sum_nmax, "sum_nmx": sum_nmx, "sum_warm": sum_warm,
-            "sum_kc16": sum_kc16,
+            "sum_kc16": sum_kc16, "sum_kc16_half": sum_kc16_half,
             "rows": int(x.shape[0] * grid.size), "nbin": int(np.asarray(spec["frac"]).shape[0]),
             "nang": int(np.asarray(spec["ang"]).size)}
