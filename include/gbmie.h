@@ -279,6 +279,20 @@ int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const double *ang_deg,
               const double *F, int32_t nnodes, double *coef, double *cnorm,
               int32_t precision);
 
+/* ---- band averages ------------------------------------------------------- */
+/* Band averages of table quantities: for every variable, bin, band and RH
+ * the mean of the variable linearly interpolated in wavenumber at 100 points
+ * spaced evenly between the band's two edges (either order), clipped to the
+ * table's wavenumber range.  Replaces geosmie/bandaverage.py doAverage
+ * (:18-50) as looped by fun (:163-179); the arithmetic follows its numpy
+ * linspace / clip / interp / pairwise-sum steps.  wavenum [nlam]: the
+ * table's wavenumbers in cm^-1 (any order, 1/(100 lambda[m])); vin
+ * [nvar][nbin][nlam][nrh]; edge_a, edge_b [nband] band edges in cm^-1;
+ * out [nvar][nbin][nband][nrh].  Device pointers; nlam >= 1. */
+int gbmie_band_average(gbmie_ctx *ctx, int32_t nvar, int32_t nbin, int32_t nlam, int32_t nrh,
+                       const double *wavenum, const double *vin, int32_t nband,
+                       const double *edge_a, const double *edge_b, double *out);
+
 /* ---- measurement helper ------------------------------------------------- */
 /* Sustained FP64 FMA throughput of this device (GFLOP/s, host), measured by
  * a dependent-chain-free DFMA loop over the whole GPU. */

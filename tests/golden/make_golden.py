@@ -20,6 +20,9 @@ Outputs (small .npz files, committed):
   table_*.npz      dointegration.fun on small particle definitions, with the
                    inputs (JSON text, refractive-index tables, water table)
                    needed to rerun them without the reference tree.
+  bands.npz        bandaverage.fun (GEOS5, RRTMG, RRTMGP, PURDUE; GEOS5 also
+                   with noIR) on a seeded synthetic table of 60 wavelengths,
+                   with its inputs, and doAverage on edge cases.
 """
 import argparse
 import contextlib
@@ -59,11 +62,17 @@ def _install_shims():
     nc = types.ModuleType("netCDF4")
 
     class Var:
-        def __init__(self, shape):
-            self.data = np.zeros(shape)
+        def __init__(self, shape, dtype="f8"):
+            self.data = np.full(shape, "", dtype="<U1") if dtype == "c" else np.zeros(shape)
 
         def __setitem__(self, k, v):
-            self.data[k] = v
+            try:
+                self.data[k] = v
+            except ValueError:
+                # bandaverage.fun (GEOS5) writes 11 band centres into its
+                # 18-band dimension, which netCDF4 rejects too: keep what it wrote
+                self.data = np.asarray(v)
+                self.mismatch = True
 
         def __getitem__(self, k):
             return self.data[k]
@@ -83,7 +92,7 @@ def _install_shims():
         def createVariable(self, name, dtype, dims, **kw):
             if isinstance(dims, str):
                 dims = (dims,)
-            v = Var(tuple(self.dims[d] for d in dims))
+            v = Var(tuple(self.dims[d] for d in dims), dtype)
             v.dims = dims
             self.variables[name] = v
             return v
@@ -263,6 +272,63 @@ def gen_tables(ref_src, Dataset):
             print("table_%s: p11 %s" % (name, out["out_p11"].shape))
 
 
+BAND_MODES = [("GEOS5", False), ("GEOS5", True), ("RRTMG", False), ("RRTMGP", False), ("PURDUE", False)]
+
+
+def bands_input():
+    """A seeded synthetic table: 2 bins x 60 wavelengths (0.2-40 um) x 3 RH,
+    smooth positive quantities with some structure in wavelength."""
+    rng = np.random.default_rng(20261203)
+    nbin, nlam, nrh = 2, 60, 3
+    lam = np.logspace(np.log10(0.2e-6), np.log10(40e-6), nlam)
+    rh = np.array([0.0, 0.5, 0.95])
+    ll = np.log(lam)[None, :, None]
+    data = {"wavelength": lam, "rh": rh, "bin": np.arange(1, nbin + 1, dtype=np.float64)}
+    for k, name in enumerate(["qsca", "qext", "bsca", "bext", "g", "bbck", "refreal", "refimag"]):
+        a = rng.uniform(0.5, 2.0, (nbin, 1, nrh))
+        b = rng.uniform(-1.0, 1.0, (nbin, 1, nrh))
+        c = rng.uniform(0.5, 3.0)
+        data[name] = a * (1.5 + np.sin(c * ll + b)) * np.exp(-0.1 * (ll - ll.mean()) ** 2)
+    data["rEff"] = rng.uniform(0.1e-6, 2e-6, (nbin, nrh))
+    data["rMass"] = rng.uniform(0.1e-6, 2e-6, (nbin, nrh))
+    data["rLow"] = np.tile(np.array([[0.01e-6], [0.1e-6]]), (1, nrh))
+    data["rUp"] = np.tile(np.array([[0.1e-6], [1.0e-6]]), (1, nrh))
+    return data
+
+
+def gen_bands(ref_src, Dataset):
+    sys.path.insert(0, os.path.join(ref_src, "geosmie"))
+    import bandaverage
+    data = bands_input()
+
+    class In:
+        variables = data
+    out = {("in_" + k): v for k, v in data.items()}
+    for mode, noir in BAND_MODES:
+        Dataset.opened.clear()
+        tag = "%s%s" % (mode, "_noIR" if noir else "")
+        try:
+            with contextlib.redirect_stdout(io.StringIO()):
+                bandaverage.fun(In, "su", "unused.nc", mode, False, noir)
+        except TypeError as e:
+            # RRTMGP: the band edges stay Python lists and `lBandLow * 1e6`
+            # (bandaverage.py:260) raises after the averages were written
+            out["error_%s" % tag] = np.array(str(e))
+        ds = Dataset.opened[-1]
+        for k, v in ds.variables.items():
+            out["out_%s_%s" % (tag, k)] = v.data
+    # doAverage edge cases: a band partly and wholly outside the table, a
+    # band with reversed edges, wavelength edges
+    lam = data["wavelength"]
+    var = data["qext"][0, :, 1]
+    cases = [(100.0, 300.0, True), (10.0, 40.0, True), (30000.0, 60000.0, True), (60000.0, 52000.0, True),
+             (0.175e-6, 0.225e-6, False), (29.412e-6, 40e-6, False), (3.333e-6, 5.263e-6, False)]
+    out["edge_cases"] = np.array(cases, dtype=np.float64)
+    out["edge_out"] = np.array([bandaverage.doAverage(lam, var, l, r, w, None) for (l, r, w) in cases])
+    np.savez_compressed(os.path.join(HERE, "bands.npz"), **out)
+    print("bands: %d arrays" % len(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -273,7 +339,7 @@ def main():
     sys.path.insert(0, os.path.join(src, "pymiecoated"))
     sys.path.insert(0, os.path.join(src, "geosmie"))
     from pymiecoated import mie_coated
-    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables"]
+    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables", "bands"]
     if "single" in sel:
         gen_single(mie_coated)
     if "coated" in sel:
@@ -282,6 +348,8 @@ def main():
         gen_size_range(mie_coated)
     if "tables" in sel:
         gen_tables(src, Dataset)
+    if "bands" in sel:
+        gen_bands(src, Dataset)
 
 
 if __name__ == "__main__":

@@ -46,10 +46,10 @@ def _mixed_plain(spec, n_gsf=0, n_gsf_nodes=0):
     return out
 
 
-def _check_mixed(a, b, n_gsf):
+def _check_mixed(a, b, n_gsf, phase_tol=1e-6):
     p11 = np.abs(a["p11"])
     for k in SCAT:
-        assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, k
+        assert np.max(np.abs(b[k] - a[k]) / p11) < phase_tol, k
     for k in TIGHT + LOOSE:
         assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, k
     assert np.max(np.abs(b["qabs"] - a["qabs"]) / np.abs(a["qext"])) < 1e-6
@@ -135,3 +135,23 @@ def test_coated_table_gpu():
     spec, _ = workloads.coated_bc()
     a, b = _mixed_plain(spec)
     _check_mixed(a, b, 0)
+
+
+@pytest.mark.gpu
+def test_large_nmax_table_gpu():
+    """Real sea-salt/nitrate tables reach nmax ~7600: one wavelength, 8 radii
+    up to x ~ 7540, FP64 against the oracle and mixed against FP64.  The
+    mixed path's phase elements are held to 2e-6 of P11 here (measured
+    1.2e-6 for p34 at side angles: the FP32 sum over ~160 accumulation
+    windows of terms that cancel to a small S); bulk quantities to 1e-6."""
+    from oracle import integration
+    lam = np.array([0.2e-6])
+    r = np.logspace(np.log10(20e-6), np.log10(240e-6), 8)
+    m = np.full((1, 1, 1), 1.50 + 1e-6j)
+    spec = workloads._lognormal_spec(lam, r, m, [1.0], [100e-6], 1.6, 2200.0, np.linspace(0.0, 180.0, 181))
+    counts = workloads.work_counts(spec)
+    assert counts["sum_nmax"] > 7 * 1000
+    a, b = _mixed_plain(spec)
+    ref = integration.run_spec(spec)
+    _check_table(a, ref)
+    _check_mixed(a, b, 0, phase_tol=2e-6)
