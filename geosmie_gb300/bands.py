@@ -104,11 +104,12 @@ def band_average(lam, values, low, up, use_wavenum, device=0):
     return out.cpu().numpy()
 
 
-def fun(data, part, mode, useSolar=False, noIR=False, device=0):
-    """bandaverage.fun (:126-294) without the NetCDF write: {name: array} of
-    the band file's variables (non-legacy layout [bin][band][rh]).  data
-    holds 'wavelength' (m), 'rh', 'bin', 'rEff', 'rMass', 'rLow', 'rUp' and
-    the eight averaged quantities [bin][wavelength][rh]."""
+def fun(data, part, mode, useSolar=False, noIR=False, device=0, opfn=None):
+    """bandaverage.fun (:126-294): {name: array} of the band file's variables
+    (non-legacy layout [bin][band][rh]), written to opfn as a NetCDF classic
+    file (lutfile.write_bands) when opfn is given.  data holds 'wavelength'
+    (m), 'rh', 'bin', 'rEff', 'rMass', 'rLow', 'rUp' and the eight averaged
+    quantities [bin][wavelength][rh]."""
     lam = np.asarray(data["wavelength"], np.float64)
     rh = np.asarray(data["rh"], np.float64)
     reff = np.asarray(data["rEff"], np.float64)
@@ -148,4 +149,7 @@ def fun(data, part, mode, useSolar=False, noIR=False, device=0):
                     "bandLow": ("wavelength",), "bandUp": ("wavelength",), "qname": ("bin", "nchar"),
                     "bin": ("bin",), "rLow": ("bin",), "rUp": ("bin",), "rEff": ("bin", "rh"),
                     "rMass": ("bin", "rh")}
+    if opfn is not None:
+        from . import lutfile
+        lutfile.write_bands(opfn, out)
     return out

@@ -416,12 +416,18 @@ def load_particle(path, data_dir=None):
 
 
 def fun(partID0, datatype="json", oppfx=".", oppclassic=False, data_dir=None, n_gsf=0,
-        precision=_native.GBMIE_PLAIN_FP64):
-    """dointegration.fun (:672): returns the table dict instead of writing
-    optics_<id>.nomom.nc4 (the NetCDF writer is outside this module)."""
+        precision=_native.GBMIE_PLAIN_FP64, write=True, version=2):
+    """dointegration.fun (:672): computes the table and, like the reference,
+    writes oppfx/optics_<id>.nomom.nc4 (legacy layout: .nomom.legacy.nc4)
+    as a NetCDF classic file (lutfile); returns the table dict."""
     if datatype != "json":
         raise ValueError("bad datatype: %s" % datatype)
     params, mlist, waterm = load_particle(partID0, data_dir)
     if params.get("mode", "mie") != "mie":
         raise NotImplementedError("kernel (GRASP) mode is not a Mie table")
-    return run_table(params, mlist, waterm, n_gsf=n_gsf, precision=precision)
+    out = run_table(params, mlist, waterm, n_gsf=n_gsf, precision=precision)
+    if write:
+        from . import lutfile
+        path = os.path.join(oppfx, lutfile.optics_filename(partID0, oppclassic))
+        lutfile.write_optics(path, out, params["rh"], mlist[0][0], angmie(), oppclassic, version=version)
+    return out

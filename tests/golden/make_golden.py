@@ -23,6 +23,9 @@ Outputs (small .npz files, committed):
   bands.npz        bandaverage.fun (GEOS5, RRTMG, RRTMGP, PURDUE; GEOS5 also
                    with noIR) on a seeded synthetic table of 60 wavelengths,
                    with its inputs, and doAverage on edge cases.
+  hydrophobic.npz  hydrophobic.doConversion on the one-bin tables above
+                   (table_trivial, table_seasalt), non-legacy and legacy
+                   layout, from files laid out by geosmie_gb300.lutfile.
 """
 import argparse
 import contextlib
@@ -329,6 +332,111 @@ def gen_bands(ref_src, Dataset):
     print("bands: %d arrays" % len(out))
 
 
+def gen_hydrophobic(ref_src):
+    """hydrophobic.doConversion on the one-bin reference tables (table_trivial,
+    table_seasalt), non-legacy and legacy layout, through an in-memory
+    netCDF4 with the parts doConversion uses."""
+    sys.path.insert(0, os.path.join(ref_src, "geosmie"))
+
+    class Dim:
+        def __init__(self, n):
+            self.n = n
+
+        def __len__(self):
+            return self.n
+
+    class Var:
+        def __init__(self, data, dims, dtype):
+            object.__setattr__(self, "_a", {})
+            self.data = np.array(data, dtype=dtype)
+            self.dimensions = tuple(dims)
+            self.dtype = np.dtype(dtype)
+
+        @property
+        def shape(self):
+            return self.data.shape
+
+        def ncattrs(self):
+            return list(self._a)
+
+        def __setattr__(self, k, v):
+            if k in ("data", "dimensions", "dtype"):
+                object.__setattr__(self, k, v)
+            else:
+                self._a[k] = v
+
+        def __getattr__(self, k):
+            a = object.__getattribute__(self, "_a")
+            if k in a:
+                return a[k]
+            raise AttributeError(k)
+
+        def __getitem__(self, k):
+            return self.data[k]
+
+        def __setitem__(self, k, v):
+            self.data[k] = v
+
+    files = {}
+
+    class Dataset:
+        def __init__(self, path, mode="r"):
+            self.path = path
+            if mode == "w":
+                self.dimensions = {}
+                self.variables = {}
+                files[path] = self
+            else:
+                src = files[path]
+                self.dimensions = src.dimensions
+                self.variables = src.variables
+
+        def ncattrs(self):
+            return []
+
+        def createDimension(self, name, size):
+            self.dimensions[name] = Dim(size)
+
+        def createVariable(self, name, dtype, dims, **kw):
+            v = Var(np.zeros(tuple(len(self.dimensions[d]) for d in dims)), dims, dtype)
+            self.variables[name] = v
+            return v
+
+        def close(self):
+            pass
+
+    nc = types.ModuleType("netCDF4")
+    nc.Dataset = Dataset
+    saved = sys.modules.get("netCDF4")
+    sys.modules["netCDF4"] = nc
+    sys.modules.pop("hydrophobic", None)
+    import hydrophobic
+    from geosmie_gb300 import lutfile
+    out = {}
+    for name in ("trivial", "seasalt"):
+        d = np.load(os.path.join(HERE, "table_%s.npz" % name))
+        table = {k[4:]: d[k] for k in d.files if k.startswith("out_")}
+        for legacy in (False, True):
+            dims, variables = lutfile.optics_file(table, table["rh"], table["wavelength"], table["ang"], legacy)
+            src = Dataset("in.nc", "w")
+            for dn, size in dims:
+                src.createDimension(dn, size)
+            for vn, code, vdims, data, attrs in variables:
+                v = src.createVariable(vn, "f8" if code == "f8" else "i8", vdims)
+                v.data[...] = data
+                for ak, av in attrs.items():
+                    setattr(v, ak, av)
+            hydrophobic.doConversion("in.nc", "out.nc", "", legacy)
+            res = files["out.nc"]
+            tag = "%s_%s" % (name, "legacy" if legacy else "new")
+            for vn, v in res.variables.items():
+                out["%s__%s" % (tag, vn)] = v.data
+    if saved is not None:
+        sys.modules["netCDF4"] = saved
+    np.savez_compressed(os.path.join(HERE, "hydrophobic.npz"), **out)
+    print("hydrophobic: %d arrays" % len(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -339,7 +447,7 @@ def main():
     sys.path.insert(0, os.path.join(src, "pymiecoated"))
     sys.path.insert(0, os.path.join(src, "geosmie"))
     from pymiecoated import mie_coated
-    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables", "bands"]
+    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables", "bands", "hydrophobic"]
     if "single" in sel:
         gen_single(mie_coated)
     if "coated" in sel:
@@ -350,6 +458,9 @@ def main():
         gen_tables(src, Dataset)
     if "bands" in sel:
         gen_bands(src, Dataset)
+    if "hydrophobic" in sel:
+        sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+        gen_hydrophobic(src)
 
 
 if __name__ == "__main__":
