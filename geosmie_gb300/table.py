@@ -22,7 +22,7 @@ import os
 import numpy as np
 import torch
 
-from . import _native
+from . import _native, growth
 from ._native import GRID_RADIUS, GRID_X, PSD_LOGNORM, PSD_POWER4, PSD_WEIGHTS  # noqa: F401
 
 SCATKEYS = ["p11", "p12", "p22", "p33", "p34", "p44"]
@@ -245,7 +245,8 @@ def _x_grid(params, b, minlam, maxlam):
 
 
 def _growth(rhdep, siz0, rh, allrh):
-    """humidityGrowth (particleparams.py:85-108) for 'simple', 'trivial', 'ss'."""
+    """humidityGrowth (particleparams.py:85-108): 'simple', 'trivial', 'ss'
+    (Gerber) and 'su' (CARMA sulfate, growth.grow_v75)."""
     rhi = list(allrh).index(rh)
     t = rhdep["type"]
     p = rhdep["params"]
@@ -256,7 +257,38 @@ def _growth(rhdep, siz0, rh, allrh):
             return siz0
         siz = siz0 * 100
         return (p["c1"] * siz ** p["c2"] / (p["c3"] * siz ** p["c4"] - np.log10(rh)) + siz ** 3.0) ** (1.0 / 3.0) / 100.0
-    raise NotImplementedError("growth law '%s' (CARMA 'su') is not implemented" % t)
+    if t == "su":
+        if rh == 0.0:
+            return siz0
+        return siz0 * float(growth.grow_v75(rh, siz0, temp=p["temp"]))
+    raise NotImplementedError("growth law '%s' is not implemented" % t)
+
+
+def _lognorm_weights(params, b, rh_list, x, dx, lams):
+    """Lognormal PSD weights of bin b with size-dependent growth ('su'):
+    calculatePSD's lognorm branch (dointegration.py:549-583) -- every mode
+    radius and upper bound grown by humidityGrowth at its own dry size,
+    getLogNormPSD (particleparams.py:113-128) in size-parameter space, times
+    the grid's dx, normalised -- [nl, nrh, ncomp, ns]."""
+    pp = params["psd"]["params"]
+    ncomp = len(pp["r0"][b])
+    out = np.zeros((lams.size, len(rh_list), ncomp, x.size))
+    for li, lam in enumerate(lams):
+        xconv = 2 * np.pi / lam
+        for ri, onerh in enumerate(rh_list):
+            for k in range(ncomp):
+                rmode = _growth(params["rhDep"], pp["r0"][b][k], onerh, rh_list)
+                rmax = _growth(params["rhDep"], pp["rmax0"][b][k], onerh, rh_list)
+                rmin = pp["rmin0"][b][k]
+                sig = pp["sigma"][b][k]
+                xmode, xmax, xmin = rmode * xconv, rmax * xconv, rmin * xconv
+                d = 1. / (x * (2 * np.pi) ** 0.5 * np.log(sig)) * np.exp(-(np.log(x / xmode) ** 2) /
+                                                                         (2. * np.log(sig) ** 2))
+                d[np.where(x >= xmax)] = 0.
+                d[np.where(x <= xmin)] = 0.
+                d = d * dx
+                out[li, ri, k] = d / np.sum(d)
+    return out
 
 
 def _ss_weights(params, b, rh_list, x, lams):
@@ -310,13 +342,13 @@ def bin_spec(params, b, mlist, waterm, ang, lambdas=None):
         if rtype in ("simple", "trivial"):
             gf[ri] = params["rhDep"]["params"]["gf"][ri]
             rrat[ri] = 1.0 / gf[ri]
-        elif rtype == "ss":
-            rminmaj = pp["rMinMaj"][b] if "rMinMaj" in pp else pp["rmin0"][b][0]
+        elif rtype in ("ss", "su"):   # getHumidRefractiveIndex :512-531
+            rminmaj = pp["rMinMaj"][b] if (rtype == "ss" and "rMinMaj" in pp) else pp["rmin0"][b][0]
             rminuse = _growth(params["rhDep"], rminmaj, rh[ri], rh)
             rrat[ri] = rminmaj / rminuse
             gf[ri] = 1.0 / rrat[ri]
         else:
-            raise NotImplementedError("growth law '%s' (CARMA 'su') is not implemented" % rtype)
+            raise NotImplementedError("growth law '%s' is not implemented" % rtype)
     # volume mixing (dointegration.py:505); components follow the PSD (one RI
     # table is shared by every component, as the reference replicates it)
     fr = list(pp["fracs"][b])
@@ -330,7 +362,16 @@ def bin_spec(params, b, mlist, waterm, ang, lambdas=None):
         "rhop": (rrat ** 3.0 * rhop0v + (1.0 - rrat ** 3.0) * 1000.0)[None, :], "rhop0": np.array([rhop0v]),
         "gf": gf, "ang": np.asarray(ang, np.float64), "rh0_index": rh.index(0.0) if 0.0 in rh else 0,
     }
-    if ptype == "lognorm":
+    if ptype == "lognorm" and rtype == "su":
+        # growth depends on the dry size: host-side weights of the grown modes
+        spec["psd_kind"] = PSD_WEIGHTS
+        spec["dgrid"] = dx
+        spec["weights"] = _lognorm_weights(params, b, rh_run, x, dx, lam)[:, :, None, :, :]
+        spec["psd_param"] = np.array([[[pp["r0"][b][k], pp["rmin0"][b][k], pp["rmax0"][b][k], pp["sigma"][b][k]]
+                                       for k in range(ncomp)]])
+        spec["rlow"] = np.array([pp["rmin0"][b][0]])
+        spec["rup"] = np.array([pp["rmax0"][b][0]])
+    elif ptype == "lognorm":
         spec["psd_kind"] = PSD_LOGNORM
         spec["dgrid"] = dx
         spec["psd_param"] = np.array([[[pp["r0"][b][k], pp["rmin0"][b][k], pp["rmax0"][b][k], pp["sigma"][b][k]]

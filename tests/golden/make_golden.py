@@ -224,6 +224,21 @@ TABLE_CASES = {
             "sigma": [[2.0]], "numperdec": [15], "fracs": [[1.0]]}},
         "ri": [[0.35, 1.75, -0.46], [0.55, 1.75, -0.44], [1.2, 1.77, -0.45]],
     },
+    # sulfate: CARMA 'su' growth (Tabazadeh weight percent, Kelvin effect; the
+    # growth of each mode radius depends on its dry size), two lognormal bins
+    "su": {
+        "rhop0": 1923.0,
+        "rh": [0.0, 0.5, 0.9, 0.99],
+        "rhDep": {"type": "su", "params": {"temp": 220.0}},
+        "psd": {"type": "lognorm", "params": {
+            "r0": [[0.0695e-6], [0.03e-6, 0.2e-6]],
+            "rmin0": [[0.005e-6], [0.004e-6, 0.004e-6]],
+            "rmax0": [[0.3e-6], [0.4e-6, 0.4e-6]],
+            "sigma": [[2.03], [1.6, 2.0]],
+            "numperdec": [15, 12],
+            "fracs": [[1.0], [0.6, 0.4]]}},
+        "ri": [[0.40, 1.44, -1e-8], [0.55, 1.43, -1e-8], [1.00, 1.42, -2e-6]],
+    },
     # sea-salt: Gerber growth, Gong PSD, maxrh capping
     "seasalt": {
         "rhop0": 2200.0,
@@ -247,7 +262,10 @@ def gen_tables(ref_src, Dataset):
         waterm = pp.getWaterM()
     finally:
         os.chdir(cwd)
+    only = os.environ.get("GOLDEN_TABLES")
     for name, case in TABLE_CASES.items():
+        if only and name not in only.split(","):
+            continue
         with tempfile.TemporaryDirectory() as td:
             ri = np.array(case["ri"], dtype=np.float64)
             rifile = os.path.join(td, "ri-%s.wsv" % name)

@@ -38,7 +38,7 @@ def _check_table(got, ref, prefix=""):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt"])
+@pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt", "su"])
 def test_reference_tables_gpu(name):
     from geosmie_gb300 import table
     g = load_golden("table_%s.npz" % name)
