@@ -70,8 +70,9 @@ __device__ __forceinline__ float f64_to_f32_bits(double v)
 }
 
 // N / (N - i M) in FP32 for N = (nr, ni), M = (mr, mi), with both scaled by
-// the denominator's largest component (no overflow of |q|^2 for any size).
-__device__ __forceinline__ float2 mie_ratio_f32(float nr, float ni, float mr, float mi)
+// the denominator's largest component (no overflow of |q|^2 for any size);
+// dsq = 1 / |N - i M|^2 (capped at the FP32 maximum, so that 0 x dsq = 0).
+__device__ __forceinline__ float2 mie_ratio_f32(float nr, float ni, float mr, float mi, float &dsq)
 {
     float qr = nr + mi, qi = ni - mr;
     const float s = __frcp_rn(fmaxf(fabsf(qr), fabsf(qi)));
@@ -80,6 +81,7 @@ __device__ __forceinline__ float2 mie_ratio_f32(float nr, float ni, float mr, fl
     nr *= s;
     ni *= s;
     const float inv = __frcp_rn(fmaf(qr, qr, qi * qi));
+    dsq = fminf(s * (s * inv), 3.4028235e38f);
     return make_float2(fmaf(nr, qr, ni * qi) * inv, fmaf(ni, qr, -nr * qi) * inv);
 }
 
@@ -98,8 +100,18 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 //     (D~ = D/m + n/x or D m + n/x), which cancel -- N for small x, both once
 //     psi and chi oscillate (n < x);
 // and the rest in FP32: D~ imaginary parts, the products N.im, M.im and the
-// ratio a = N / (N - i M).  Coefficients go to emit(k, a, b) from k = nmax
+// ratio a = N / (N - i M).  Coefficients go to emit(k, a, b, t) from k = nmax
 // down to 1.  row1 / rowf: psi_n, chi_n of x (FP64 / FP32) at [n - 1].
+//
+// t is the order's absorption without cancellation.  With r = M / N,
+// a = 1 / (1 - i r) and Re a - |a|^2 = Im(r) |a|^2; Im(M N*) = Im(D~) W with
+// W = psi_n chi_{n-1} - chi_n psi_{n-1} = -1 (the Riccati-Bessel Wronskian in
+// pymiecoated's sign, chi = -x y_n), so
+//   Re a - |a|^2 = -Im(D~) / |N - i M|^2
+// and t = Im(D~_a) / |N_a - i M_a|^2 + Im(D~_b) / |N_b - i M_b|^2, the two of
+// the same sign for a passive particle.  Re a - |a|^2 formed from the
+// coefficients themselves cancels: Re a and |a|^2 agree to 1 - 1e-8 for the
+// sulfate-like indices (Im m ~ 1e-8), far past FP32.
 // Emulated against the FP64 recurrences for x in [1e-3, 650] and the
 // benchmark indices: within 2.2e-7 of each instance's largest coefficient.
 template <class Emit>
@@ -154,9 +166,10 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
         const float mar = f64_to_f32_bits(fma(dar, pn.y, -pm.y)), mbr = f64_to_f32_bits(fma(dbr, pn.y, -pm.y));
         const float Dr = f64_to_f32_bits(D.re), Di = f64_to_f32_bits(D.im);
         const float dai = fmaf(Dr, mifi, Di * mifr), dbi = fmaf(Dr, mfi, Di * mfr);
-        const float2 a = mie_ratio_f32(nar, dai * pnf.x, mar, dai * pnf.y);
-        const float2 b = mie_ratio_f32(nbr, dbi * pnf.x, mbr, dbi * pnf.y);
-        emit(k, a, b);
+        float ida, idb;   // 1 / |N - i M|^2 of a and b
+        const float2 a = mie_ratio_f32(nar, dai * pnf.x, mar, dai * pnf.y, ida);
+        const float2 b = mie_ratio_f32(nbr, dbi * pnf.x, mbr, dbi * pnf.y, idb);
+        emit(k, a, b, fmaf(dai, ida, dbi * idb));
         pn = pm;
         pnf = pmf;
         nx -= xinv;
@@ -167,24 +180,28 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
 // pymiecoated/mie_props.py:28-70 from the FP32 a_n, b_n with Kahan
 // compensation (the accumulated rounding stays at the FP32 unit roundoff
 // whatever nmax is):
-//   ext = sum (2n+1) Re(a + b),  sca = sum (2n+1)(|a|^2 + |b|^2),
+//   sca = sum (2n+1)(|a|^2 + |b|^2),
+//   abs = sum (2n+1) t_n  (t_n of homog_core_mixed: -(Re(a + b) - |a|^2 - |b|^2)),
 //   asy = sum n(n+2)/(n+1) Re(a_n a*_{n+1} + b_n b*_{n+1}) + (2n+1)/(n(n+1)) Re(a_n b*_n),
 //   qb  = sum (2n+1)(-1)^n (a_n - b_n).
+// The reference's ext = sum (2n+1) Re(a + b) is formed as sca - abs: both
+// terms keep their relative precision, so qext, qsca and qabs = qext - qsca
+// all do, however weak or strong the absorption.
 struct EmitMixed {
     float4 *cf;
     float amax;
-    float ext, sca, asy, qbr, qbi;
-    float ext_c, sca_c, asy_c, qbr_c, qbi_c;   // Kahan compensations
+    float ab, sca, asy, qbr, qbi;
+    float ab_c, sca_c, asy_c, qbr_c, qbi_c;   // Kahan compensations
     float2 pa, pb;                             // a, b of order n+1 (zero above nmax)
     float inv_n1;                              // 1/(n+1)
-    __device__ __forceinline__ void operator()(int k, float2 a, float2 b) {
+    __device__ __forceinline__ void operator()(int k, float2 a, float2 b, float t) {
         const float4 q = make_float4(a.x + b.x, a.y + b.y, a.x - b.x, a.y - b.y);
         cf[k - 1] = q;
         amax = fmaxf(amax, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
         const float fk = (float)k;
         const float cn = 2.f * fk + 1.f;
         const float inv_n = __frcp_rn(fk);
-        kahan(ext, ext_c, cn * q.x);
+        kahan(ab, ab_c, cn * t);
         kahan(sca, sca_c, cn * (fmaf(a.x, a.x, a.y * a.y) + fmaf(b.x, b.x, b.y * b.y)));
         const float up = fmaf(a.x, pa.x, fmaf(a.y, pa.y, fmaf(b.x, pb.x, b.y * pb.y)));
         const float rab = fmaf(a.x, b.x, a.y * b.y);
@@ -336,15 +353,15 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     EmitMixed emit;
     emit.cf = cf + c;
     emit.amax = 0.f;
-    emit.ext = emit.sca = emit.asy = emit.qbr = emit.qbi = 0.f;
-    emit.ext_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
+    emit.ab = emit.sca = emit.asy = emit.qbr = emit.qbi = 0.f;
+    emit.ab_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
     emit.pa = emit.pb = make_float2(0.f, 0.f);
     emit.inv_n1 = __frcp_rn((float)(nmax + 1));
     homog_core_mixed(x, rc.z, rc.x, rc.y, h, v.pc + o, v.pcf + o, nmax, emit);
     const double iy2 = rc.z * rc.z;   // 1 / x^2
-    const double qext = 2.0 * ((double)emit.ext - (double)emit.ext_c) * iy2;
     const double sca = (double)emit.sca - (double)emit.sca_c;
     const double qsca = 2.0 * sca * iy2;
+    const double qext = qsca - 2.0 * ((double)emit.ab - (double)emit.ab_c) * iy2;
     const double qr = (double)emit.qbr - (double)emit.qbr_c, qi = (double)emit.qbi - (double)emit.qbi_c;
     double *o4 = v.eff4 + t * 4;
     o4[0] = qext;
