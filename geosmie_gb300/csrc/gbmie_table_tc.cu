@@ -69,6 +69,19 @@ __device__ __forceinline__ float f64_to_f32_bits(double v)
     return __uint_as_float(sign | ((unsigned)ef << 23) | mant);
 }
 
+// x 2^k as FP64 by integer operations on the bit pattern (exact: the FP64
+// exponent range holds every FP32 value times the powers of two used here;
+// zeros and FP32 subnormals give zero).  FP64 arithmetic and conversions
+// occupy GB300's narrow FP64 pipe; these are integer instructions.
+__device__ __forceinline__ double f32_to_f64_pow2(float x, int k)
+{
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0u) return 0.0;
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u + (unsigned)k) << 20) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // N / (N - i M) in FP32 for N = (nr, ni), M = (mr, mi), with both scaled by
 // the denominator's largest component (no overflow of |q|^2 for any size);
 // dsq = 1 / |N - i M|^2 (capped at the FP32 maximum, so that 0 x dsq = 0).
@@ -463,14 +476,18 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 // their PSD-weighted sums over sizes stay in its registers: no shared-memory
 // staging, no shuffles and no barrier among the epilogue warps.
 //
-// Pipeline (one CTA per SM, persistent, 10 warps):
+// Pipeline (one CTA per SM, persistent, 12 warps):
 //   warps 0-7   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
 //               angles) and columns of sizes 16 (w / 4) .. + 15 of the half
 //               tile; window sums -> Mueller -> PSD-weighted sums
-//   warp 8      MMA issue (one thread)
+//   warps 8, 10 MMA issue (one thread each; items alternate between them)
 //   warp 9      producer (one thread): bulk copies of the coefficient half
 //               tiles (split_rows) and of the angle functions of orders > 16
 //               into a TC_NS-stage shared-memory ring
+//   warp 11     weights: per item the chunk count, the unit's constants and
+//               the PSD weights, scaled and paired for the epilogue's packed
+//               FMAs, into a TC_NW-slot shared-memory ring (the epilogue
+//               warps make no global loads)
 // Work items are (unit, angle block, 64-size tile, half tile); a half tile
 // without sizes (the last tile of a grid) is skipped by every role.  TMEM
 // holds TC_NSETS accumulator sets (S+ 64 columns | S- 64 columns), so the
@@ -503,26 +520,31 @@ struct TcArgs {
 #define TC_NS 4                                        // ring stages
 #define TC_WIN_MAX TC_NS                               // longest accumulation window (chunks)
 #define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
-// resident angle-function chunks (angle blocks): 3 leave room for the running
-// sums of 6-8 bins
-#define TC_B0_SLOTS(NB) ((NB) > 5 ? 3 : 4)
+// resident angle-function chunks (angle blocks)
+#define TC_B0_SLOTS(NB) 4
 #define TC_A_BYTES (4 * TC_MAT_A)                      // P_hi P_lo Q_hi Q_lo of a chunk: 16 KB
 #define TC_B_BYTES (4 * TC_MAT_B)                      // C_hi C_lo D_hi D_lo of a half chunk: 8 KB
 #define TC_STAGE_BYTES (TC_B_BYTES + TC_A_BYTES)       // 24 KB
 #define TC_EPI_WARPS 8
 #define TC_EPI_THREADS (32 * TC_EPI_WARPS)
-#define TC_THREADS (TC_EPI_THREADS + 96)               // + two MMA warps and the producer warp
+#define TC_THREADS (TC_EPI_THREADS + 128)              // + two MMA warps, the producer and the weights warp
 // register bound of 12 warps: three warps on an SM sub-partition fit its
 // 16K registers at 168 each
 #define TC_REG_BOUND_THREADS 384
-#define TC_WBUF_FLOATS (2 * 16 * 16)                   // per epilogue warp: 2 items x 16 sizes x 8 bins x 2
-#define TC_SUM_FLOATS(NB) (2 * 4 * (NB) * TC_EPI_THREADS) // running sums (hi, lo) [2][4 NB][thread]
+#define TC_NW 6                                        // weight-ring slots (items)
+// mbarriers (2 TC_NS + 2 + 2 TC_NSETS + 1 + 2 TC_NW), the TMEM address, the
+// abort flag and the stages' chunk tags
+#define TC_CTRL_BYTES 512
+#define TC_WSLOT_FLOATS (16 + 32 * 16)                 // header + 32 sizes x 8 bins x (w, w)
+#define TC_SUM_FLOATS(NB) (4 * (NB) * TC_EPI_THREADS)  // running sums [bin][thread] of (E0 pair, E1 pair)
 #define TC_SMEM_BYTES(NB)                                                                                  \
-    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS * TC_STAGE_BYTES + TC_EPI_WARPS * TC_WBUF_FLOATS * 4 +               \
-     TC_SUM_FLOATS(NB) * 4 + 256)
+    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS * TC_STAGE_BYTES + TC_NW * TC_WSLOT_FLOATS * 4 +                     \
+     TC_SUM_FLOATS(NB) * 4 + TC_CTRL_BYTES)
+#define TC_NO_EX (-0x40000000)                         // no size: its weights are dropped
 #define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
 
 static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
+static_assert(8 * (2 * TC_NS + 2 + 2 * TC_NSETS + 1 + 2 * TC_NW) + 4 + 8 + 4 * TC_NS <= TC_CTRL_BYTES, "control block");
 static_assert(TC_SMEM_BYTES(5) <= 227 * 1024 && TC_SMEM_BYTES(8) <= 227 * 1024, "shared memory");
 
 // k-th unit of CTA `cta` among G CTAs: units in decreasing-work order,
@@ -538,13 +560,14 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sB0 = smem;                                            // resident angle chunks, orders 1..16
     uint8_t *sStage = sB0 + TC_B0_SLOTS(NB) * TC_A_BYTES;           // TC_NS x (coeff 8 KB | angles 16 KB)
-    float *sW = (float *)(sStage + TC_NS * TC_STAGE_BYTES);         // per epilogue warp [2][16 sizes][8 bins]
-    float *sSum = sW + TC_EPI_WARPS * TC_WBUF_FLOATS;               // per-(unit, block) sums [2][4 NB][thread]
+    float *sW = (float *)(sStage + TC_NS * TC_STAGE_BYTES);         // weight ring [TC_NW][TC_WSLOT_FLOATS]
+    float *sSum = sW + TC_NW * TC_WSLOT_FLOATS;                     // per-(unit, block) running sums
     uint64_t *bars = (uint64_t *)(sSum + TC_SUM_FLOATS(NB));
     uint64_t *full = bars, *empty = bars + TC_NS;
     uint64_t *b0_full = bars + 2 * TC_NS, *b0_empty = b0_full + 1;
     uint64_t *acc_full = b0_full + 2, *acc_empty = acc_full + TC_NSETS, *drain = acc_empty + TC_NSETS;
-    uint32_t *s_tmem = (uint32_t *)(drain + 1);
+    uint64_t *w_full = drain + 1, *w_empty = w_full + TC_NW;
+    uint32_t *s_tmem = (uint32_t *)(w_empty + TC_NW);
     volatile int *s_abort = (volatile int *)(s_tmem + 1);
     // s_chunk[st]: the chunk the producer is loading into stage st.  An issuer
     // skips the other issuer's chunks, so it can wait on a stage two phases
@@ -573,6 +596,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             mbar_init(acc_empty + i, TC_EPI_WARPS);
         }
         mbar_init(drain, 2);
+        for (int i = 0; i < TC_NW; ++i) {
+            mbar_init(w_full + i, 1);                 // the weights warp's lane 0
+            mbar_init(w_empty + i, TC_EPI_WARPS);     // every epilogue warp, after its compute
+        }
         fence_mbar_init();
         *s_abort = 0;
         for (int i = 0; i < TC_NS; ++i) s_chunk[i] = -1;
@@ -791,30 +818,26 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             }
         }
         __syncwarp();
-    } else {
-        // ================= epilogue (warps 0-7) =================
-        // Items in the MMA's order.  The PSD weights and the order count of
-        // item i + 1 are loaded while item i is processed; the weights go into
-        // this warp's other weight buffer at the start of item i + 1.
-        // Per size the thread forms E0 = (|S+|^2, |S-|^2) and
-        // E1 = (Re S+ S-*, Im S- S+*) and adds w_b E0, w_b E1 with packed FP32
-        // pair FMAs; the constant factors of the Mueller elements
-        //   s11 = (|S+|^2 + |S-|^2)/4, s12 = -Re(S+ S-*)/2,
-        //   s33 = (|S+|^2 - |S-|^2)/4, s34 = -Im(S- S+*)/2
-        // are applied to the unit's sums.
-        const int q = warp & 3, wh = warp >> 2;
-        float *wbuf = sW + warp * TC_WBUF_FLOATS;   // [2 items][16 sizes][8 bins][w, w]
-        // per-unit constants of this CTA's kq-th unit (valid = false past its last unit)
-        struct UnitC {
+    } else if (warp == 11) {
+        // ================= item info and PSD weights (one warp) =================
+        // Item i (the epilogue's order) gets weight-ring slot i % TC_NW: a
+        // header (the tile's 16-order chunk count, the unit's largest exponent
+        // E, its (wavelength, RH) index and component) and, per size s of the
+        // half tile (lane s), the bins' weights as pairs (w_b 2^(2 (e_s - E)),
+        // the same): the scaled, duplicated form the epilogue's packed FMAs read
+        // (E is the unit's largest exponent, so the power is <= 1; below 2^-126
+        // the weight is dropped).  The loads of item i + 1 are issued before the
+        // wait for item i's slot, so their latency overlaps it.
+        struct UnitW {
             bool valid;
             int comp, lr, E;
             const float *Wb;
             const int *ex;
-            const int64_t *off;
+            const int *tcb;
         };
-        auto unit_c = [&](int kq) -> UnitC {
-            UnitC u;
-            const int64_t uidx = tc_unit_index(kq, cta, G);
+        auto unit_w = [&](int k) -> UnitW {
+            UnitW u;
+            const int64_t uidx = tc_unit_index(k, cta, G);
             u.valid = uidx < n_units;
             if (!u.valid) return u;
             const int unit = g.unit_order[uidx];
@@ -825,61 +848,120 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             u.Wb = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + u.comp) * v.n_size;
             u.ex = g.eexp + (size_t)unit * v.n_size;
             u.E = g.eunit[unit];
-            u.off = v.off + (int64_t)v.le(lam) * v.n_size;
+            u.tcb = g.tile_cbase + (size_t)v.le(lam) * (ntl + 1);
             return u;
         };
-        // PSD weights scaled by 2^(2 (e_i - E)) (E is the unit's largest
-        // exponent, so the power is <= 1; below 2^-126 the weight is dropped)
-        // of this warp's 16 sizes of half tile h: lane l holds size l / 2,
-        // bins 4 (l % 2) .. + 3
-        // (loads only: the scaling waits for them at the next item's start)
-        auto fetch_w = [&](const UnitC &u, int tile, int h, float4 &wv, int &wex) {
-            const int si = tile * TC_INST + TC_HALF * h + 16 * wh + (lane >> 1);
-            const int b0 = 4 * (lane & 1);
-            float w[4] = {0.f, 0.f, 0.f, 0.f};
-            wex = -100000;
-            if (si < v.n_size && b0 < NB) {
-                wex = ldg_pin_s32(u.ex + si) - u.E;
+        struct WItem {
+            int cb0, cb1, ex;   // chunk bases of the tile; this lane's size exponent (TC_NO_EX: none)
+            float w[NB];
+        };
+        auto load_item = [&](const UnitW &u, int tile, int h, WItem &it) {
+            it.cb0 = ldg_pin_s32(u.tcb + tile);
+            it.cb1 = ldg_pin_s32(u.tcb + tile + 1);
+            const int si = tile * TC_INST + TC_HALF * h + lane;
+            it.ex = TC_NO_EX;
 #pragma unroll
-                for (int bb = 0; bb < 4; ++bb) {
-                    const int b = b0 + bb;
-                    if (b < v.n_bin && b < NB) w[bb] = ldg_pin_f32(u.Wb + (size_t)b * v.n_comp * v.n_size + si);
+            for (int b = 0; b < NB; ++b) it.w[b] = 0.f;
+            if (si < v.n_size) {
+                it.ex = ldg_pin_s32(u.ex + si);
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+                    if (b < v.n_bin) it.w[b] = ldg_pin_f32(u.Wb + (size_t)b * v.n_comp * v.n_size + si);
+            }
+        };
+        bool ok = true;
+        uint32_t iw = 0;
+        int kq = 0, ab = 0, tile = 0, h = 0;
+        UnitW u = unit_w(0);
+        // One step: issue the loads of the next item into nxt, wait for the
+        // current item's slot, store it from cur.  Steps alternate the roles
+        // of the two buffers (no register copies: a copy would wait for the
+        // loads it copies).
+        auto step = [&](const WItem &cur, WItem &nxt) {
+            const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
+            int nk = kq, nab = ab, nt = tile, nh = h + 1;
+            if (nh == 2 || TC_HALF * nh >= ntile) {
+                nh = 0;
+                if (++nt == ntl) {
+                    nt = 0;
+                    if (++nab == nblocks) {
+                        nab = 0;
+                        ++nk;
+                    }
                 }
             }
-            wv = make_float4(w[0], w[1], w[2], w[3]);
+            const UnitW un = nk == kq ? u : unit_w(nk);
+            if (un.valid) load_item(un, nt, nh, nxt);
+            const uint32_t slot = iw % TC_NW;
+            int go = 1;
+            if (lane == 0 && iw >= TC_NW)
+                go = mbar_wait_or_abort(w_empty + slot, (iw / TC_NW - 1) & 1u, s_abort, TC_SLEEP_NS) ? 1 : 0;
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) {
+                ok = false;
+                return;
+            }
+            float *ws = sW + slot * TC_WSLOT_FLOATS;
+            const int e = cur.ex == TC_NO_EX ? -100000 : 2 * (cur.ex - u.E);
+            const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
+            float w8[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) w8[b] = b < NB ? cur.w[b] * p2 : 0.f;
+            float4 *dst = (float4 *)(ws + 16 + 16 * lane);
+#pragma unroll
+            for (int b = 0; b < 8; b += 2) dst[b / 2] = make_float4(w8[b], w8[b], w8[b + 1], w8[b + 1]);
+            if (lane == 0) *(int4 *)ws = make_int4(cur.cb1 - cur.cb0, u.E, u.lr, u.comp);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(w_full + slot);
+            ++iw;
+            u = un;
+            kq = nk;
+            ab = nab;
+            tile = nt;
+            h = nh;
         };
-        // 16-order chunks of a tile (its last size has the largest nmax)
-        auto tile_chunks = [&](const UnitC &u, int tile) -> int {
-            const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
-            return (int)((ldg_pin_s64(u.off + t0 + ntile) - ldg_pin_s64(u.off + t0 + ntile - 1) + TC_KC16 - 1) /
-                         TC_KC16);
-        };
+        WItem ia, ib;
+        if (u.valid) load_item(u, 0, 0, ia);
+        while (ok && u.valid) {
+            step(ia, ib);
+            if (!ok || !u.valid) break;
+            step(ib, ia);
+        }
+        if (!ok && lane == 0) {
+            *s_abort = 1;
+            atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
+        }
+    } else {
+        // ================= epilogue (warps 0-7) =================
+        // Items in the MMA's order; each item's chunk count, unit constants
+        // and scaled PSD weights come from the weights warp's ring.
+        // Per size the thread forms E0 = (|S+|^2, |S-|^2) and
+        // E1 = (Re S+ S-*, Im S- S+*) and adds w_b E0, w_b E1 with packed FP32
+        // pair FMAs; the constant factors of the Mueller elements
+        //   s11 = (|S+|^2 + |S-|^2)/4, s12 = -Re(S+ S-*)/2,
+        //   s33 = (|S+|^2 - |S-|^2)/4, s34 = -Im(S- S+*)/2
+        // are applied to the unit's sums.
+        const int q = warp & 3, wh = warp >> 2;
         constexpr int NP = (NB + 1) / 2;   // 16-byte weight loads per size: two bins each
         bool ok = true;
         uint32_t wce[2] = {0u, 0u}, ie = 0;   // windows read per issuer; items
         int kq = 0, ab = 0, tile = 0, h = 0;
-        UnitC cu = unit_c(0);
-        float4 wn = make_float4(0.f, 0.f, 0.f, 0.f);
-        int wnex = -100000;
-        int nc = 0;
-        if (cu.valid) {
-            nc = tile_chunks(cu, 0);
-            if (32 * q < v.n_ang) fetch_w(cu, 0, 0, wn, wnex);
-        }
-        // tile sums in registers; per-(unit, block) sums as unevaluated pairs
-        // (hi + lo) in this thread's column of sSum: [hi, lo][bin][thread] of
-        // (E0 pair, E1 pair), 16 bytes per access
+        // Sums over sizes: acc[e][b] (registers) collects a tile's w_b E_e
+        // (packed pairs); at the tile's end the running sum H (this thread's
+        // column of sSum: [bin][thread] of (E0 pair, E1 pair), 16 bytes per
+        // access) takes H + acc by an exact two-sum whose rounding error
+        // stays in acc as the next tile's start (block-wise compensated
+        // summation), so the per-(unit, block) sum H + acc keeps FP32
+        // relative precision whatever the size count.
         f32x2 acc[2][NB];
-        ulonglong2 *suh = (ulonglong2 *)sSum + tid, *sul = suh + NB * TC_EPI_THREADS;
+        ulonglong2 *sh = (ulonglong2 *)sSum + tid;
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
             acc[0][b] = acc[1][b] = 0ull;
-            suh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
-            sul[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
+            sh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
         }
-        while (ok && cu.valid) {
+        while (ok && tc_unit_index(kq, cta, G) < n_units) {
             const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
-            const int nwin = (nc + g.win - 1) / g.win;
             const bool active = TC_ABLK * ab + 32 * q < v.n_ang;   // this warp has angles in the block
             // the next item
             int nk = kq, nab = ab, nt = tile, nh = h + 1;
@@ -893,22 +975,24 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     }
                 }
             }
-            const UnitC nu = nk == kq ? cu : unit_c(nk);
-            float *wb = wbuf + (ie & 1) * (TC_WBUF_FLOATS / 2);
-            if (active) {   // duplicated pairs (w_b, w_b) for the packed FMAs
-                const int e = 2 * wnex;
-                const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
-                const float4 w = make_float4(wn.x * p2, wn.y * p2, wn.z * p2, wn.w * p2);
-                *(float4 *)(wb + 8 * lane) = make_float4(w.x, w.x, w.y, w.y);
-                *(float4 *)(wb + 8 * lane + 4) = make_float4(w.z, w.z, w.w, w.w);
+            // the item's slot of the weight ring
+            const uint32_t wsl = ie % TC_NW;
+            {
+                int go = 1;
+                if (lane == 0) go = mbar_wait_or_abort(w_full + wsl, (ie / TC_NW) & 1u, s_abort) ? 1 : 0;
+                go = __shfl_sync(0xffffffffu, go, 0);
+                if (!go) {
+                    ok = false;
+                    break;
+                }
             }
-            __syncwarp();
-            int nc_next = 0;
-            if (nu.valid) {   // in flight during this item
-                nc_next = nh == 0 ? tile_chunks(nu, nt) : nc;
-                if (TC_ABLK * nab + 32 * q < v.n_ang) fetch_w(nu, nt, nh, wn, wnex);
-            }
-            // window sums of S+ and S- (this lane's angle, 16 sizes x Re/Im)
+            const float *ws = sW + wsl * TC_WSLOT_FLOATS;
+            const int4 hdr = *(const int4 *)ws;   // chunk count, E, (wavelength, RH) index, component
+            const int nwin = (hdr.x + g.win - 1) / g.win;
+            const float *wb = ws + 16 + 16 * 16 * wh;   // this warp's 16 sizes
+            // window sums of S+ and S- (this lane's angle, 16 sizes x Re/Im);
+            // later windows are added in pieces of 4 sizes (fewer live
+            // registers)
             float rp[32], rm[32];
             const uint32_t ip = ie & 1u;   // the item's issuer
             for (int w = 0; w < nwin; ++w) {
@@ -927,12 +1011,15 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     if (w == 0) {
                         tmem_ld32x2(ta, ta + 64, rp, rm);
                     } else {
-                        float t[32], u[32];
-                        tmem_ld32x2(ta, ta + 64, t, u);
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) {
-                            rp[i] += t[i];
-                            rm[i] += u[i];
+                        for (int hf = 0; hf < 4; ++hf) {
+                            float t[8], u[8];
+                            tmem_ld8x2(ta + 8 * hf, ta + 64 + 8 * hf, t, u);
+#pragma unroll
+                            for (int i = 0; i < 8; ++i) {
+                                rp[8 * hf + i] += t[i];
+                                rm[8 * hf + i] += u[i];
+                            }
                         }
                     }
                 }
@@ -944,85 +1031,106 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             }
             if (!ok) break;
             if (active) {
-                // all sizes' pairs first (independent work for the scheduler), then
-                // the weighted sums; rp/rm die as E0/E1 are formed
-                f32x2 E0[16], E1[16];
+                // per group of 8 sizes: the pairs first (independent work for the
+                // scheduler), then the weighted sums; rp/rm die as E0/E1 are formed
 #pragma unroll
-                for (int s = 0; s < 16; ++s) {
-                    const float pr = rp[2 * s], pi = rp[2 * s + 1], mr = rm[2 * s], mi = rm[2 * s + 1];
-                    E0[s] = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
-                    E1[s] = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
-                }
+                for (int sg = 0; sg < 16; sg += 8) {
+                    f32x2 E0[8], E1[8];
 #pragma unroll
-                for (int s = 0; s < 16; ++s) {
-                    const f32x2 e0 = E0[s], e1 = E1[s];
-                    const ulonglong2 *wp = (const ulonglong2 *)(wb + 16 * s);
+                    for (int s = 0; s < 8; ++s) {
+                        const float pr = rp[2 * (sg + s)], pi = rp[2 * (sg + s) + 1], mr = rm[2 * (sg + s)],
+                                    mi = rm[2 * (sg + s) + 1];
+                        E0[s] = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
+                        E1[s] = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
+                    }
 #pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        const ulonglong2 w2 = wp[p];   // (w_2p, w_2p), (w_2p+1, w_2p+1)
-                        acc[0][2 * p] = f2_fma(w2.x, e0, acc[0][2 * p]);
-                        acc[1][2 * p] = f2_fma(w2.x, e1, acc[1][2 * p]);
-                        if (2 * p + 1 < NB) {
-                            acc[0][2 * p + 1] = f2_fma(w2.y, e0, acc[0][2 * p + 1]);
-                            acc[1][2 * p + 1] = f2_fma(w2.y, e1, acc[1][2 * p + 1]);
+                    for (int s = 0; s < 8; ++s) {
+                        const f32x2 e0 = E0[s], e1 = E1[s];
+                        const ulonglong2 *wp = (const ulonglong2 *)(wb + 16 * (sg + s));
+#pragma unroll
+                        for (int p = 0; p < NP; ++p) {
+                            const ulonglong2 w2 = wp[p];   // (w_2p, w_2p), (w_2p+1, w_2p+1)
+                            acc[0][2 * p] = f2_fma(w2.x, e0, acc[0][2 * p]);
+                            acc[1][2 * p] = f2_fma(w2.x, e1, acc[1][2 * p]);
+                            if (2 * p + 1 < NB) {
+                                acc[0][2 * p + 1] = f2_fma(w2.y, e0, acc[0][2 * p + 1]);
+                                acc[1][2 * p + 1] = f2_fma(w2.y, e1, acc[1][2 * p + 1]);
+                            }
                         }
                     }
                 }
             }
+            // the slot is read (every warp, active or not, waited for it first)
+            __syncwarp();
+            if (lane == 0) mbar_arrive(w_empty + wsl);
             if (nh == 0) {
-                // end of a tile: two-sum (hi + lo) += acc, exactly rounded
-                ulonglong2 H[NB], Lo[NB];
-#pragma unroll
-                for (int b = 0; b < NB; ++b) {
-                    H[b] = suh[b * TC_EPI_THREADS];
-                    Lo[b] = sul[b * TC_EPI_THREADS];
-                }
-                auto two_sum = [](f32x2 &hi, f32x2 &lo, f32x2 a) {
+                // end of a tile: H += acc exactly rounded, the error stays in acc
+                auto two_sum = [](f32x2 &hi, f32x2 &a) {
                     const f32x2 sum = f2_add(hi, a);
                     const f32x2 bp = f2_sub(sum, hi);
-                    lo = f2_add(lo, f2_add(f2_sub(hi, f2_sub(sum, bp)), f2_sub(a, bp)));
+                    a = f2_add(f2_sub(hi, f2_sub(sum, bp)), f2_sub(a, bp));
                     hi = sum;
                 };
 #pragma unroll
                 for (int b = 0; b < NB; ++b) {
-                    two_sum(H[b].x, Lo[b].x, acc[0][b]);
-                    two_sum(H[b].y, Lo[b].y, acc[1][b]);
-                    acc[0][b] = acc[1][b] = 0ull;
-                    suh[b * TC_EPI_THREADS] = H[b];
-                    sul[b * TC_EPI_THREADS] = Lo[b];
+                    ulonglong2 Hb = sh[b * TC_EPI_THREADS];
+                    two_sum(Hb.x, acc[0][b]);
+                    two_sum(Hb.y, acc[1][b]);
+                    sh[b * TC_EPI_THREADS] = Hb;
                 }
                 if (nt == 0) {
-                    // end of the (unit, angle block): this thread's share of the unit's sums
+                    // end of the (unit, angle block): this thread's share of the unit's
+                    // sums.  Each sum is the unevaluated pair H + acc; the Mueller
+                    // combinations are formed on the pairs in FP32 (two-sum for
+                    // E0a +- E0b) and both parts go to the FP64 accumulator, scaled by
+                    // 2^(2 (E - 13)) exactly in the integer domain.
                     const int ang = TC_ABLK * ab + 32 * q + lane;
                     if (ang < v.n_ang) {
-                        const double f2 = ldexp(1.0, 2 * (cu.E - SHIFT_BITS));
+                        const int k2 = 2 * (hdr.y - SHIFT_BITS);
 #pragma unroll
                         for (int b = 0; b < NB; ++b) {
                             if (b < v.n_bin) {
-                                const double f = v.frac[(size_t)b * v.n_comp + cu.comp] * f2;
-                                double e[4];
-                                const ulonglong2 hb = suh[b * TC_EPI_THREADS], lb = sul[b * TC_EPI_THREADS];
-#pragma unroll
-                                for (int ee = 0; ee < 2; ++ee) {
-                                    float h0, h1, l0, l1;
-                                    f2_unpack(ee ? hb.y : hb.x, h0, h1);
-                                    f2_unpack(ee ? lb.y : lb.x, l0, l1);
-                                    e[2 * ee] = (double)h0 + (double)l0;
-                                    e[2 * ee + 1] = (double)h1 + (double)l1;
+                                const double fr = v.frac[(size_t)b * v.n_comp + hdr.w];
+                                const ulonglong2 Hb = sh[b * TC_EPI_THREADS];
+                                float h0, h1, h2, h3, l0, l1, l2, l3;
+                                f2_unpack(Hb.x, h0, h1);
+                                f2_unpack(Hb.y, h2, h3);
+                                f2_unpack(acc[0][b], l0, l1);
+                                f2_unpack(acc[1][b], l2, l3);
+                                float mh[4], ml[4];
+                                {
+                                    const float sp = h0 + h1, bp = sp - h0;
+                                    const float ep = (h0 - (sp - bp)) + (h1 - bp);
+                                    const float sm = h0 - h1, bm = sm - h0;
+                                    const float em = (h0 - (sm - bm)) + (-h1 - bm);
+                                    mh[0] = 0.25f * sp;
+                                    ml[0] = 0.25f * (ep + (l0 + l1));
+                                    mh[2] = 0.25f * sm;
+                                    ml[2] = 0.25f * (em + (l0 - l1));
+                                    mh[1] = -0.5f * h2;
+                                    ml[1] = -0.5f * l2;
+                                    mh[3] = -0.5f * h3;
+                                    ml[3] = -0.5f * l3;
                                 }
-                                const double m[4] = {0.25 * (e[0] + e[1]), -0.5 * e[2], 0.25 * (e[0] - e[1]),
-                                                     -0.5 * e[3]};
+                                const bool unit_frac = __double_as_longlong(fr) == 0x3FF0000000000000ll;
 #pragma unroll
-                                for (int k = 0; k < 4; ++k)
-                                    atomicAdd(v.pacc + (((size_t)cu.lr * v.n_bin + b) * 4 + k) * v.n_ang + ang,
-                                              f * m[k]);
+                                for (int k = 0; k < 4; ++k) {
+                                    double a = f32_to_f64_pow2(mh[k], k2), c = f32_to_f64_pow2(ml[k], k2);
+                                    if (!unit_frac) {
+                                        a *= fr;
+                                        c *= fr;
+                                    }
+                                    double *dst = v.pacc + (((size_t)hdr.z * v.n_bin + b) * 4 + k) * v.n_ang + ang;
+                                    atomicAdd(dst, a);
+                                    atomicAdd(dst, c);
+                                }
                             }
                         }
                     }
 #pragma unroll
                     for (int b = 0; b < NB; ++b) {
-                        suh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
-                        sul[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
+                        acc[0][b] = acc[1][b] = 0ull;
+                        sh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
                     }
                 }
             }
@@ -1030,8 +1138,6 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             ab = nab;
             tile = nt;
             h = nh;
-            cu = nu;
-            nc = nc_next;
             ++ie;
         }
         if (!ok && lane == 0) {
