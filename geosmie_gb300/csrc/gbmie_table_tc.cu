@@ -676,9 +676,13 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                     const uint32_t c = it + j, st = c % TC_NS, par = (c / TC_NS) & 1u;
                                     ok = false;
                                     for (uint32_t tr = 0; tr < (1u << 26); ++tr) {
-                                        if (s_chunk[st] == (int)c && mbar_try(full + st, par)) {
-                                            ok = true;
-                                            break;
+                                        if (s_chunk[st] == (int)c) {
+                                            if (mbar_try(full + st, par)) {
+                                                ok = true;
+                                                break;
+                                            }
+                                        } else {
+                                            __nanosleep(TC_SLEEP_NS);   // the producer has not reached c
                                         }
                                         if ((tr & 255u) == 255u && *s_abort) break;
                                     }
@@ -821,7 +825,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
     } else if (warp == 11) {
         // ================= item info and PSD weights (one warp) =================
         // Item i (the epilogue's order) gets weight-ring slot i % TC_NW: a
-        // header (the tile's 16-order chunk count, the unit's largest exponent
+        // header (the tile's accumulation-window count, the unit's largest exponent
         // E, its (wavelength, RH) index and component) and, per size s of the
         // half tile (lane s), the bins' weights as pairs (w_b 2^(2 (e_s - E)),
         // the same): the scaled, duplicated form the epilogue's packed FMAs read
@@ -910,7 +914,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             float4 *dst = (float4 *)(ws + 16 + 16 * lane);
 #pragma unroll
             for (int b = 0; b < 8; b += 2) dst[b / 2] = make_float4(w8[b], w8[b], w8[b + 1], w8[b + 1]);
-            if (lane == 0) *(int4 *)ws = make_int4(cur.cb1 - cur.cb0, u.E, u.lr, u.comp);
+            if (lane == 0) *(int4 *)ws = make_int4((cur.cb1 - cur.cb0 + g.win - 1) / g.win, u.E, u.lr, u.comp);
             __syncwarp();
             if (lane == 0) mbar_arrive(w_full + slot);
             ++iw;
@@ -987,8 +991,8 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 }
             }
             const float *ws = sW + wsl * TC_WSLOT_FLOATS;
-            const int4 hdr = *(const int4 *)ws;   // chunk count, E, (wavelength, RH) index, component
-            const int nwin = (hdr.x + g.win - 1) / g.win;
+            const int4 hdr = *(const int4 *)ws;   // windows, E, (wavelength, RH) index, component
+            const int nwin = hdr.x;
             const float *wb = ws + 16 + 16 * 16 * wh;   // this warp's 16 sizes
             // window sums of S+ and S- (this lane's angle, 16 sizes x Re/Im);
             // later windows are added in pieces of 4 sizes (fewer live
