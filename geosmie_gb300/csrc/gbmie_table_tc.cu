@@ -23,6 +23,7 @@
 // absorb 2^(2(e_i - E)) with E the unit's largest exponent), accumulating
 // per unit in FP64.  Per-size phase matrices never reach global memory.
 #include "common.cuh"
+#include "df.cuh"
 #include "mie_device.cuh"
 #include "table_internal.cuh"
 #include "tc.cuh"
@@ -107,14 +108,21 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 }
 
 // The homogeneous recurrences of homog_core (pymiecoated/mie_coeffs.py:132-180)
-// with FP64 kept where stability needs it:
-//   * the downward D_n recurrence (its reciprocal by rcp_newton),
+// with double-float pairs (df.cuh, ~2^-46) where stability needs more than
+// FP32:
+//   * the downward D_n recurrence (r_k = (k+1)/z formed per step, the
+//     reciprocal by df_rcp),
 //   * the real parts of N = D~ psi_n - psi_{n-1} and M = D~ chi_n - chi_{n-1}
 //     (D~ = D/m + n/x or D m + n/x), which cancel -- N for small x, both once
 //     psi and chi oscillate (n < x);
 // and the rest in FP32: D~ imaginary parts, the products N.im, M.im and the
 // ratio a = N / (N - i M).  Coefficients go to emit(k, a, b, t) from k = nmax
-// down to 1.  row1 / rowf: psi_n, chi_n of x (FP64 / FP32) at [n - 1].
+// down to 1.  rowd: psi_n, chi_n of x as pairs (psi hi, lo, chi hi, lo) at
+// [n - 1].  GB300's FP64 pipe issues a small fraction of the FP32 rate, so
+// the pairs (a few FP32 operations per FP64 one) run these recurrences
+// several times faster than FP64 did; the precision they keep (2^-46 against
+// 2^-53) is far below the FP32 coefficients this path emits: the largest
+// cancellation, N at the smallest sizes (O(x^2), x >= 1e-3), costs 20 bits.
 //
 // t is the order's absorption without cancellation.  With r = M / N,
 // a = 1 / (1 - i r) and Re a - |a|^2 = Im(r) |a|^2; Im(M N*) = Im(D~) W with
@@ -125,18 +133,17 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 // the same sign for a passive particle.  Re a - |a|^2 formed from the
 // coefficients themselves cancels: Re a and |a|^2 agree to 1 - 1e-8 for the
 // sulfate-like indices (Im m ~ 1e-8), far past FP32.
-// Emulated against the FP64 recurrences for x in [1e-3, 650] and the
-// benchmark indices: within 2.2e-7 of each instance's largest coefficient.
 template <class Emit>
 __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double sx, double cxv, const HomogIndex &h,
-                                                 const double2 *__restrict__ row1, const float2 *__restrict__ rowf,
-                                                 int nmax, Emit &emit)
+                                                 const float4 *__restrict__ rowd, int nmax, Emit &emit)
 {
-    const cplx m = h.m, minv = h.minv;
-    const float mfr = (float)m.re, mfi = (float)m.im, mifr = (float)minv.re, mifi = (float)minv.im;
+    const float mfr = (float)h.m.re, mfi = (float)h.m.im, mifr = (float)h.minv.re, mifi = (float)h.minv.im;
+    const df m_re = df_from_f64(h.m.re), m_im = df_from_f64(h.m.im);
+    const df mi_re = df_from_f64(h.minv.re), mi_im = df_from_f64(h.minv.im);
     const double az = h.azm * x;
     const int nmx = (int)rint(fmax((double)nmax, az) + 16.0);
-    const cplx zinv = h.zminv * xinv;
+    const cdf zinv = cdf{df_from_f64(h.zminv.re * xinv), df_from_f64(h.zminv.im * xinv)};
+    const df xi = df_from_f64(xinv);
     // Warm-up steps above nmax.  When |z| < nmax + 1 every step lies where
     // the recurrence damps the start error by (|z| / (2n+1))^2 per step, so
     // the steps are counted for a damping of e^-23 (1e-10; the FP64 path
@@ -148,44 +155,40 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
         const int need = (int)ceilf(23.0f / q) + 2;
         if (need < warm) warm = need;
     }
-    cplx D = cx(0.0, 0.0);
-    // r_k = (k+1)/z and k/x step down by 1/z and 1/x (no integer conversion
-    // per order; the accumulated rounding stays near 1e-13)
-    cplx r = zinv * (double)(nmax + warm + 1);
+    cdf D = cdf{df{0.f, 0.f}, df{0.f, 0.f}};
     for (int k = nmax + warm; k > nmax; --k) {
-        const cplx w = D + r;
-        const double iw = rcp_newton(abs2(w));
-        D = cx(fma(-w.re, iw, r.re), fma(w.im, iw, r.im));   // r - 1/w
-        r = r - zinv;
+        const cdf r = cdf_mul_f(zinv, (float)(k + 1));   // (k+1)/z
+        const cdf w = cdf_add(D, r);
+        const df iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
+        D = cdf{df_fma(df_neg(w.re), iw, r.re), df_fma(w.im, iw, r.im)};   // r - 1/w
     }
-    cplx rk = r;                            // r_nmax = (nmax+1)/z
-    cplx w = D + rk;                        // D_{nmax+1} + r_nmax
-    double iw = rcp_newton(abs2(w));
-    double2 pn = row1[nmax - 1];
-    float2 pnf = rowf[nmax - 1];
-    double nx = (double)nmax * xinv;        // k/x
+    cdf rk = cdf_mul_f(zinv, (float)(nmax + 1));   // r_nmax = (nmax+1)/z
+    cdf w = cdf_add(D, rk);                         // D_{nmax+1} + r_nmax
+    df iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
+    float4 pn = rowd[nmax - 1];
+    const df s0 = df_from_f64(sx), c0 = df_from_f64(cxv);   // psi_0 = sin x, chi_0 = cos x
     for (int k = nmax; k >= 1; --k) {
-        D = cx(fma(-w.re, iw, rk.re), fma(w.im, iw, rk.im));   // D_k
-        rk = rk - zinv;                                          // r_{k-1} = k/z
+        D = cdf{df_fma(df_neg(w.re), iw, rk.re), df_fma(w.im, iw, rk.im)};   // D_k
         if (k > 1) {
-            w = D + rk;
-            iw = rcp_newton(abs2(w));
+            rk = cdf_mul_f(zinv, (float)k);   // r_{k-1} = k/z
+            w = cdf_add(D, rk);
+            iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
         }
-        const double2 pm = (k > 1) ? row1[k - 2] : make_double2(sx, cxv);
-        const float2 pmf = (k > 1) ? rowf[k - 2] : make_float2((float)sx, (float)cxv);
-        const double dar = fma(D.re, minv.re, fma(-D.im, minv.im, nx));   // Re(D/m) + k/x
-        const double dbr = fma(D.re, m.re, fma(-D.im, m.im, nx));         // Re(D m) + k/x
-        const float nar = f64_to_f32_bits(fma(dar, pn.x, -pm.x)), nbr = f64_to_f32_bits(fma(dbr, pn.x, -pm.x));
-        const float mar = f64_to_f32_bits(fma(dar, pn.y, -pm.y)), mbr = f64_to_f32_bits(fma(dbr, pn.y, -pm.y));
-        const float Dr = f64_to_f32_bits(D.re), Di = f64_to_f32_bits(D.im);
+        const float4 pm = (k > 1) ? rowd[k - 2] : make_float4(s0.hi, s0.lo, c0.hi, c0.lo);
+        const df nx = df_mul_f(xi, (float)k);   // k/x
+        const df dar = df_fma(D.re, mi_re, df_fma(df_neg(D.im), mi_im, nx));   // Re(D/m) + k/x
+        const df dbr = df_fma(D.re, m_re, df_fma(df_neg(D.im), m_im, nx));     // Re(D m) + k/x
+        const df psn = df{pn.x, pn.y}, chn = df{pn.z, pn.w};
+        const df psm = df{-pm.x, -pm.y}, chm = df{-pm.z, -pm.w};
+        const float nar = df_fma(dar, psn, psm).hi, nbr = df_fma(dbr, psn, psm).hi;
+        const float mar = df_fma(dar, chn, chm).hi, mbr = df_fma(dbr, chn, chm).hi;
+        const float Dr = D.re.hi, Di = D.im.hi;
         const float dai = fmaf(Dr, mifi, Di * mifr), dbi = fmaf(Dr, mfi, Di * mfr);
         float ida, idb;   // 1 / |N - i M|^2 of a and b
-        const float2 a = mie_ratio_f32(nar, dai * pnf.x, mar, dai * pnf.y, ida);
-        const float2 b = mie_ratio_f32(nbr, dbi * pnf.x, mbr, dbi * pnf.y, idb);
+        const float2 a = mie_ratio_f32(nar, dai * pn.x, mar, dai * pn.z, ida);
+        const float2 b = mie_ratio_f32(nbr, dbi * pn.x, mbr, dbi * pn.z, idb);
         emit(k, a, b, fmaf(dai, ida, dbi * idb));
         pn = pm;
-        pnf = pmf;
-        nx -= xinv;
     }
 }
 
@@ -370,7 +373,7 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     emit.ab_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
     emit.pa = emit.pb = make_float2(0.f, 0.f);
     emit.inv_n1 = __frcp_rn((float)(nmax + 1));
-    homog_core_mixed(x, rc.z, rc.x, rc.y, h, v.pc + o, v.pcf + o, nmax, emit);
+    homog_core_mixed(x, rc.z, rc.x, rc.y, h, v.pcd + o, nmax, emit);
     const double iy2 = rc.z * rc.z;   // 1 / x^2
     const double sca = (double)emit.sca - (double)emit.sca_c;
     const double qsca = 2.0 * sca * iy2;
@@ -387,13 +390,15 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     split_rows(v, unit, i, ex, nmax, cf + c, tile_cbase, unit_cbase, ntiles, asplit);
 }
 
-// FP32 copy of the psi/chi rows for the FP32 parts of the mixed recurrences.
-__global__ void k_f64x2_to_f32x2(int64_t n, const double2 *__restrict__ src, float2 *__restrict__ dst)
+// The psi/chi rows as FP32 pairs (psi hi, lo, chi hi, lo) for the mixed
+// recurrences.
+__global__ void k_rows_df(int64_t n, const double2 *__restrict__ src, float4 *__restrict__ dst)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         const double2 v = src[i];
-        dst[i] = make_float2((float)v.x, (float)v.y);
+        const df p = df_from_f64(v.x), c = df_from_f64(v.y);
+        dst[i] = make_float4(p.hi, p.lo, c.hi, c.lo);
     }
 }
 
@@ -1166,8 +1171,8 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     int *eexp = (int *)(scr + p->o_eexp);
     int *eunit = (int *)(scr + p->o_eunit);
     ctx_pre_launch(ctx);
-    k_f64x2_to_f32x2<<<(unsigned)ceil_div64(p->pc_total, 256), 256, 0, st>>>(p->pc_total, v.pc, v.pcf);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_f64x2_to_f32x2"));
+    k_rows_df<<<(unsigned)ceil_div64(p->pc_total, 256), 256, 0, st>>>(p->pc_total, v.pc, v.pcd);
+    GBMIE_TRY(ctx_check_launch(ctx, "k_rows_df"));
     ctx_pre_launch(ctx);
     k_fill_int<<<(unsigned)ceil_div64(p->n_units, 256), 256, 0, st>>>((int)p->n_units, eunit, -100000);
     GBMIE_TRY(ctx_check_launch(ctx, "k_fill_int"));

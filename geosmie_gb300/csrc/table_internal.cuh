@@ -105,7 +105,7 @@ struct TabView {
     double4 *rowc;      // per size row: sin x, cos x, 1/x
     HomogIndex *hidx;   // per unit: medium constants of the recurrences
     const double2 *pq;
-    float2 *pcf;        // FP32 copy of pc (mixed path)
+    float4 *pcd;        // pc as FP32 pairs: psi hi, lo, chi hi, lo (mixed path)
     // PSD weights, their radius moments and reff0 do not depend on the
     // wavelength when the grid is a radius grid and the PSD is analytic
     // (x = 2 pi r / lambda: the lognormal argument ln(x / x_mode) and the
