@@ -573,6 +573,8 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.rowc = (double4 *)(scr + p->o_rowc);
     v.hidx = (HomogIndex *)(scr + p->o_hidx);
     v.pcd = p->d.precision == GBMIE_MIXED ? (float4 *)(scr + p->o_pcf) : nullptr;
+    v.hdf = p->d.precision == GBMIE_MIXED ? (float4 *)(scr + p->o_hdf) : nullptr;
+    v.rowcd = p->d.precision == GBMIE_MIXED ? (float4 *)(scr + p->o_rowcd) : nullptr;
     return v;
 }
 
@@ -819,6 +821,8 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
         p->o_asplit = carve(mixed ? (size_t)16384 * (size_t)p->n_chunks : 16);
         p->o_pcf = carve(mixed ? sizeof(float4) * (size_t)p->pc_total : 16);
+        p->o_hdf = carve(mixed ? 4 * sizeof(float4) * (size_t)p->n_units : 16);
+        p->o_rowcd = carve(mixed ? 2 * sizeof(float4) * (size_t)p->n_le * d.n_size : 16);
         p->o_dscr = carve(d.m_core ? 5 * sizeof(double2) * (size_t)p->ab_total : 16);
         p->o_wf = carve(mixed ? sizeof(float) * nW * d.n_size : 16);
         p->o_tw = carve(sizeof(double) * d.n_ang);

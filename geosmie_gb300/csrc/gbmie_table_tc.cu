@@ -83,6 +83,9 @@ __device__ __forceinline__ double f32_to_f64_pow2(float x, int k)
     return __hiloint2double((int)hi, (int)(u << 29));
 }
 
+// pair -> FP64 (one FP64 addition)
+__device__ __forceinline__ double df_to_f64(df a) { return f32_to_f64_pow2(a.hi, 0) + f32_to_f64_pow2(a.lo, 0); }
+
 // N / (N - i M) in FP32 for N = (nr, ni), M = (mr, mi), with both scaled by
 // the denominator's largest component (no overflow of |q|^2 for any size);
 // dsq = 1 / |N - i M|^2 (capped at the FP32 maximum, so that 0 x dsq = 0).
@@ -133,25 +136,29 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 // the same sign for a passive particle.  Re a - |a|^2 formed from the
 // coefficients themselves cancels: Re a and |a|^2 agree to 1 - 1e-8 for the
 // sulfate-like indices (Im m ~ 1e-8), far past FP32.
+//
+// hd: the unit's constants as pairs (k_mixed_consts): m, 1/m, x/z, (|z|/x);
+// r0 = (sin x, cos x) = (psi_0, chi_0) and xi = 1/x as pairs, xf = x.
 template <class Emit>
-__device__ __forceinline__ void homog_core_mixed(double x, double xinv, double sx, double cxv, const HomogIndex &h,
+__device__ __forceinline__ void homog_core_mixed(const float4 *__restrict__ hd, float4 r0, df xi, float xf,
                                                  const float4 *__restrict__ rowd, int nmax, Emit &emit)
 {
-    const float mfr = (float)h.m.re, mfi = (float)h.m.im, mifr = (float)h.minv.re, mifi = (float)h.minv.im;
-    const df m_re = df_from_f64(h.m.re), m_im = df_from_f64(h.m.im);
-    const df mi_re = df_from_f64(h.minv.re), mi_im = df_from_f64(h.minv.im);
-    const double az = h.azm * x;
-    const int nmx = (int)rint(fmax((double)nmax, az) + 16.0);
-    const cdf zinv = cdf{df_from_f64(h.zminv.re * xinv), df_from_f64(h.zminv.im * xinv)};
-    const df xi = df_from_f64(xinv);
+    const float4 hm = hd[0], hmi = hd[1], hz = hd[2];
+    const float azm = hd[3].x;
+    const df m_re = df{hm.x, hm.y}, m_im = df{hm.z, hm.w};
+    const df mi_re = df{hmi.x, hmi.y}, mi_im = df{hmi.z, hmi.w};
+    const float mfr = m_re.hi, mfi = m_im.hi, mifr = mi_re.hi, mifi = mi_im.hi;
+    const float az = azm * xf;
+    const int nmx = (int)rintf(fmaxf((float)nmax, az) + 16.0f);
+    const cdf zinv = cdf{df_mul(df{hz.x, hz.y}, xi), df_mul(df{hz.z, hz.w}, xi)};   // 1/z
     // Warm-up steps above nmax.  When |z| < nmax + 1 every step lies where
     // the recurrence damps the start error by (|z| / (2n+1))^2 per step, so
     // the steps are counted for a damping of e^-23 (1e-10; the FP64 path
     // asks for 1e-17); emulated for x in [1e-3, 650]: the same coefficients
     // to 2.2e-7 with 24% fewer steps on the sulfate-like table.
     int warm = nmx - 1 - nmax;
-    if (az < (double)(nmax + 1)) {
-        const float q = 2.f * logf((2.f * (float)(nmax + 1) + 1.f) / (float)az);
+    if (az < (float)(nmax + 1)) {
+        const float q = 2.f * logf((2.f * (float)(nmax + 1) + 1.f) / az);
         const int need = (int)ceilf(23.0f / q) + 2;
         if (need < warm) warm = need;
     }
@@ -165,16 +172,19 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
     cdf rk = cdf_mul_f(zinv, (float)(nmax + 1));   // r_nmax = (nmax+1)/z
     cdf w = cdf_add(D, rk);                         // D_{nmax+1} + r_nmax
     df iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
+    // psi_k, chi_k (pn) and psi_{k-1}, chi_{k-1} (pm); the row entry of the
+    // next order is loaded one order ahead (its latency overlaps an order's
+    // arithmetic)
     float4 pn = rowd[nmax - 1];
-    const df s0 = df_from_f64(sx), c0 = df_from_f64(cxv);   // psi_0 = sin x, chi_0 = cos x
+    float4 pm = nmax > 1 ? rowd[nmax - 2] : r0;
     for (int k = nmax; k >= 1; --k) {
+        const float4 pnext = k > 2 ? rowd[k - 3] : r0;
         D = cdf{df_fma(df_neg(w.re), iw, rk.re), df_fma(w.im, iw, rk.im)};   // D_k
         if (k > 1) {
             rk = cdf_mul_f(zinv, (float)k);   // r_{k-1} = k/z
             w = cdf_add(D, rk);
             iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
         }
-        const float4 pm = (k > 1) ? rowd[k - 2] : make_float4(s0.hi, s0.lo, c0.hi, c0.lo);
         const df nx = df_mul_f(xi, (float)k);   // k/x
         const df dar = df_fma(D.re, mi_re, df_fma(df_neg(D.im), mi_im, nx));   // Re(D/m) + k/x
         const df dbr = df_fma(D.re, m_re, df_fma(df_neg(D.im), m_im, nx));     // Re(D m) + k/x
@@ -189,6 +199,7 @@ __device__ __forceinline__ void homog_core_mixed(double x, double xinv, double s
         const float2 b = mie_ratio_f32(nbr, dbi * pn.x, mbr, dbi * pn.z, idb);
         emit(k, a, b, fmaf(dai, ida, dbi * idb));
         pn = pm;
+        pm = pnext;
     }
 }
 
@@ -363,9 +374,8 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     const int64_t o = v.off[row];
     const int nmax = (int)(v.off[row + 1] - o);
     const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
-    const double x = v.xg[row];
-    const double4 rc = v.rowc[row];
-    const HomogIndex h = v.hidx[unit];
+    const float4 rc0 = v.rowcd[2 * row], rc1 = v.rowcd[2 * row + 1];
+    const df xi = df{rc1.x, rc1.y};
     EmitMixed emit;
     emit.cf = cf + c;
     emit.amax = 0.f;
@@ -373,17 +383,23 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     emit.ab_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
     emit.pa = emit.pb = make_float2(0.f, 0.f);
     emit.inv_n1 = __frcp_rn((float)(nmax + 1));
-    homog_core_mixed(x, rc.z, rc.x, rc.y, h, v.pcd + o, nmax, emit);
-    const double iy2 = rc.z * rc.z;   // 1 / x^2
-    const double sca = (double)emit.sca - (double)emit.sca_c;
-    const double qsca = 2.0 * sca * iy2;
-    const double qext = qsca - 2.0 * ((double)emit.ab - (double)emit.ab_c) * iy2;
-    const double qr = (double)emit.qbr - (double)emit.qbr_c, qi = (double)emit.qbi - (double)emit.qbi_c;
+    homog_core_mixed(v.hdf + 4 * unit, rc0, xi, rc1.z, v.pcd + o, nmax, emit);
+    // efficiencies from the compensated sums (value = sum - compensation), in
+    // pairs; one FP64 addition per output
+    const df iy2 = df_mul(xi, xi);   // 1 / x^2
+    const df sca = df_two_sum(emit.sca, -emit.sca_c);
+    const df sca2 = df_mul(sca, iy2);
+    const df qsca = df{2.f * sca2.hi, 2.f * sca2.lo};
+    const df ab2 = df_mul(df_two_sum(emit.ab, -emit.ab_c), iy2);
+    const df qext = df_sub(qsca, df{2.f * ab2.hi, 2.f * ab2.lo});
+    const df qr = df_two_sum(emit.qbr, -emit.qbr_c), qi = df_two_sum(emit.qbi, -emit.qbi_c);
+    const df qbv = df_mul(df_fma(qr, qr, df_mul(qi, qi)), iy2);
+    const df asy = df_mul(df_two_sum(emit.asy, -emit.asy_c), df_rcp(sca));   // 4/x^2 asy / qsca, halved
     double *o4 = v.eff4 + t * 4;
-    o4[0] = qext;
-    o4[1] = qsca;
-    o4[2] = (qr * qr + qi * qi) * iy2;
-    o4[3] = 2.0 * ((double)emit.asy - (double)emit.asy_c) / sca;   // 4/x^2 asy / qsca
+    o4[0] = df_to_f64(qext);
+    o4[1] = df_to_f64(qsca);
+    o4[2] = df_to_f64(qbv);
+    o4[3] = df_to_f64(df{2.f * asy.hi, 2.f * asy.lo});
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
@@ -399,6 +415,32 @@ __global__ void k_rows_df(int64_t n, const double2 *__restrict__ src, float4 *__
         const double2 v = src[i];
         const df p = df_from_f64(v.x), c = df_from_f64(v.y);
         dst[i] = make_float4(p.hi, p.lo, c.hi, c.lo);
+    }
+}
+
+// Per-unit and per-row constants of the mixed recurrences as FP32 pairs:
+// hdf[4 u] = m, 1/m, x/z (1/z = (x/z)(1/x)), (|z|/x); rowcd[2 j] = (sin x, cos x),
+// (1/x, x).
+__global__ void k_mixed_consts(int64_t n_units, const HomogIndex *__restrict__ hidx, float4 *__restrict__ hdf,
+                               int64_t nrows, const double4 *__restrict__ rowc, const double *__restrict__ xg,
+                               float4 *__restrict__ rowcd)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_units) {
+        const HomogIndex h = hidx[i];
+        const df a = df_from_f64(h.m.re), b = df_from_f64(h.m.im);
+        const df c = df_from_f64(h.minv.re), d = df_from_f64(h.minv.im);
+        const df e = df_from_f64(h.zminv.re), f = df_from_f64(h.zminv.im);
+        hdf[4 * i] = make_float4(a.hi, a.lo, b.hi, b.lo);
+        hdf[4 * i + 1] = make_float4(c.hi, c.lo, d.hi, d.lo);
+        hdf[4 * i + 2] = make_float4(e.hi, e.lo, f.hi, f.lo);
+        hdf[4 * i + 3] = make_float4((float)h.azm, 0.f, 0.f, 0.f);
+    }
+    if (i < nrows) {
+        const double4 rc = rowc[i];
+        const df s = df_from_f64(rc.x), c = df_from_f64(rc.y), xi = df_from_f64(rc.z);
+        rowcd[2 * i] = make_float4(s.hi, s.lo, c.hi, c.lo);
+        rowcd[2 * i + 1] = make_float4(xi.hi, xi.lo, (float)xg[i], 0.f);
     }
 }
 
@@ -1173,6 +1215,14 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     ctx_pre_launch(ctx);
     k_rows_df<<<(unsigned)ceil_div64(p->pc_total, 256), 256, 0, st>>>(p->pc_total, v.pc, v.pcd);
     GBMIE_TRY(ctx_check_launch(ctx, "k_rows_df"));
+    {
+        const int64_t nrows = (int64_t)p->n_le * v.n_size;
+        const int64_t nc = nrows > p->n_units ? nrows : p->n_units;
+        ctx_pre_launch(ctx);
+        k_mixed_consts<<<(unsigned)ceil_div64(nc, 256), 256, 0, st>>>(p->n_units, v.hidx, v.hdf, nrows, v.rowc, v.xg,
+                                                                      v.rowcd);
+        GBMIE_TRY(ctx_check_launch(ctx, "k_mixed_consts"));
+    }
     ctx_pre_launch(ctx);
     k_fill_int<<<(unsigned)ceil_div64(p->n_units, 256), 256, 0, st>>>((int)p->n_units, eunit, -100000);
     GBMIE_TRY(ctx_check_launch(ctx, "k_fill_int"));

@@ -24,7 +24,7 @@ struct gbmie_table_plan {
     int nmax_max;
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
     // mixed precision (tensor-core) path
-    size_t o_cf, o_eexp, o_eunit, o_wf, o_tw, o_rowc, o_hidx, o_pcf, o_dscr;
+    size_t o_cf, o_eexp, o_eunit, o_wf, o_tw, o_rowc, o_hidx, o_pcf, o_dscr, o_hdf, o_rowcd;
     __half *bt;          // B operands of the contraction (plan-owned, built once at plan time)
     int n_pad_total;     // angles padded to whole 128-angle blocks (mixed path)
     int k_pad;           // orders padded to 32
@@ -106,6 +106,8 @@ struct TabView {
     HomogIndex *hidx;   // per unit: medium constants of the recurrences
     const double2 *pq;
     float4 *pcd;        // pc as FP32 pairs: psi hi, lo, chi hi, lo (mixed path)
+    float4 *hdf;        // per unit, FP32 pairs: m, 1/m, x/z, (|z|/x) (mixed path)
+    float4 *rowcd;      // per size row, FP32 pairs: (sin x, cos x), (1/x, x) (mixed path)
     // PSD weights, their radius moments and reff0 do not depend on the
     // wavelength when the grid is a radius grid and the PSD is analytic
     // (x = 2 pi r / lambda: the lognormal argument ln(x / x_mode) and the
