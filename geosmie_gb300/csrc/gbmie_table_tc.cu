@@ -28,6 +28,7 @@
 #include "table_internal.cuh"
 #include "tc.cuh"
 
+#define TC_KC16 16                      // orders per chunk (one MMA K step)
 #define TC_INST 64                      // sizes per tile
 #define TC_HALF 32                      // sizes per half tile (MMA N = 64: Re, Im)
 #define TC_ABLK 128                     // angles per block (MMA M)
@@ -215,7 +216,8 @@ __device__ __forceinline__ void homog_core_mixed(const float4 *__restrict__ hd, 
 // terms keep their relative precision, so qext, qsca and qabs = qext - qsca
 // all do, however weak or strong the absorption.
 struct EmitMixed {
-    float4 *cf;
+    float4 *cf;    // order k at cf[(k - 1) * cs]
+    int cs;
     float amax;
     float ab, sca, asy, qbr, qbi;
     float ab_c, sca_c, asy_c, qbr_c, qbi_c;   // Kahan compensations
@@ -223,7 +225,7 @@ struct EmitMixed {
     float inv_n1;                              // 1/(n+1)
     __device__ __forceinline__ void operator()(int k, float2 a, float2 b, float t) {
         const float4 q = make_float4(a.x + b.x, a.y + b.y, a.x - b.x, a.y - b.y);
-        cf[k - 1] = q;
+        cf[(k - 1) * cs] = q;
         amax = fmaxf(amax, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
         const float fk = (float)k;
         const float cn = 2.f * fk + 1.f;
@@ -265,18 +267,33 @@ struct EmitCf {
 // one instance (size i of its unit): FP32 (c, d) orders 1..nmax -> FP16
 // hi/lo scaled by 2^(13 - e_i), in every chunk of the instance's tile, zero
 // past nmax.  The coefficient kernels call it
-// once an instance is done: its coefficients are still in L2, and the
-// integer/FP32/LSU work hides under their FP64 recurrences.
-__device__ __forceinline__ void split_rows(const TabView &v, int64_t unit, int i, int ex, int nmax,
-                                           const float4 *__restrict__ cfi, const int *__restrict__ tile_cbase,
-                                           const int64_t *__restrict__ unit_cbase, int ntiles,
-                                           uint8_t *__restrict__ asplit)
+// once an instance is done: its coefficients are still in L2.  The chunk
+// bases of the tile (SplitIdx) are loaded when the instance starts, so their
+// latency overlaps the recurrences.
+struct SplitIdx {
+    int cb0, cb1;    // tile_cbase[tile], [tile + 1] of the instance's grid
+    long long ucb;   // unit_cbase[unit]
+};
+__device__ __forceinline__ SplitIdx split_idx(const TabView &v, int64_t unit, int i,
+                                              const int *__restrict__ tile_cbase,
+                                              const int64_t *__restrict__ unit_cbase, int ntiles)
 {
     const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
-    const int *tcb = tile_cbase + (size_t)v.le(lam) * (ntiles + 1);
+    const int *tcb = tile_cbase + (size_t)v.le(lam) * (ntiles + 1) + (i >> 6);
+    SplitIdx s;
+    s.cb0 = ldg_pin_s32(tcb);
+    s.cb1 = ldg_pin_s32(tcb + 1);
+    s.ucb = ldg_pin_s64(unit_cbase + unit);
+    return s;
+}
+// cfi[k * cstride]: order k + 1 (global memory, stride 1, or this thread's
+// column of the block's shared staging, stride blockDim)
+__device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int nmax, const float4 *cfi, int cstride,
+                                           const SplitIdx &si, uint8_t *__restrict__ asplit)
+{
     const int tile = i >> 6, ia = i & 63;
-    const int nc = tcb[tile + 1] - tcb[tile];
-    uint8_t *dst = asplit + (size_t)(unit_cbase[unit] + tcb[tile]) * 16384;
+    const int nc = si.cb1 - si.cb0;
+    uint8_t *dst = asplit + (size_t)(si.ucb + si.cb0) * 16384;
     const float sc = ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - ex)));
     const int hh = ia >> 5, r0 = 2 * (ia & 31), r1 = r0 + 1;
     for (int j = 0; j < nc; ++j)
@@ -287,7 +304,7 @@ __device__ __forceinline__ void split_rows(const TabView &v, int64_t unit, int i
             for (int jj = 0; jj < 8; ++jj) {
                 const int k = 16 * j + 8 * kg + jj;
                 float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (k < nmax) q = cfi[k];
+                if (k < nmax) q = cfi[k * cstride];
                 split_f16(q.x * sc, ch[0][jj], cl[0][jj]);
                 split_f16(q.y * sc, ch[1][jj], cl[1][jj]);
                 split_f16(q.z * sc, ch[2][jj], cl[2][jj]);
@@ -355,7 +372,7 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int6
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
-    split_rows(v, unit, i, ex, nmax, cf + c, tile_cbase, unit_cbase, ntiles, asplit);
+    split_rows(v, i, ex, nmax, cf + c, 1, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
 }
 
 __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
@@ -376,8 +393,14 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
     const float4 rc0 = v.rowcd[2 * row], rc1 = v.rowcd[2 * row + 1];
     const df xi = df{rc1.x, rc1.y};
+    // an instance of one 16-order chunk keeps its coefficients in this
+    // thread's column of the block's shared staging until split_rows reads
+    // them (no global round trip); longer ones go through cf
+    extern __shared__ float4 cf_stage[];
+    const bool staged = nmax <= TC_KC16;
     EmitMixed emit;
-    emit.cf = cf + c;
+    emit.cf = staged ? cf_stage + threadIdx.x : cf + c;
+    emit.cs = staged ? (int)blockDim.x : 1;
     emit.amax = 0.f;
     emit.ab = emit.sca = emit.asy = emit.qbr = emit.qbi = 0.f;
     emit.ab_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
@@ -403,7 +426,7 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
-    split_rows(v, unit, i, ex, nmax, cf + c, tile_cbase, unit_cbase, ntiles, asplit);
+    split_rows(v, i, ex, nmax, emit.cf, emit.cs, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
 }
 
 // The psi/chi rows as FP32 pairs (psi hi, lo, chi hi, lo) for the mixed
@@ -563,7 +586,6 @@ struct TcArgs {
     int *flags;
 };
 
-#define TC_KC16 16                                     // orders per chunk (one MMA K step)
 #define TC_NS 4                                        // ring stages
 #define TC_WIN_MAX TC_NS                               // longest accumulation window (chunks)
 #define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
@@ -1205,6 +1227,22 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
 // ---------------------------------------------------------------------------
 // host launchers (called from gbmie_table_run)
 // ---------------------------------------------------------------------------
+// shared staging of k_tab_coeffs_mixed: 16 orders x float4 per thread
+static size_t coef_stage_bytes(int block) { return (size_t)TC_KC16 * sizeof(float4) * (size_t)block; }
+// the attribute is set once per device, on the first (uncaptured) run: a
+// table run may be recorded into a CUDA graph later
+static int coef_stage_attr(gbmie_ctx *ctx)
+{
+    static volatile bool done[64];
+    const int dev = ctx->device;
+    if (dev >= 0 && dev < 64 && done[dev]) return GBMIE_OK;
+    const int st = ctx_cuda(ctx, cudaFuncSetAttribute(k_tab_coeffs_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)coef_stage_bytes(256)),
+                            "k_tab_coeffs_mixed shared memory");
+    if (st == GBMIE_OK && dev >= 0 && dev < 64) done[dev] = true;
+    return st;
+}
+
 int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr)
 {
     const gbmie_table_desc &d = p->d;
@@ -1233,8 +1271,10 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
             v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed_coated"));
     } else {
-        k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, p->coef_block), p->coef_block, 0, st>>>(
-            v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
+        GBMIE_TRY(coef_stage_attr(ctx));
+        k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, p->coef_block), p->coef_block,
+                             coef_stage_bytes(p->coef_block), st>>>(v, p->n_inst, cf, eexp, eunit, ctx->d_flags,
+                                                                   p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
     }
     TcArgs a;
@@ -1279,6 +1319,7 @@ size_t table_mixed_smem_bytes() { return TC_SMEM_BYTES(8); }
 // per plan into plan-owned memory (plan creation synchronises afterwards).
 int build_table_bt(gbmie_ctx *ctx, gbmie_table_plan *p)
 {
+    GBMIE_TRY(coef_stage_attr(ctx));   // at plan time: never inside a graph capture
     const size_t bytes = 4 * 2 * (size_t)p->n_pad_total * p->k_pad;
     GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&p->bt, bytes), "B operand tables"));
     ctx_pre_launch(ctx);
@@ -1307,7 +1348,7 @@ int tune_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr,
             for (int rep = 0; rep < 2; ++rep) {
                 const int bs = blocks[c];
                 cudaEventRecord(e0, st);
-                k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, bs), bs, 0, st>>>(
+                k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, bs), bs, coef_stage_bytes(bs), st>>>(
                     v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles,
                     (uint8_t *)(scr + p->o_asplit));
                 cudaEventRecord(e1, st);

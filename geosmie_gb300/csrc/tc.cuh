@@ -259,6 +259,12 @@ __device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float *a, 
     }
 }
 
+// A global line into L1 (no register written, nothing waits for it).
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // Read-only global loads issued where they stand (volatile asm keeps the
 // compiler from sinking a prefetch next to its use); the value is consumed
 // later, so the load's latency overlaps the work in between.
