@@ -110,7 +110,23 @@ struct gbmie_ctx {
         int32_t params[13];
     } tune_cache[16];
     int n_tune;
+    // angle-function operands of mixed table plans (they depend only on the
+    // angles and the largest nmax): shared by plans with the same key,
+    // reference-counted, freed when evicted unused or with the context
+    struct AngleOp {
+        void *bt;
+        int n_ang, n_pad, k_pad, nmax;
+        double *hcos;   // host copy of the key's cos(theta)
+        int refs;
+    } angle_ops[4];
 };
+
+// Angle-function operand for (cos theta on the host, sizes): a cached one
+// or a fresh cache entry the caller fills; *entry is its index (release it
+// with ctx_angle_op_release).  *fresh = 1 when the caller must build it.
+int ctx_angle_op_get(gbmie_ctx *ctx, const double *hcos, int n_ang, int n_pad, int k_pad, int nmax, size_t bytes,
+                     void **bt, int *entry, int *fresh);
+void ctx_angle_op_release(gbmie_ctx *ctx, int entry);
 
 int ctx_fail(gbmie_ctx *ctx, int status, const char *fmt, ...);
 int ctx_cuda(gbmie_ctx *ctx, cudaError_t e, const char *what);

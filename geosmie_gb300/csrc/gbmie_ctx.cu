@@ -69,6 +69,65 @@ int ctx_scratch(gbmie_ctx *ctx, size_t bytes, void **ptr)
     return GBMIE_OK;
 }
 
+int ctx_angle_op_get(gbmie_ctx *ctx, const double *hcos, int n_ang, int n_pad, int k_pad, int nmax, size_t bytes,
+                     void **bt, int *entry, int *fresh)
+{
+    *bt = nullptr;
+    *entry = -1;
+    *fresh = 0;
+    const int cap = (int)(sizeof(ctx->angle_ops) / sizeof(ctx->angle_ops[0]));
+    for (int i = 0; i < cap; ++i) {
+        gbmie_ctx::AngleOp &e = ctx->angle_ops[i];
+        if (e.bt && e.n_ang == n_ang && e.n_pad == n_pad && e.k_pad == k_pad && e.nmax == nmax &&
+            memcmp(e.hcos, hcos, sizeof(double) * n_ang) == 0) {
+            ++e.refs;
+            *bt = e.bt;
+            *entry = i;
+            return GBMIE_OK;
+        }
+    }
+    // a free slot, else an unused entry is evicted
+    int slot = -1;
+    for (int i = 0; i < cap && slot < 0; ++i)
+        if (!ctx->angle_ops[i].bt) slot = i;
+    for (int i = 0; i < cap && slot < 0; ++i)
+        if (ctx->angle_ops[i].refs == 0) {
+            cudaFree(ctx->angle_ops[i].bt);
+            free(ctx->angle_ops[i].hcos);
+            ctx->angle_ops[i].bt = nullptr;
+            slot = i;
+        }
+    void *mem = nullptr;
+    GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&mem, bytes), "angle-function operand"));
+    if (slot < 0) {   // every entry in use: a plan-owned operand outside the cache
+        *bt = mem;
+        *fresh = 1;
+        return GBMIE_OK;
+    }
+    gbmie_ctx::AngleOp &e = ctx->angle_ops[slot];
+    e.hcos = (double *)malloc(sizeof(double) * n_ang);
+    if (!e.hcos) {
+        cudaFree(mem);
+        return GBMIE_ERR_NOMEM;
+    }
+    memcpy(e.hcos, hcos, sizeof(double) * n_ang);
+    e.bt = mem;
+    e.n_ang = n_ang;
+    e.n_pad = n_pad;
+    e.k_pad = k_pad;
+    e.nmax = nmax;
+    e.refs = 1;
+    *bt = mem;
+    *entry = slot;
+    *fresh = 1;
+    return GBMIE_OK;
+}
+
+void ctx_angle_op_release(gbmie_ctx *ctx, int entry)
+{
+    if (entry >= 0 && ctx->angle_ops[entry].refs > 0) --ctx->angle_ops[entry].refs;
+}
+
 extern "C" {
 
 const char *gbmie_status_string(int status)
@@ -120,6 +179,10 @@ int gbmie_ctx_destroy(gbmie_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     else cudaDeviceSynchronize();
     if (ctx->scratch) cudaFree(ctx->scratch);
+    for (auto &e : ctx->angle_ops) {
+        if (e.bt) cudaFree(e.bt);
+        free(e.hcos);
+    }
     if (ctx->timers) {
         for (int i = 0; i < GBMIE_TIMER_CAP; ++i)
             if (ctx->timers[i].start) {

@@ -586,7 +586,11 @@ static void plan_free(gbmie_table_plan *p)
     if (p->unit_base) cudaFree(p->unit_base);
     if (p->unit_order) cudaFree(p->unit_order);
     if (p->tile_cbase) cudaFree(p->tile_cbase);
-    if (p->bt) cudaFree(p->bt);
+    if (p->bt) {
+        if (p->bt_entry >= 0) ctx_angle_op_release(p->ctx, p->bt_entry);
+        else cudaFree(p->bt);
+    }
+    free(p->hcos);
     if (p->brange) cudaFree(p->brange);
     if (p->unit_cbase) cudaFree(p->unit_cbase);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
@@ -661,6 +665,14 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     if (st == GBMIE_OK)
         st = ctx_cuda(ctx, cudaMemcpy(hoff, p->off, sizeof(int64_t) * (nrows + 1), cudaMemcpyDeviceToHost),
                       "plan offsets copy");
+    p->bt_entry = -1;
+    if (st == GBMIE_OK && d.precision == GBMIE_MIXED) {   // the key of the angle-function operand
+        p->hcos = (double *)malloc(sizeof(double) * d.n_ang);
+        if (!p->hcos) st = GBMIE_ERR_NOMEM;
+        else
+            st = ctx_cuda(ctx, cudaMemcpy(p->hcos, d.cos_theta, sizeof(double) * d.n_ang, cudaMemcpyDeviceToHost),
+                          "plan angles copy");
+    }
     if (st == GBMIE_OK) {
         p->pc_total = total;
         int nm = 2;
@@ -835,6 +847,8 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         st = ctx_scratch(ctx, p->bytes, &scr);
     }
     if (st == GBMIE_OK && d.precision == GBMIE_MIXED) st = build_table_bt(ctx, p);
+    free(p->hcos);
+    p->hcos = nullptr;
     if (st == GBMIE_OK) table_tune_lookup(ctx, p);
     if (st == GBMIE_OK && d.n_gsf > 0) {
         st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf,

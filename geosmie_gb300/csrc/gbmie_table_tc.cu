@@ -1321,11 +1321,18 @@ int build_table_bt(gbmie_ctx *ctx, gbmie_table_plan *p)
 {
     GBMIE_TRY(coef_stage_attr(ctx));   // at plan time: never inside a graph capture
     const size_t bytes = 4 * 2 * (size_t)p->n_pad_total * p->k_pad;
-    GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&p->bt, bytes), "B operand tables"));
+    void *mem = nullptr;
+    int fresh = 0;
+    GBMIE_TRY(ctx_angle_op_get(ctx, p->hcos, p->d.n_ang, p->n_pad_total, p->k_pad, p->nmax_max, bytes, &mem,
+                               &p->bt_entry, &fresh));
+    p->bt = (__half *)mem;
+    if (!fresh) return GBMIE_OK;   // the same angles and orders: the cached operand
     ctx_pre_launch(ctx);
     k_tab_bt_f16<<<(p->n_pad_total + 127) / 128, 128, 0, ctx->stream>>>(p->d.n_ang, p->n_pad_total, p->k_pad,
                                                                          p->nmax_max, p->d.cos_theta, p->bt);
-    return ctx_check_launch(ctx, "k_tab_bt_f16");
+    const int st = ctx_check_launch(ctx, "k_tab_bt_f16");
+    if (st != GBMIE_OK && p->bt_entry >= 0) ctx->angle_ops[p->bt_entry].n_ang = -1;   // never matched again
+    return st;
 }
 
 // Autotuning of the mixed path on the plan's own data (after one full run

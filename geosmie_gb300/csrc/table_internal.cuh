@@ -25,7 +25,9 @@ struct gbmie_table_plan {
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
     // mixed precision (tensor-core) path
     size_t o_cf, o_eexp, o_eunit, o_wf, o_tw, o_rowc, o_hidx, o_pcf, o_dscr, o_hdf, o_rowcd;
-    __half *bt;          // B operands of the contraction (plan-owned, built once at plan time)
+    __half *bt;          // angle-function operand of the contraction (built once per key, see ctx angle_ops)
+    int bt_entry;        // its context cache entry, or -1 when plan-owned
+    double *hcos;        // host copy of cos(theta) (plan creation only)
     int n_pad_total;     // angles padded to whole 128-angle blocks (mixed path)
     int k_pad;           // orders padded to 32
     int *unit_order;     // [n_units] units by decreasing work (plan-owned)

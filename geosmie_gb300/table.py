@@ -86,24 +86,38 @@ class TablePlan(object):
         ns = len(spec["grid"])
         f64 = torch.float64
 
-        def d(a, dt=f64):
-            return torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dv)
-
-        self.t = {
-            "lambda": d(lam), "grid": d(spec["grid"]), "dgrid": d(spec["dgrid"]),
-            "m": d(m, torch.complex128), "frac": d(frac), "rhop": d(spec["rhop"]),
-            "rhop0": d(spec["rhop0"]), "gf": d(spec["gf"]), "rlow": d(spec["rlow"]), "rup": d(spec["rup"]),
-            "cos_theta": d(np.cos(theta)), "theta": d(theta),
+        # every input array in one page-locked staging block (256-byte aligned
+        # parts) and one host -> device copy
+        arrays = {
+            "lambda": lam, "grid": spec["grid"], "dgrid": spec["dgrid"], "m": m, "frac": frac,
+            "rhop": spec["rhop"], "rhop0": spec["rhop0"], "gf": spec["gf"], "rlow": spec["rlow"],
+            "rup": spec["rup"], "cos_theta": np.cos(theta), "theta": theta,
         }
         if spec.get("m_core") is not None:   # coated spheres: core index per unit, core/outer size per RH
-            self.t["m_core"] = d(np.asarray(spec["m_core"], np.complex128).reshape(m.shape), torch.complex128)
-            self.t["core_ratio"] = d(np.asarray(spec["core_ratio"], np.float64))
+            arrays["m_core"] = np.asarray(spec["m_core"], np.complex128).reshape(m.shape)
+            arrays["core_ratio"] = spec["core_ratio"]
         psd_kind = int(spec["psd_kind"])
         if psd_kind == PSD_WEIGHTS:
-            self.t["weights"] = d(spec["weights"])
+            arrays["weights"] = spec["weights"]
         else:
-            self.t["psd_param"] = d(spec["psd_param"])
-            self.t["gf_psd"] = d(spec["gf_psd"])
+            arrays["psd_param"] = spec["psd_param"]
+            arrays["gf_psd"] = spec["gf_psd"]
+        parts, off = {}, 0
+        for k, a in arrays.items():
+            a = np.ascontiguousarray(a, np.complex128 if k in ("m", "m_core") else np.float64)
+            parts[k] = (off, a)
+            off += (a.nbytes + 255) // 256 * 256
+        host = torch.empty(max(off, 256), dtype=torch.uint8, pin_memory=True)
+        hv = host.numpy()
+        for k, (o, a) in parts.items():
+            hv[o:o + a.nbytes] = a.reshape(-1).view(np.uint8)
+        self._inputs = torch.empty(host.shape, dtype=torch.uint8, device=dv)
+        self._inputs.copy_(host, non_blocking=True)
+        torch.cuda.current_stream(dv).synchronize()   # the plan's kernels run on the context's stream
+        self.t = {}
+        for k, (o, a) in parts.items():
+            dt = torch.complex128 if a.dtype == np.complex128 else f64
+            self.t[k] = self._inputs[o:o + a.nbytes].view(dt).view(a.shape)
         desc = _Desc()
         desc.n_lambda, desc.n_rh, desc.n_size, desc.n_bin, desc.n_comp = nl, nrh, ns, nbin, ncomp
         desc.n_ang = ang.size
@@ -132,14 +146,17 @@ class TablePlan(object):
         self.h = h
         self.scratch_bytes = nbytes.value
         ne = nbin * nl * nrh
-        self.out_t = {
-            "phase": torch.empty((nbin, nl, nrh, 6, ang.size), dtype=f64, device=dv),
-            "pback": torch.empty((nbin, nl, nrh, 6), dtype=f64, device=dv),
-            "scalar": torch.empty((nbin, nl, nrh, _native.NSCALAR), dtype=f64, device=dv),
-            "nl": torch.empty((nbin, nl, nrh, _native.NNL), dtype=f64, device=dv),
-        }
+        # all outputs in one device block (one device -> host copy in results())
+        shapes = {"phase": (nbin, nl, nrh, 6, ang.size), "pback": (nbin, nl, nrh, 6),
+                  "scalar": (nbin, nl, nrh, _native.NSCALAR), "nl": (nbin, nl, nrh, _native.NNL)}
         if n_gsf:
-            self.out_t["pmom"] = torch.empty((nbin, nl, nrh, 6, n_gsf), dtype=f64, device=dv)
+            shapes["pmom"] = (nbin, nl, nrh, 6, n_gsf)
+        self._out_off, n = {}, 0
+        for k, shp in shapes.items():
+            self._out_off[k] = (n, shp)
+            n += (int(np.prod(shp)) + 31) // 32 * 32   # 256-byte aligned parts
+        self._out_block = torch.empty(n, dtype=f64, device=dv)
+        self.out_t = {k: self._out_block[o:o + int(np.prod(shp))].view(shp) for k, (o, shp) in self._out_off.items()}
         out = _Out()
         for k, v in self.out_t.items():
             setattr(out, k, v.data_ptr())
@@ -188,15 +205,16 @@ class TablePlan(object):
         nrh] (per wavelength), pmom [nbin, nl, nrh, 6, n_gsf] (p order P11
         P12 P33 P34 P22 P44, i.e. alpha1 beta1 alpha3 beta2 alpha2 alpha4)."""
         self.sync()
-        # device -> page-locked host buffers (about 5x the bandwidth of
-        # pageable copies for the 130 MB sulfate table); fresh buffers per
-        # call, so earlier results stay valid (torch caches page-locked blocks)
-        host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in self.out_t.items()}
+        # the output block -> a page-locked host block in one copy (about 5x
+        # the bandwidth of pageable copies for the 130 MB sulfate table); a
+        # fresh block per call, so earlier results stay valid (torch caches
+        # page-locked blocks)
+        hb = torch.empty(self._out_block.shape, dtype=self._out_block.dtype, pin_memory=True)
         cs = torch.cuda.current_stream(self.ctx.device)
         with torch.cuda.stream(cs):
-            for k, v in self.out_t.items():
-                host[k].copy_(v, non_blocking=True)
+            hb.copy_(self._out_block, non_blocking=True)
         cs.synchronize()
+        host = {k: hb[o:o + int(np.prod(shp))].view(shp) for k, (o, shp) in self._out_off.items()}
         ph = host["phase"].numpy()
         sc = host["scalar"].numpy()
         nlv = host["nl"].numpy()
