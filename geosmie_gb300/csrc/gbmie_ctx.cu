@@ -52,7 +52,8 @@ int ctx_scratch(gbmie_ctx *ctx, size_t bytes, void **ptr)
 {
     if (bytes == 0) bytes = 256;
     if (bytes > ctx->scratch_bytes) {
-        GBMIE_TRY(ctx_cuda(ctx, cudaStreamSynchronize(ctx->stream), "scratch sync"));
+        // the scratch block may be in use on any stream the context was bound to
+        GBMIE_TRY(ctx_cuda(ctx, cudaDeviceSynchronize(), "scratch sync"));
         if (ctx->scratch) cudaFree(ctx->scratch);
         ctx->scratch = NULL;
         ctx->scratch_bytes = 0;
@@ -167,6 +168,17 @@ int gbmie_ctx_create(int device, gbmie_ctx **out)
         return GBMIE_ERR_NOMEM;
     }
     cudaMemset(ctx->d_flags, 0, 64);
+    // plan arrays are stream-ordered allocations from the device's default
+    // pool: keep freed blocks in the pool (the default threshold returns them
+    // to the driver at every synchronisation) so that plan creation reuses
+    // them; a process-level attribute of the pool, no device setting
+    {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     cudaDeviceSynchronize();
     *out = ctx;
     return GBMIE_OK;

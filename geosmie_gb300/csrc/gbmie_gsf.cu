@@ -197,7 +197,7 @@ int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, Gs
     t->L = L;
     t->nang = nang;
     const size_t bytes = sizeof(double) * (2 * (size_t)ng + 4 * (size_t)ng * L + ng) + sizeof(int) * ng;
-    GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&t->mem, bytes), "gsf tables"));
+    GBMIE_TRY(ctx_cuda(ctx, cudaMallocAsync(&t->mem, bytes, ctx->stream), "gsf tables"));
     char *p = (char *)t->mem;
     t->z = (double *)p; p += sizeof(double) * ng;
     t->w = (double *)p; p += sizeof(double) * ng;
@@ -218,11 +218,11 @@ int gsf_prepare(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, Gs
     return GBMIE_OK;
 }
 
-void gsf_release(GsfTables *t)
+void gsf_release(GsfTables *t, cudaStream_t s)
 {
-    if (t->mem) cudaFree(t->mem);
+    if (t->mem) cudaFreeAsync(t->mem, s);
     t->mem = nullptr;
-    if (t->tc.mem) cudaFree(t->tc.mem);
+    if (t->tc.mem) cudaFreeAsync(t->tc.mem, s);
     t->tc.mem = nullptr;
 }
 
@@ -276,6 +276,6 @@ extern "C" int gbmie_gsf(gbmie_ctx *ctx, int32_t ntab, int32_t nang, const doubl
     int st = launch_gsf_expand(ctx, &t, ntab, F, (int64_t)6 * nang, nang, map, coef, (int64_t)6 * nnodes, nnodes,
                                cnorm, precision);
     cudaStreamSynchronize(ctx->stream);
-    gsf_release(&t);
+    gsf_release(&t, ctx->stream);
     return st;
 }

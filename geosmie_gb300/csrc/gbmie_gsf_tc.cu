@@ -394,7 +394,7 @@ int gsf_tc_prepare(gbmie_ctx *ctx, GsfTables *t, int ntab_max)
     const size_t c_bytes = sizeof(double) * 4 * (size_t)b.rows_cap * b.lpad;
     const size_t e_bytes = sizeof(int) * 4 * (size_t)b.rows_cap;
     const size_t total = align_up(bt_bytes, 256) + align_up(a_bytes, 256) + align_up(c_bytes, 256) + e_bytes;
-    GBMIE_TRY(ctx_cuda(ctx, cudaMalloc(&t->tc.mem, total), "gsf tensor-core buffers"));
+    GBMIE_TRY(ctx_cuda(ctx, cudaMallocAsync(&t->tc.mem, total, ctx->stream), "gsf tensor-core buffers"));
     char *p = (char *)t->tc.mem;
     t->tc.bt = (__half *)p;
     p += align_up(bt_bytes, 256);

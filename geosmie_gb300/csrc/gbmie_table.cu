@@ -578,24 +578,28 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     return v;
 }
 
+// The plan's device arrays are stream-ordered allocations, freed in order on
+// the context's stream after its last use there: destroying a plan neither
+// waits for the device nor stalls work in flight on other streams.
 static void plan_free(gbmie_table_plan *p)
 {
     if (!p) return;
-    if (p->xg) cudaFree(p->xg);
-    if (p->off) cudaFree(p->off);
-    if (p->unit_base) cudaFree(p->unit_base);
-    if (p->unit_order) cudaFree(p->unit_order);
-    if (p->tile_cbase) cudaFree(p->tile_cbase);
+    cudaStream_t s = p->ctx->stream;
+    if (p->xg) cudaFreeAsync(p->xg, s);
+    if (p->off) cudaFreeAsync(p->off, s);
+    if (p->unit_base) cudaFreeAsync(p->unit_base, s);
+    if (p->unit_order) cudaFreeAsync(p->unit_order, s);
+    if (p->tile_cbase) cudaFreeAsync(p->tile_cbase, s);
     if (p->bt) {
         if (p->bt_entry >= 0) ctx_angle_op_release(p->ctx, p->bt_entry);
         else cudaFree(p->bt);
     }
     free(p->hcos);
-    if (p->brange) cudaFree(p->brange);
-    if (p->unit_cbase) cudaFree(p->unit_cbase);
+    if (p->brange) cudaFreeAsync(p->brange, s);
+    if (p->unit_cbase) cudaFreeAsync(p->unit_cbase, s);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
-    gsf_release(&p->gsf);
+    gsf_release(&p->gsf, s);
     free(p);
 }
 
@@ -603,7 +607,8 @@ extern "C" int gbmie_table_plan_destroy(gbmie_table_plan *plan)
 {
     if (plan) {
         cudaSetDevice(plan->ctx->device);
-        cudaStreamSynchronize(plan->ctx->stream);
+        // a captured graph is destroyed only once no replay is in flight
+        if (plan->gexec) cudaStreamSynchronize(plan->ctx->stream);
     }
     plan_free(plan);
     return GBMIE_OK;
@@ -644,10 +649,10 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     p->n_inst = p->n_units * d.n_size;
     p->n_entries = (int64_t)d.n_lambda * d.n_rh * d.n_bin;
     const int64_t nrows = (int64_t)p->n_le * d.n_size;
-    int st = ctx_cuda(ctx, cudaMalloc(&p->xg, sizeof(double) * nrows), "plan x grid");
-    if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMalloc(&p->off, sizeof(int64_t) * (nrows + 1)), "plan offsets");
+    int st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->xg, sizeof(double) * nrows, ctx->stream), "plan x grid");
+    if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->off, sizeof(int64_t) * (nrows + 1), ctx->stream), "plan offsets");
     if (st == GBMIE_OK)
-        st = ctx_cuda(ctx, cudaMalloc(&p->unit_base, sizeof(int64_t) * p->n_units), "plan unit base");
+        st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->unit_base, sizeof(int64_t) * p->n_units, ctx->stream), "plan unit base");
     if (st == GBMIE_OK) {
         ctx_pre_launch(ctx);
         k_tab_make_x<<<(unsigned)ceil_div64(nrows, 256), 256, 0, ctx->stream>>>(p->n_le, d.n_size, d.grid_kind,
@@ -663,16 +668,17 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         if (!hoff) st = GBMIE_ERR_NOMEM;
     }
     if (st == GBMIE_OK)
-        st = ctx_cuda(ctx, cudaMemcpy(hoff, p->off, sizeof(int64_t) * (nrows + 1), cudaMemcpyDeviceToHost),
+        st = ctx_cuda(ctx, cudaMemcpyAsync(hoff, p->off, sizeof(int64_t) * (nrows + 1), cudaMemcpyDeviceToHost, ctx->stream),
                       "plan offsets copy");
     p->bt_entry = -1;
     if (st == GBMIE_OK && d.precision == GBMIE_MIXED) {   // the key of the angle-function operand
         p->hcos = (double *)malloc(sizeof(double) * d.n_ang);
         if (!p->hcos) st = GBMIE_ERR_NOMEM;
         else
-            st = ctx_cuda(ctx, cudaMemcpy(p->hcos, d.cos_theta, sizeof(double) * d.n_ang, cudaMemcpyDeviceToHost),
+            st = ctx_cuda(ctx, cudaMemcpyAsync(p->hcos, d.cos_theta, sizeof(double) * d.n_ang, cudaMemcpyDeviceToHost, ctx->stream),
                           "plan angles copy");
     }
+    if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaStreamSynchronize(ctx->stream), "plan offsets sync");
     if (st == GBMIE_OK) {
         p->pc_total = total;
         int nm = 2;
@@ -745,26 +751,26 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
             }
             p->n_chunks = nch;
             if (st == GBMIE_OK)
-                st = ctx_cuda(ctx, cudaMalloc(&p->tile_cbase, sizeof(int) * (size_t)p->n_le * ntp), "tile chunks");
+                st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->tile_cbase, sizeof(int) * (size_t)p->n_le * ntp, ctx->stream), "tile chunks");
             if (st == GBMIE_OK)
-                st = ctx_cuda(ctx, cudaMalloc(&p->unit_cbase, sizeof(int64_t) * p->n_units), "unit chunks");
+                st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->unit_cbase, sizeof(int64_t) * p->n_units, ctx->stream), "unit chunks");
             if (st == GBMIE_OK)
-                st = ctx_cuda(ctx, cudaMemcpy(p->tile_cbase, tcb, sizeof(int) * (size_t)p->n_le * ntp,
-                                              cudaMemcpyHostToDevice), "tile chunks copy");
+                st = ctx_cuda(ctx, cudaMemcpyAsync(p->tile_cbase, tcb, sizeof(int) * (size_t)p->n_le * ntp,
+                                              cudaMemcpyHostToDevice, ctx->stream), "tile chunks copy");
             if (st == GBMIE_OK)
-                st = ctx_cuda(ctx, cudaMemcpy(p->unit_cbase, ucb, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice),
+                st = ctx_cuda(ctx, cudaMemcpyAsync(p->unit_cbase, ucb, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice, ctx->stream),
                               "unit chunks copy");
             free(tcb);
             free(ucb);
-            if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMalloc(&p->unit_order, sizeof(int) * p->n_units), "unit order");
+            if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->unit_order, sizeof(int) * p->n_units, ctx->stream), "unit order");
             if (st == GBMIE_OK)
-                st = ctx_cuda(ctx, cudaMemcpy(p->unit_order, ord, sizeof(int) * p->n_units, cudaMemcpyHostToDevice),
+                st = ctx_cuda(ctx, cudaMemcpyAsync(p->unit_order, ord, sizeof(int) * p->n_units, cudaMemcpyHostToDevice, ctx->stream),
                               "unit order copy");
             free(cost);
             free(ord);
         }
         if (ub) {
-            st = ctx_cuda(ctx, cudaMemcpy(p->unit_base, ub, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice),
+            st = ctx_cuda(ctx, cudaMemcpyAsync(p->unit_base, ub, sizeof(int64_t) * p->n_units, cudaMemcpyHostToDevice, ctx->stream),
                           "plan unit base copy");
             free(ub);
         }
@@ -795,9 +801,9 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         }
         p->bmaxlen[GBMIE_TUNE_BUCKETS] = d.n_size;
         if (st == GBMIE_OK)
-            st = ctx_cuda(ctx, cudaMalloc(&p->brange, sizeof(int2) * nb1 * (size_t)p->n_le), "bucket ranges");
+            st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->brange, sizeof(int2) * nb1 * (size_t)p->n_le, ctx->stream), "bucket ranges");
         if (st == GBMIE_OK)
-            st = ctx_cuda(ctx, cudaMemcpy(p->brange, hb, sizeof(int2) * nb1 * (size_t)p->n_le, cudaMemcpyHostToDevice),
+            st = ctx_cuda(ctx, cudaMemcpyAsync(p->brange, hb, sizeof(int2) * nb1 * (size_t)p->n_le, cudaMemcpyHostToDevice, ctx->stream),
                           "bucket ranges copy");
         free(hb);
         const int thr = d.n_ang >= 256 ? 256 : ((d.n_ang + 31) / 32) * 32;

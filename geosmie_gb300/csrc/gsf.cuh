@@ -46,7 +46,8 @@ int gsf_tc_prepare(gbmie_ctx *ctx, GsfTables *t, int ntab_max);
 int launch_gsf_expand_tc(gbmie_ctx *ctx, const GsfTables *t, int ntab, const double *F, int64_t entry_stride,
                          int64_t row_stride, GsfMap map, double *coef, int64_t out_stride, int64_t out_row_stride,
                          double *cnorm);
-void gsf_release(GsfTables *t);
+// stream-ordered free of the tables on s (after their last use there)
+void gsf_release(GsfTables *t, cudaStream_t s);
 // precision: GBMIE_PLAIN_FP64 (FP64 sums) or GBMIE_MIXED (split-FP16
 // tensor-core GEMMs, gbmie_gsf_tc.cu)
 int launch_gsf_expand(gbmie_ctx *ctx, const GsfTables *t, int ntab, const double *F, int64_t entry_stride,

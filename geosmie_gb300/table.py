@@ -73,9 +73,14 @@ class TablePlan(object):
     synchronisation, capturable in a CUDA graph).
     """
 
-    def __init__(self, spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=0, device=0, n_gsf_nodes=0):
+    def __init__(self, spec, precision=_native.GBMIE_PLAIN_FP64, n_gsf=0, device=0, n_gsf_nodes=0,
+                 setup_stream=None):
+        """setup_stream: a torch CUDA stream for the plan's own setup (input
+        copy, layout kernels, operand tables), so that creating a plan does not
+        wait for tables in flight on the caller's stream (run_tables)."""
         self.ctx = _native.context(device)
         dv = self.ctx.device
+        self._run_stream = None
         ang = np.asarray(spec["ang"], np.float64)
         theta = np.radians(ang)
         lam = np.asarray(spec["lambda"], np.float64)
@@ -111,9 +116,11 @@ class TablePlan(object):
         hv = host.numpy()
         for k, (o, a) in parts.items():
             hv[o:o + a.nbytes] = a.reshape(-1).view(np.uint8)
-        self._inputs = torch.empty(host.shape, dtype=torch.uint8, device=dv)
-        self._inputs.copy_(host, non_blocking=True)
-        torch.cuda.current_stream(dv).synchronize()   # the plan's kernels run on the context's stream
+        setup = setup_stream if setup_stream is not None else torch.cuda.current_stream(dv)
+        with torch.cuda.stream(setup):
+            self._inputs = torch.empty(host.shape, dtype=torch.uint8, device=dv)
+            self._inputs.copy_(host, non_blocking=True)
+        setup.synchronize()   # the plan's kernels run on the context's stream
         self.t = {}
         for k, (o, a) in parts.items():
             dt = torch.complex128 if a.dtype == np.complex128 else f64
@@ -142,7 +149,8 @@ class TablePlan(object):
         self.n_gsf = int(n_gsf)
         h = ctypes.c_void_p()
         nbytes = ctypes.c_int64()
-        self.ctx.call("gbmie_table_plan_create", ctypes.byref(desc), ctypes.byref(h), ctypes.byref(nbytes))
+        with torch.cuda.stream(setup):   # synchronises the setup stream only
+            self.ctx.call("gbmie_table_plan_create", ctypes.byref(desc), ctypes.byref(h), ctypes.byref(nbytes))
         self.h = h
         self.scratch_bytes = nbytes.value
         ne = nbin * nl * nrh
@@ -168,7 +176,13 @@ class TablePlan(object):
         """Launch the table pipeline on the context stream.  graph=True
         replays it as one CUDA graph (captured on the first such call,
         gbmie_table_run_graph)."""
+        rs = torch.cuda.current_stream(self.ctx.device)
+        if self._run_stream is None or rs != self._run_stream:
+            self._inputs.record_stream(rs)   # the inputs may come from another (setup) stream
+        self._run_stream = rs
         self.ctx.call("gbmie_table_run_graph" if graph else "gbmie_table_run", self.h, ctypes.byref(self.out))
+        self._run_done = torch.cuda.Event()   # this run's end (later work on rs is not waited for)
+        self._run_done.record(rs)
 
     def autotune(self):
         """Tune the launch parameters on this plan's data (synchronous; ends
@@ -186,11 +200,21 @@ class TablePlan(object):
                 "plain_threads": list(q[7:12]), "coef_block": int(q[12]), "tc_window": int(q[13])}
 
     def sync(self):
-        self.ctx.sync()
+        """Wait for the plan's last run (on its stream) and raise on a device
+        error flag."""
+        rs = self._run_stream if self._run_stream is not None else torch.cuda.current_stream(self.ctx.device)
+        with torch.cuda.stream(rs):
+            self.ctx.bind_stream()
+            self.ctx.sync()
 
     def close(self):
+        """Destroy the plan: its arrays are freed in order on the stream of its
+        last run (no wait for the device)."""
         if getattr(self, "h", None) is not None and self.h.value:
-            self.ctx.lib.gbmie_table_plan_destroy(self.h)
+            rs = self._run_stream if self._run_stream is not None else torch.cuda.current_stream(self.ctx.device)
+            with torch.cuda.stream(rs):
+                self.ctx.bind_stream()
+                self.ctx.lib.gbmie_table_plan_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -198,6 +222,35 @@ class TablePlan(object):
             self.close()
         except Exception:
             pass
+
+    def results_async(self, copy_stream):
+        """Start the device -> host copy of the tables after the last run, on
+        copy_stream; returns a PendingResults whose get() waits for the copy
+        only (tables launched afterwards keep running)."""
+        hb = torch.empty(self._out_block.shape, dtype=self._out_block.dtype, pin_memory=True)
+        if self._run_stream is None:
+            copy_stream.wait_stream(torch.cuda.current_stream(self.ctx.device))
+        else:
+            copy_stream.wait_event(self._run_done)
+        with torch.cuda.stream(copy_stream):
+            hb.copy_(self._out_block, non_blocking=True)
+        self._out_block.record_stream(copy_stream)
+        done = torch.cuda.Event()
+        done.record(copy_stream)
+        return PendingResults(self, hb, done, copy_stream)
+
+    def _unpack(self, hb):
+        host = {k: hb[o:o + int(np.prod(shp))].view(shp) for k, (o, shp) in self._out_off.items()}
+        ph = host["phase"].numpy()
+        sc = host["scalar"].numpy()
+        nlv = host["nl"].numpy()
+        res = {k: ph[..., i, :] for i, k in enumerate(SCATKEYS)}
+        res.update({k: sc[..., i] for i, k in enumerate(SCALAR_ORDER)})
+        res.update({"nl_" + k: nlv[..., i] for i, k in enumerate(NL_ORDER)})
+        res["pback"] = host["pback"].numpy()
+        if "pmom" in host:
+            res["pmom"] = host["pmom"].numpy()
+        return res
 
     def results(self):
         """Host dict: scatkeys [nbin, nl, nrh, nang], scalar keys [nbin, nl,
@@ -214,17 +267,55 @@ class TablePlan(object):
         with torch.cuda.stream(cs):
             hb.copy_(self._out_block, non_blocking=True)
         cs.synchronize()
-        host = {k: hb[o:o + int(np.prod(shp))].view(shp) for k, (o, shp) in self._out_off.items()}
-        ph = host["phase"].numpy()
-        sc = host["scalar"].numpy()
-        nlv = host["nl"].numpy()
-        res = {k: ph[..., i, :] for i, k in enumerate(SCATKEYS)}
-        res.update({k: sc[..., i] for i, k in enumerate(SCALAR_ORDER)})
-        res.update({"nl_" + k: nlv[..., i] for i, k in enumerate(NL_ORDER)})
-        res["pback"] = host["pback"].numpy()
-        if "pmom" in host:
-            res["pmom"] = host["pmom"].numpy()
-        return res
+        return self._unpack(hb)
+
+
+class PendingResults(object):
+    """A table's results on their way to the host (TablePlan.results_async)."""
+
+    def __init__(self, plan, hb, done, stream):
+        self.plan, self.hb, self.done, self.stream = plan, hb, done, stream
+
+    def get(self):
+        """Wait for the copy; the device status (error flags) is read on the
+        copy stream, so that tables in flight elsewhere are not waited for."""
+        self.done.synchronize()
+        with torch.cuda.stream(self.stream):
+            self.plan.ctx.bind_stream()
+            self.plan.ctx.sync()
+        return self.plan._unpack(self.hb)
+
+
+def run_tables(specs, precision=_native.GBMIE_MIXED, n_gsf=0, device=0, n_gsf_nodes=0):
+    """Tables of a sequence of specs, pipelined on one GPU: plan i + 1 is
+    created (host work, input copy and setup kernels on a setup stream) while
+    table i runs, and table i's results are copied back (on a copy stream)
+    while table i + 1 runs; plans are closed without waiting for the device.
+    Yields each table's results dict (TablePlan.results) in order."""
+    dv = _native.context(device).device
+    setup = torch.cuda.Stream(dv)
+    copy = torch.cuda.Stream(dv)
+    it = iter(specs)
+    try:
+        spec = next(it)
+    except StopIteration:
+        return
+    plan = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=device, n_gsf_nodes=n_gsf_nodes,
+                     setup_stream=setup)
+    plan.run()
+    while plan is not None:
+        try:
+            spec = next(it)
+            nxt = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=device, n_gsf_nodes=n_gsf_nodes,
+                            setup_stream=setup)
+            nxt.run()
+        except StopIteration:
+            nxt = None
+        pend = plan.results_async(copy)
+        res = pend.get()
+        plan.close()
+        yield res
+        plan = nxt
 
 
 # ---------------------------------------------------------------------------

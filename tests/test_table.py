@@ -238,3 +238,30 @@ def test_autotune_gpu(precision):
     again.run()
     d = again.results()
     assert np.max(np.abs(d["p11"] - b["p11"]) / p11) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_run_tables_pipelined_equals_sequential_gpu(precision):
+    """run_tables overlaps plan creation, runs and result copies of a sequence
+    of tables (setup and copy streams, stream-ordered frees): every table
+    equals the same table planned, run and read back on its own, to the
+    order of the FP64 atomic additions (1e-12 relative); shapes differ
+    between neighbours so that no buffer of one table can stand in for the
+    next one's."""
+    from geosmie_gb300.table import TablePlan, run_tables
+    specs = [synthetic_spec(nl=2, nrh=3, ns=300, seed=1), synthetic_spec(nl=3, nrh=2, ns=257, nbin=2, seed=2),
+             synthetic_spec(nl=2, nrh=3, ns=300, seed=3), synthetic_spec(nl=1, nrh=4, ns=400, nbin=4, seed=4)]
+    ref = []
+    for sp in specs:
+        plan = TablePlan(sp, precision=precision, n_gsf=16)
+        plan.run()
+        ref.append(plan.results())
+        plan.close()
+    got = list(run_tables(specs, precision=precision, n_gsf=16))
+    assert len(got) == len(specs)
+    for a, b in zip(ref, got):
+        for k in SCAT + TIGHT + ["qabs", "pback", "pmom"]:
+            scale = np.maximum(np.abs(a[k]), 1e-300)
+            assert a[k].shape == b[k].shape, k
+            assert np.max(np.abs(b[k] - a[k]) / scale) < 1e-12 or np.max(np.abs(b[k] - a[k])) < 1e-14 * np.max(np.abs(a[k])), k
