@@ -295,7 +295,7 @@ __device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int 
     const int nc = si.cb1 - si.cb0;
     uint8_t *dst = asplit + (size_t)(si.ucb + si.cb0) * 16384;
     const float sc = ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - ex)));
-    const int hh = ia >> 5, r0 = 2 * (ia & 31), r1 = r0 + 1;
+    const int hh = ia >> 5, r0 = 2 * (ia & 31);
     for (int j = 0; j < nc; ++j)
 #pragma unroll
         for (int kg = 0; kg < 2; ++kg) {
@@ -310,17 +310,14 @@ __device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int 
                 split_f16(q.z * sc, ch[2][jj], cl[2][jj]);
                 split_f16(q.w * sc, ch[3][jj], cl[3][jj]);
             }
+            // rows r0 (Re) and r1 = r0 + 1 (Im) of a matrix are 32 contiguous,
+            // 32-byte aligned bytes (r0 even): one 256-bit store each
             const uint32_t o0 = hh * 8192 + kg * 1024 + (r0 >> 3) * 128 + (r0 & 7) * 16;
-            const uint32_t o1 = hh * 8192 + kg * 1024 + (r1 >> 3) * 128 + (r1 & 7) * 16;
             uint8_t *blk = dst + (size_t)j * 16384;
-            *(uint4 *)(blk + 0 * 2048 + o0) = *(uint4 *)ch[0];
-            *(uint4 *)(blk + 0 * 2048 + o1) = *(uint4 *)ch[1];
-            *(uint4 *)(blk + 1 * 2048 + o0) = *(uint4 *)cl[0];
-            *(uint4 *)(blk + 1 * 2048 + o1) = *(uint4 *)cl[1];
-            *(uint4 *)(blk + 2 * 2048 + o0) = *(uint4 *)ch[2];
-            *(uint4 *)(blk + 2 * 2048 + o1) = *(uint4 *)ch[3];
-            *(uint4 *)(blk + 3 * 2048 + o0) = *(uint4 *)cl[2];
-            *(uint4 *)(blk + 3 * 2048 + o1) = *(uint4 *)cl[3];
+            st_global_32b(blk + 0 * 2048 + o0, *(uint4 *)ch[0], *(uint4 *)ch[1]);
+            st_global_32b(blk + 1 * 2048 + o0, *(uint4 *)cl[0], *(uint4 *)cl[1]);
+            st_global_32b(blk + 2 * 2048 + o0, *(uint4 *)ch[2], *(uint4 *)ch[3]);
+            st_global_32b(blk + 3 * 2048 + o0, *(uint4 *)cl[2], *(uint4 *)cl[3]);
         }
     // the last size of a partial tile also zeroes the rows of the sizes the
     // tile lacks (their PSD weights are zero, but 0 x NaN would not be); a

@@ -259,6 +259,14 @@ __device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float *a, 
     }
 }
 
+// 32 bytes (a, then b) to a 32-byte aligned global address in one store.
+__device__ __forceinline__ void st_global_32b(void *p, uint4 a, uint4 b)
+{
+    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(a.x), "r"(a.y), "r"(a.z),
+                 "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+                 : "memory");
+}
+
 // A global line into L1 (no register written, nothing waits for it).
 __device__ __forceinline__ void prefetch_l1(const void *p)
 {
