@@ -226,11 +226,20 @@ typedef struct {
 typedef struct gbmie_table_plan gbmie_table_plan;
 
 /* Plan a table: validates the descriptor, computes the per-wavelength
- * coefficient layout on the device and sizes the scratch memory
- * (synchronous).  The descriptor's pointers must stay valid until the plan
- * is destroyed.  *scratch_bytes (host) receives the scratch size. */
+ * coefficient layout on the device and sizes the scratch memory.  Its
+ * device work runs on the context's stream at the time of the call and it
+ * returns once that stream has done it (other streams are not waited for:
+ * a plan can be created on a side stream while tables run on another).
+ * The plan's arrays are stream-ordered allocations; the angle-function
+ * operand of mixed plans is shared, through the context, by plans with the
+ * same angles and largest nmax.  The descriptor's pointers must stay valid
+ * until the plan is destroyed.  *scratch_bytes (host) receives the scratch
+ * size. */
 int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *desc,
                             gbmie_table_plan **plan, int64_t *scratch_bytes);
+/* Destroy a plan: its arrays are freed in order on the context's stream at
+ * the time of the call (bind the stream of the plan's last run); no wait
+ * for the device unless the plan holds a captured graph. */
 int gbmie_table_plan_destroy(gbmie_table_plan *plan);
 /* Run a planned table: replaces the (bin x lambda x RH) loop of
  * geosmie/dointegration.py:786-1031 (rawMie, calculateScatVals,
