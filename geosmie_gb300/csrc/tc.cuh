@@ -237,40 +237,12 @@ __device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float *a, f
     }
 }
 
-// Columns [ta, ta + 16) and [tb, tb + 16) of this warp's lanes with one wait.
-__device__ __forceinline__ void tmem_ld16x2(uint32_t ta, uint32_t tb, float *a, float *b)
-{
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
-        "tcgen05.wait::ld.sync.aligned;"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(ta), "r"(tb));
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        a[i] = __uint_as_float(r[i]);
-        b[i] = __uint_as_float(r[16 + i]);
-    }
-}
-
 // 32 bytes (a, then b) to a 32-byte aligned global address in one store.
 __device__ __forceinline__ void st_global_32b(void *p, uint4 a, uint4 b)
 {
     asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(a.x), "r"(a.y), "r"(a.z),
                  "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
                  : "memory");
-}
-
-// A global line into L1 (no register written, nothing waits for it).
-__device__ __forceinline__ void prefetch_l1(const void *p)
-{
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
 // Read-only global loads issued where they stand (volatile asm keeps the
