@@ -844,8 +844,8 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                         }
                         // the coefficient chunks of the next tile into L2, and the
                         // PSD weights and exponents of the tile after it (the
-                        // epilogue reads them one item ahead; they were evicted by
-                        // the coefficient operand)
+                        // weights warp reads them a few items ahead; they were
+                        // evicted by the coefficient operand)
                         if (ab == 0 && tile + 1 < ntl)
                             bulk_prefetch_l2(ua + (size_t)cb0 * (2 * TC_B_BYTES), (uint32_t)(cb1 - cb0) * (2 * TC_B_BYTES));
                         if (tile + 2 < ntl || (tile + 2 - ntl < ntl && ab + 1 < nblocks)) {
