@@ -93,6 +93,10 @@ struct gbmie_timer_rec {
 struct gbmie_ctx {
     int device;
     cudaStream_t stream;
+    // a side stream for independent work inside a table run (forked from and
+    // joined back into `stream` by the two events)
+    cudaStream_t side;
+    cudaEvent_t ev_fork, ev_join;
     int timing;               // per-kernel event timing enabled
     int timer_open;           // a start event is recorded and awaits its kernel
     int ntimer;

@@ -163,7 +163,10 @@ int gbmie_ctx_create(int device, gbmie_ctx **out)
     ctx->stream = 0;
     if (cudaMalloc(&ctx->d_flags, 64) != cudaSuccess ||
         cudaMallocHost(&ctx->h_flags, 64) != cudaSuccess ||
-        cudaMallocHost(&ctx->h_pinned, 4096) != cudaSuccess) {
+        cudaMallocHost(&ctx->h_pinned, 4096) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         gbmie_ctx_destroy(ctx);
         return GBMIE_ERR_NOMEM;
     }
@@ -203,6 +206,12 @@ int gbmie_ctx_destroy(gbmie_ctx *ctx)
             }
         free(ctx->timers);
     }
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);

@@ -944,10 +944,18 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     ctx_pre_launch(ctx);
     k_tab_index<<<(unsigned)ceil_div64(p->n_units, 128), 128, 0, st>>>(p->n_units, v.m, v.hidx, ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_index"));
+    // the PSD weights on the side stream, alongside the recurrences (they are
+    // first read by the angular kernels and the scalar sums: joined there)
     const int64_t nW = (int64_t)(v.lam_shared ? 1 : d.n_lambda) * d.n_rh * d.n_bin * d.n_comp;
+    GBMIE_TRY(ctx_cuda(ctx, cudaEventRecord(ctx->ev_fork, st), "fork"));
+    GBMIE_TRY(ctx_cuda(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0), "fork"));
+    ctx->stream = ctx->side;
     ctx_pre_launch(ctx);
-    k_tab_weights<<<(unsigned)nW, 256, 0, st>>>(v, d.weights);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_tab_weights"));
+    k_tab_weights<<<(unsigned)nW, 256, 0, ctx->side>>>(v, d.weights);
+    const int wst = ctx_check_launch(ctx, "k_tab_weights");
+    ctx->stream = st;
+    GBMIE_TRY(wst);
+    GBMIE_TRY(ctx_cuda(ctx, cudaEventRecord(ctx->ev_join, ctx->side), "join"));
     ctx_pre_launch(ctx);
     if (d.precision == GBMIE_MIXED) {
         GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
@@ -962,6 +970,7 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
         k_tab_coeffs<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(v, p->n_inst, ctx->d_flags);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs"));
     }
+    GBMIE_TRY(ctx_cuda(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0), "join"));   // the PSD weights
     GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
     GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
                        "pacc clear"));

@@ -1274,6 +1274,7 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
                                                                    p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
     }
+    GBMIE_TRY(ctx_cuda(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0), "join"));   // the PSD weights
     TcArgs a;
     a.v = v;
     a.cf = cf;
