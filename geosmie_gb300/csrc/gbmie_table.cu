@@ -898,7 +898,7 @@ static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, co
     k_tab_trapz<<<1, 256, 0, st>>>(d.n_ang, d.theta, v.tw);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_trapz"));
     ctx_pre_launch(ctx);
-    k_tab_finalize<<<(unsigned)p->n_entries, 256, 0, st>>>(v, *out);
+    k_tab_finalize<<<(unsigned)p->n_entries, 64, 0, st>>>(v, *out);   // 2-3 angles per thread
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
     if (p->has_gsf) {
         GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
