@@ -173,7 +173,7 @@ int gbmie_ctx_create(int device, gbmie_ctx **out)
     cudaMemset(ctx->d_flags, 0, 64);
     // plan arrays are stream-ordered allocations from the device's default
     // pool: keep freed blocks in the pool (the default threshold returns them
-    // to the driver at every synchronisation) so that plan creation reuses
+    // to the CUDA driver at every synchronisation) so that plan creation reuses
     // them; a process-level attribute of the pool, no device setting
     {
         cudaMemPool_t pool;
