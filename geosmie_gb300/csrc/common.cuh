@@ -123,7 +123,11 @@ struct gbmie_ctx {
         double *hcos;   // host copy of the key's cos(theta)
         int refs;
     } angle_ops[4];
+    void *table_cache;   // GSF tables of table plans (gbmie_table.cu), or NULL
 };
+
+// Frees the context's cached table-plan tables (gbmie_table.cu).
+void table_cache_release(gbmie_ctx *ctx);
 
 // Angle-function operand for (cos theta on the host, sizes): a cached one
 // or a fresh cache entry the caller fills; *entry is its index (release it

@@ -194,6 +194,7 @@ int gbmie_ctx_destroy(gbmie_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     else cudaDeviceSynchronize();
     if (ctx->scratch) cudaFree(ctx->scratch);
+    table_cache_release(ctx);
     for (auto &e : ctx->angle_ops) {
         if (e.bt) cudaFree(e.bt);
         free(e.hcos);

@@ -578,6 +578,103 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     return v;
 }
 
+// GSF tables of table plans (Gauss nodes, generalized spherical functions,
+// interpolation, the digit operand and the row buffers of the tensor-core
+// expansion): they depend on the node and moment counts, the angles, the
+// entry count and the precision only, so plans with the same key share them
+// through the context (plans run one after another on a context, as they
+// share its scratch).  Reference-counted; unused entries are evicted.
+struct GsfCacheEntry {
+    bool used;
+    GsfTables t;
+    int ng, L, nang, ntab_max, precision;
+    double *hkey;   // [2 nang]: cos(theta), theta of the key
+    int refs;
+};
+struct TableCache {
+    GsfCacheEntry gsf[2];
+};
+
+void table_cache_release(gbmie_ctx *ctx)
+{
+    TableCache *c = (TableCache *)ctx->table_cache;
+    if (!c) return;
+    cudaDeviceSynchronize();
+    for (GsfCacheEntry &e : c->gsf)
+        if (e.used) {
+            gsf_release(&e.t, ctx->stream);
+            free(e.hkey);
+        }
+    free(c);
+    ctx->table_cache = nullptr;
+}
+
+static void table_gsf_release(gbmie_ctx *ctx, int entry)
+{
+    TableCache *c = (TableCache *)ctx->table_cache;
+    if (c && entry >= 0 && c->gsf[entry].refs > 0) --c->gsf[entry].refs;
+}
+
+// The GSF tables for a plan: a cached entry with the same key, else freshly
+// prepared (into a cache entry when one is free or unused, else plan-owned,
+// *entry = -1).  hkey: cos(theta) then theta on the host.
+static int table_gsf_get(gbmie_ctx *ctx, int ng, int L, int nang, const double *theta, const double *hkey,
+                         int ntab_max, int precision, GsfTables *t, int *entry)
+{
+    *entry = -1;
+    if (!ctx->table_cache) ctx->table_cache = calloc(1, sizeof(TableCache));
+    TableCache *c = (TableCache *)ctx->table_cache;
+    const int cap = (int)(sizeof(c->gsf) / sizeof(c->gsf[0]));
+    for (int i = 0; c && i < cap; ++i) {
+        GsfCacheEntry &e = c->gsf[i];
+        if (e.used && e.ng == ng && e.L == L && e.nang == nang && e.ntab_max == ntab_max && e.precision == precision &&
+            memcmp(e.hkey, hkey, sizeof(double) * 2 * nang) == 0) {
+            ++e.refs;
+            *t = e.t;
+            *entry = i;
+            return GBMIE_OK;
+        }
+    }
+    int slot = -1;
+    for (int i = 0; c && i < cap && slot < 0; ++i)
+        if (!c->gsf[i].used) slot = i;
+    for (int i = 0; c && i < cap && slot < 0; ++i)
+        if (c->gsf[i].refs == 0) {
+            // evict: a run of the plan that last held it may still be in flight
+            // on another stream, so the device is idle before the free
+            cudaDeviceSynchronize();
+            gsf_release(&c->gsf[i].t, ctx->stream);
+            free(c->gsf[i].hkey);
+            c->gsf[i].used = false;
+            slot = i;
+        }
+    double *hk = slot >= 0 ? (double *)malloc(sizeof(double) * 2 * nang) : nullptr;
+    if (slot < 0 || !hk) {   // plan-owned tables outside the cache
+        free(hk);
+        return gsf_prepare(ctx, ng, L, nang, theta, t, ntab_max, precision);
+    }
+    GsfCacheEntry &e = c->gsf[slot];
+    e.t = GsfTables{};
+    const int st = gsf_prepare(ctx, ng, L, nang, theta, &e.t, ntab_max, precision);
+    if (st != GBMIE_OK) {
+        gsf_release(&e.t, ctx->stream);
+        free(hk);
+        return st;
+    }
+    memcpy(hk, hkey, sizeof(double) * 2 * nang);
+    e.used = true;
+    e.hkey = hk;
+    e.ng = ng;
+    e.L = L;
+    e.nang = nang;
+    e.ntab_max = ntab_max;
+    e.precision = precision;
+    e.refs = 1;
+    *t = e.t;
+    *entry = slot;
+    return GBMIE_OK;
+}
+
 // The plan's device arrays are stream-ordered allocations, freed in order on
 // the context's stream after its last use there: destroying a plan neither
 // waits for the device nor stalls work in flight on other streams.
@@ -599,7 +696,8 @@ static void plan_free(gbmie_table_plan *p)
     if (p->unit_cbase) cudaFreeAsync(p->unit_cbase, s);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
-    gsf_release(&p->gsf, s);
+    if (p->has_gsf && p->gsf_entry >= 0) table_gsf_release(p->ctx, p->gsf_entry);
+    else gsf_release(&p->gsf, s);
     free(p);
 }
 
@@ -671,11 +769,17 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         st = ctx_cuda(ctx, cudaMemcpyAsync(hoff, p->off, sizeof(int64_t) * (nrows + 1), cudaMemcpyDeviceToHost, ctx->stream),
                       "plan offsets copy");
     p->bt_entry = -1;
-    if (st == GBMIE_OK && d.precision == GBMIE_MIXED) {   // the key of the angle-function operand
-        p->hcos = (double *)malloc(sizeof(double) * d.n_ang);
+    p->gsf_entry = -1;
+    if (st == GBMIE_OK && (d.precision == GBMIE_MIXED || d.n_gsf > 0)) {
+        // the keys of the cached angle operand and GSF tables: cos(theta), theta
+        p->hcos = (double *)malloc(sizeof(double) * 2 * d.n_ang);
         if (!p->hcos) st = GBMIE_ERR_NOMEM;
         else
             st = ctx_cuda(ctx, cudaMemcpyAsync(p->hcos, d.cos_theta, sizeof(double) * d.n_ang, cudaMemcpyDeviceToHost, ctx->stream),
+                          "plan angles copy");
+        if (st == GBMIE_OK)
+            st = ctx_cuda(ctx, cudaMemcpyAsync(p->hcos + d.n_ang, d.theta, sizeof(double) * d.n_ang,
+                                               cudaMemcpyDeviceToHost, ctx->stream),
                           "plan angles copy");
     }
     if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaStreamSynchronize(ctx->stream), "plan offsets sync");
@@ -853,12 +957,10 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         st = ctx_scratch(ctx, p->bytes, &scr);
     }
     if (st == GBMIE_OK && d.precision == GBMIE_MIXED) st = build_table_bt(ctx, p);
-    free(p->hcos);
-    p->hcos = nullptr;
     if (st == GBMIE_OK) table_tune_lookup(ctx, p);
     if (st == GBMIE_OK && d.n_gsf > 0) {
-        st = gsf_prepare(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, &p->gsf,
-                         (int)p->n_entries, d.precision);
+        st = table_gsf_get(ctx, d.n_gsf_nodes > 0 ? d.n_gsf_nodes : d.n_gsf, d.n_gsf, d.n_ang, d.theta, p->hcos,
+                           (int)p->n_entries, d.precision, &p->gsf, &p->gsf_entry);
         p->has_gsf = 1;
     }
     if (st == GBMIE_OK) st = gbmie_ctx_synchronize(ctx);

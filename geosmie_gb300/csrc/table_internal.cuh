@@ -40,6 +40,7 @@ struct gbmie_table_plan {
     size_t o_asplit;
     GsfTables gsf;
     int has_gsf;
+    int gsf_entry;       // its context cache entry, or -1 when plan-owned
     // CUDA graph of one gbmie_table_run (gbmie_table_run_graph): captured on
     // a private stream, replayed on the context stream
     cudaStream_t cap_stream;

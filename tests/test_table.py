@@ -269,9 +269,9 @@ def test_run_tables_pipelined_equals_sequential_gpu(precision):
 
 @pytest.mark.gpu
 def test_angle_operand_cache_reuse_and_eviction_gpu():
-    """Mixed plans share the context's cached angle-function operand when the
-    angles and the largest nmax agree, and evict unused entries when more
-    grids than the cache holds come along: a table planned again after five
+    """Mixed plans share the context's cached angle-function operand (and GSF
+    tables) when the angles, the largest nmax (the entry count) agree, and
+    evict unused entries when more grids than the caches hold come along: a table planned again after five
     other angle grids (an eviction) equals its first planning, and plans
     alive at the same time with equal keys give equal tables."""
     from geosmie_gb300.table import TablePlan
@@ -283,15 +283,15 @@ def test_angle_operand_cache_reuse_and_eviction_gpu():
         return sp
 
     def table(sp):
-        plan = TablePlan(sp, precision=1)
+        plan = TablePlan(sp, precision=1, n_gsf=16)
         plan.run()
         res = plan.results()
         plan.close()
         return res
 
     first = table(base)
-    p1 = TablePlan(base, precision=1)
-    p2 = TablePlan(base, precision=1)   # the same key while p1 is alive: the shared entry
+    p1 = TablePlan(base, precision=1, n_gsf=16)
+    p2 = TablePlan(base, precision=1, n_gsf=16)   # the same key while p1 is alive: the shared entries
     p1.run()
     r1 = p1.results()
     p2.run()
@@ -301,7 +301,8 @@ def test_angle_operand_cache_reuse_and_eviction_gpu():
     for nang in (91, 121, 150, 211, 371):   # more grids than the cache's entries
         table(spec_with(nang))
     again = table(base)
-    for k in SCAT + TIGHT + ["pback"]:
+    for k in SCAT + TIGHT + ["pback", "pmom"]:
         scale = np.maximum(np.abs(first[k]), 1e-300)
         for other in (r1, r2, again):
-            assert np.max(np.abs(other[k] - first[k]) / scale) < 1e-12, k
+            assert np.max(np.abs(other[k] - first[k]) / scale) < 1e-12 or \
+                np.max(np.abs(other[k] - first[k])) < 1e-14 * np.max(np.abs(first[k])), k
