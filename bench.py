@@ -48,6 +48,25 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws, device=None):
+    """The largest of the ranks' x (all_reduce with MAX over the default
+    process group, on `device`: a CUDA device under NCCL, the CPU under gloo);
+    x itself on one rank."""
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, ws, steps, seconds):
+    """Whole-job throughput of ws replicas: every rank processed
+    units_per_rank x steps units; seconds is the max-over-ranks time."""
+    return ws * units_per_rank * steps / seconds
+
+
 def _oracle_unit(args):
     """One (wavelength, RH) unit of the table on the CPU with the oracle:
     per-size coefficients, per-angle S1/S2 sums (pymiecoated's algorithm),
@@ -237,9 +256,7 @@ def main():
         ctx.set_timing(False)
         plan.sync()   # device error flags -> status
         if ws > 1:
-            t = torch.tensor([ms], dtype=torch.float64, device="cuda:%d" % dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+            ms = max_over_ranks(ms, ws, device="cuda:%d" % dev)
             torch.distributed.barrier()
         return ms, launches, kt, clk
 
@@ -258,7 +275,7 @@ def main():
     # the product path: the whole table replayed as one CUDA graph
     ms, launches, _, clk = timed(plan_mixed, graph=True, with_clocks=True)
     ms_step = ms / args.steps
-    value = ws * counts["instances"] * args.steps / (ms * 1e-3)
+    value = replica_value(counts["instances"], ws, args.steps, ms * 1e-3)
     # accuracy of the mixed table against the FP64 table (same run), every output
     rb = plan_mixed.results()
     p11 = np.abs(ra["p11"])
@@ -288,14 +305,16 @@ def main():
     probe.close()
     for _ in run_tables([spec] * 2, precision=_native.GBMIE_MIXED, n_gsf=n_gsf, device=dev):
         pass   # warm-up of the streams and the allocation pool
+    if ws > 1:
+        torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     n_done = 0
     for res in run_tables([spec] * args.steps, precision=_native.GBMIE_MIXED, n_gsf=n_gsf, device=dev):
         n_done += 1
     torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
-    e2e_value = ws * counts["instances"] * n_done / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws, device="cuda:%d" % dev)
+    e2e_value = replica_value(counts["instances"], ws, n_done, e2e_s)
 
     # ---- roofline of the dominant kernel (FP64 pipe) ----
     top = max(ktimes.items(), key=lambda kv: kv[1][1]) if ktimes else (None, (0, 0.0))
@@ -384,7 +403,7 @@ def main():
         "table_gen_ms": {"mixed": ms_step, "mixed_eager_launches": ms_eager / args.steps,
                          "plain_fp64": ms_plain / args.steps},
         "mixed_vs_plain_speedup": ms_plain / ms,
-        "plain_fp64": {"value": ws * counts["instances"] * args.steps / (ms_plain * 1e-3), "unit": UNIT,
+        "plain_fp64": {"value": replica_value(counts["instances"], ws, args.steps, ms_plain * 1e-3), "unit": UNIT,
                        "kernels": kernel_table(kt_plain)},
         "accuracy_mixed_vs_fp64": acc,
         "roofline": roof,
