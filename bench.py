@@ -394,10 +394,10 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 recurrences + f16x2-split tensor contractions (f32 accumulate)", "data": "synthetic (seeded; no dataset)",
+        "vs_baseline": None, "dtype": "f32-pair (double-float) recurrences + f16x2-split tensor contractions (f32 accumulate)", "data": "synthetic (seeded; no dataset)",
         "config": {"workload": desc, "instances": counts["instances"], "sum_nmax": counts["sum_nmax"],
-                   "gsf_moments": n_gsf, "precision": "mixed: FP64 recurrences, tcgen05 split-FP16 contractions "
-                   "with FP32 accumulation", "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "gsf_moments": n_gsf, "precision": "mixed: double-float (FP32-pair) D_n and N/M recurrences on FP64-built "
+                   "psi/chi rows, tcgen05 split-FP16 contractions with FP32 accumulation", "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "l2": "flushed before every table (256 MB write inside the timed region)",
                    "launch": "whole table replayed as one CUDA graph (gbmie_table_run_graph)"},
         "table_gen_ms": {"mixed": ms_step, "mixed_eager_launches": ms_eager / args.steps,
