@@ -37,6 +37,31 @@ def _check_table(got, ref, prefix=""):
     assert err < 1e-10, ("qabs", err)
 
 
+@pytest.mark.parametrize("name", ["lognorm", "seasalt", "su", "trivial"])
+def test_bin_spec_host_fields_match_reference_cpu(name):
+    """The host side of the table driver is bit-exact against the reference's
+    written variables: RH growth and the mixed refractive index
+    (getHumidRefractiveIndex, dointegration.py:493-537), the wet density
+    (dointegration.py:874) and the bin edges.  The particle's imaginary index
+    is negated for the Mie convention, as the reference does before its Mie
+    calls (dointegration.py:814)."""
+    from geosmie_gb300 import table
+    g = load_golden("table_%s.npz" % name)
+    params = json.loads(str(g["params_json"]))
+    nrh = g["out_rh"].size
+    for b in range(g["out_bin"].size):
+        s = table.bin_spec(params, b, list(g["mlist"]), g["waterm"], table.angmie())
+        rep = nrh if s["trivial_nrh"] else 1
+        assert s["trivial_nrh"] in (0, nrh)
+        np.testing.assert_array_equal(np.repeat(s["gf"], rep), g["out_growth_factor"][b])
+        np.testing.assert_array_equal(np.repeat(s["rhop"][0], rep), g["out_rhop"][b])
+        mix = np.repeat(s["m"][:, :, 0], rep, axis=1)
+        np.testing.assert_array_equal(mix.real, g["out_refreal"][b])
+        np.testing.assert_array_equal(-mix.imag, g["out_refimag"][b])
+        assert np.all(s["rlow"][0] == g["out_rLow"][b]) and np.all(s["rup"][0] == g["out_rUp"][b])
+        assert s["grid"].size > 0 and np.all(np.diff(s["grid"]) > 0)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt", "su"])
 def test_reference_tables_gpu(name):
