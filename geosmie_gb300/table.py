@@ -332,7 +332,12 @@ def _get_dr(arr):
 
 
 def _carma_grid(minx, maxx, nbinperdecade):
-    """Volume-ratio size grid and widths (dointegration.py:103-153)."""
+    """Volume-ratio size grid and widths (dointegration.py:103-153).
+
+    The powers are taken one grid point at a time as scalars, as the
+    reference does: numpy's vectorised power rounds differently (by an ulp
+    here and there, and differently per CPU), and the grid then no longer
+    equals the reference's bit for bit."""
     rat = maxx / minx
     nbin = np.log10(maxx / minx) * nbinperdecade
     rmrat = (rat ** 3) ** (1.0 / nbin)
@@ -340,9 +345,14 @@ def _carma_grid(minx, maxx, nbinperdecade):
     cpi = 4.0 / 3.0 * np.pi
     rvolmin = cpi * rmin ** 3.0
     vrfact = ((3.0 / 2.0 / np.pi / (rmrat + 1)) ** (1.0 / 3.0)) * (rmrat ** (1.0 / 3.0) - 1.0)
-    i = np.arange(int(nbin))
-    rvol = rvolmin * rmrat ** i
-    return (rvol / cpi) ** (1.0 / 3.0), vrfact * rvol ** (1.0 / 3.0)
+    n = int(nbin)
+    r = np.empty(n)
+    dr = np.empty(n)
+    for k in range(n):
+        rvol = rvolmin * rmrat ** k
+        r[k] = (rvol / cpi) ** (1.0 / 3.0)
+        dr[k] = vrfact * rvol ** (1.0 / 3.0)
+    return r, dr
 
 
 def _x_grid(params, b, minlam, maxlam):

@@ -62,6 +62,33 @@ def test_bin_spec_host_fields_match_reference_cpu(name):
         assert s["grid"].size > 0 and np.all(np.diff(s["grid"]) > 0)
 
 
+@pytest.mark.parametrize("name", ["lognorm", "seasalt", "su", "trivial"])
+def test_host_grid_and_weights_match_oracle_cpu(name):
+    """The size-parameter grid and its widths (initializeXarr,
+    dointegration.py:425-463) equal the oracle's bit for bit (the oracle's
+    grid equals the reference's own on these definitions); the Gong sea-salt
+    weights (dointegration.py:585-624), which the table driver passes to the
+    GPU as explicit weights, agree to the last bits."""
+    from geosmie_gb300 import table
+    from oracle import integration as oi
+    g = load_golden("table_%s.npz" % name)
+    params = json.loads(str(g["params_json"]))
+    lam = np.asarray(list(g["mlist"])[0][0])
+    rh = list(params["rh"])
+    for b in range(g["out_bin"].size):
+        x, dx = table._x_grid(params, b, lam[0], lam[-1])
+        xo, dxo = oi.initialize_xarr(params, b, lam[0], lam[-1])
+        np.testing.assert_array_equal(x, xo)
+        np.testing.assert_array_equal(dx, dxo)
+        if params["psd"]["type"] != "ss":
+            continue
+        w = table._ss_weights(params, b, rh, x, lam)
+        for li, l_ in enumerate(lam):
+            for ri, r in enumerate(rh):
+                ref = oi.calculate_psd(params, b, r, rh, xo, dxo, None, l_)[0][0]
+                assert np.max(np.abs(w[li, ri] - ref)) <= 4 * np.finfo(float).eps * np.max(ref)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt", "su"])
 def test_reference_tables_gpu(name):
