@@ -302,20 +302,28 @@ def run_tables(specs, precision=_native.GBMIE_MIXED, n_gsf=0, device=0, n_gsf_no
         return
     plan = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=device, n_gsf_nodes=n_gsf_nodes,
                      setup_stream=setup)
-    plan.run()
-    while plan is not None:
-        try:
-            spec = next(it)
-            nxt = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=device, n_gsf_nodes=n_gsf_nodes,
-                            setup_stream=setup)
-            nxt.run()
-        except StopIteration:
-            nxt = None
-        pend = plan.results_async(copy)
-        res = pend.get()
-        plan.close()
-        yield res
-        plan = nxt
+    nxt = None
+    try:
+        plan.run()
+        while plan is not None:
+            try:
+                spec = next(it)
+                nxt = TablePlan(spec, precision=precision, n_gsf=n_gsf, device=device, n_gsf_nodes=n_gsf_nodes,
+                                setup_stream=setup)
+                nxt.run()
+            except StopIteration:
+                nxt = None
+            pend = plan.results_async(copy)
+            res = pend.get()
+            plan.close()
+            yield res
+            plan, nxt = nxt, None
+    finally:
+        # a consumer that stops early, or an error: the open plans are
+        # destroyed now (in order on their run streams), not at collection
+        for p_ in (plan, nxt):
+            if p_ is not None:
+                p_.close()
 
 
 # ---------------------------------------------------------------------------

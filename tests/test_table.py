@@ -358,3 +358,74 @@ def test_angle_operand_cache_reuse_and_eviction_gpu():
         for other in (r1, r2, again):
             assert np.max(np.abs(other[k] - first[k]) / scale) < 1e-12 or \
                 np.max(np.abs(other[k] - first[k])) < 1e-14 * np.max(np.abs(first[k])), k
+
+
+class _FakePlan(object):
+    """Stands in for TablePlan in the host-side pipelining test: records the
+    order of plan creation, runs, result copies and closes."""
+    log = []
+    fail_on = None
+
+    def __init__(self, spec, **kw):
+        if spec == _FakePlan.fail_on:
+            raise RuntimeError("plan %r" % spec)
+        self.spec = spec
+        self.open = True
+        _FakePlan.log.append(("create", spec))
+
+    def run(self):
+        _FakePlan.log.append(("run", self.spec))
+
+    def results_async(self, stream):
+        plan = self
+
+        class _Pending(object):
+            def get(self):
+                _FakePlan.log.append(("copy", plan.spec))
+                return {"spec": plan.spec}
+        return _Pending()
+
+    def close(self):
+        if self.open:
+            _FakePlan.log.append(("close", self.spec))
+        self.open = False
+
+
+@pytest.fixture
+def fake_pipeline(monkeypatch):
+    from geosmie_gb300 import table
+
+    class _Ctx(object):
+        device = "cpu"
+    monkeypatch.setattr(table._native, "context", lambda device=0: _Ctx())
+    monkeypatch.setattr(table.torch.cuda, "Stream", lambda device=None: object())
+    monkeypatch.setattr(table, "TablePlan", _FakePlan)
+    _FakePlan.log = []
+    _FakePlan.fail_on = None
+    return table
+
+
+def test_run_tables_order_and_cleanup_cpu(fake_pipeline):
+    """run_tables (host logic, CPU): table i + 1 is planned and launched
+    before table i's results are copied back; every plan is closed once, also
+    when the consumer stops early or a later plan fails."""
+    table = fake_pipeline
+    got = [r["spec"] for r in table.run_tables(["a", "b", "c"])]
+    assert got == ["a", "b", "c"]
+    assert _FakePlan.log == [("create", "a"), ("run", "a"), ("create", "b"), ("run", "b"), ("copy", "a"),
+                             ("close", "a"), ("create", "c"), ("run", "c"), ("copy", "b"), ("close", "b"),
+                             ("copy", "c"), ("close", "c")]
+    assert list(table.run_tables([])) == []
+    # consumer stops after the first table: the plan in flight is closed
+    _FakePlan.log = []
+    gen = table.run_tables(["a", "b", "c"])
+    assert next(gen)["spec"] == "a"
+    gen.close()
+    assert [e for e in _FakePlan.log if e[0] == "close"] == [("close", "a"), ("close", "b")]
+    assert ("create", "c") not in _FakePlan.log
+    # a later plan fails: the error reaches the consumer and the open plan is closed
+    _FakePlan.log = []
+    _FakePlan.fail_on = "b"
+    with pytest.raises(RuntimeError):
+        list(table.run_tables(["a", "b", "c"]))
+    assert [e for e in _FakePlan.log if e[0] == "close"] == [("close", "a")]
