@@ -14,6 +14,8 @@ Deliberate differences from the reference, each a fix of a reference bug:
   * ``ajv``/``ayv`` (caller-supplied Bessel arrays) are accepted and ignored:
     the Riccati-Bessel functions are always computed on the device.
 """
+import collections
+
 import numpy as np
 import torch
 
@@ -23,19 +25,31 @@ __all__ = ["Mie", "MultipleMie", "Cache"]
 
 
 class Cache(dict):
-    """FIFO cache of ten entries (pymiecoated/mie_aux.py:22-33)."""
+    """Bounded first-in-first-out cache of a Mie object's results: once more
+    than `size` (10) parameter sets are stored, the oldest one is dropped
+    (pymiecoated/mie_aux.py:22-33).  Storing a key that is already present
+    replaces its value and keeps its place in the order."""
 
     def __init__(self, size=10):
         super().__init__()
         self.size = size
-        self.log = []
+        self._order = collections.deque()
+
+    @property
+    def log(self):
+        """The stored keys, oldest first."""
+        return list(self._order)
 
     def __setitem__(self, key, value):
+        if key not in self:
+            self._order.append(key)
         super().__setitem__(key, value)
-        self.log.append(key)
-        if len(self.log) > self.size:
-            del self[self.log[0]]
-            self.log.pop(0)
+        while len(self._order) > self.size:
+            super().pop(self._order.popleft(), None)
+
+    def __delitem__(self, key):
+        super().__delitem__(key)
+        self._order.remove(key)
 
 
 def _dev(a, dtype, device):

@@ -38,6 +38,26 @@ def test_errors_cpu():
         mie.qext()                     # coated with mu != 1
 
 
+def test_cache_first_in_first_out_cpu():
+    """A Mie object's cache keeps its ten newest parameter sets
+    (mie_aux.py:22-33); re-storing a key keeps its place."""
+    from geosmie_gb300.mie import Cache
+    c = Cache()
+    for k in range(10):
+        c[k] = str(k)
+    c[3] = "again"
+    assert len(c) == 10 and c[3] == "again" and c.log == list(range(10))
+    c[10] = "10"
+    assert 0 not in c and len(c) == 10 and c.log == list(range(1, 11))
+    for k in range(11, 25):
+        c[k] = str(k)
+    assert sorted(c) == list(range(15, 25)) and c.log == list(range(15, 25))
+    del c[20]
+    c[25] = "25"
+    assert sorted(c) == [15, 16, 17, 18, 19, 21, 22, 23, 24, 25]
+    assert Mie()._cache.size == 10
+
+
 def test_m2_getter_is_fixed():
     mie = Mie(m=1.5 + 0.5j, m2=1.2 + 0.2j, x=1.5, y=5.0)
     assert abs(mie.m2 - (1.2 + 0.2j)) < 1e-15
