@@ -146,6 +146,103 @@ def run_reference(args):
     return 0
 
 
+def algorithmic_flop(counts):
+    """Algorithmic flop per launch of the table kernels, from the per-instance
+    work of the reference's algorithm: coefficients 14 nmx + 50 nmax (FP64
+    flop); angular sums 16 nmax N_ang (four complex-by-real multiply-adds per
+    order and angle); the Mueller elements, 12 flop per (instance, angle),
+    and their size integration, a multiply-add for each of the 6 elements
+    per (instance, bin, angle).  Split products, padding and the S+/S- form
+    are the implementation's, not the algorithm's, and are not counted."""
+    nang, nbin, inst = counts["nang"], counts["nbin"], counts["instances"]
+    coef = 14.0 * counts["sum_nmx"] + 50.0 * counts["sum_nmax"]
+    sums = 16.0 * counts["sum_nmax"] * nang
+    mueller = (12.0 + 12.0 * nbin) * nang * inst
+    return {"k_tab_coeffs": coef, "k_tab_coeffs_mixed": coef, "k_tab_s12_plain": sums + mueller,
+            "k_tab_s12_tc": sums, "k_tab_s12_tc_epilogue": mueller}
+
+
+def executed_flop(counts):
+    """Flop the kernels execute per launch (pipe utilisation).  FP64 pipe:
+    the plain sums in the S+/S- form (8 per order and angle; the S+ and S-
+    sums halve the reference's multiply-adds), the Mueller elements (14) and
+    the number-weighted accumulation (8 per bin) per (instance, angle); the
+    plain coefficients 12 per D_n step and 89 per order.  The mixed
+    coefficient kernel's double-float work counted as the FP64 flop of the
+    same steps: 15 per warm-up D_n step, 32 per order.  Tensor cores: 6 MMAs
+    (M 128 angles x N 64 (32 sizes, Re/Im) x K 16) per 16-order chunk of a
+    half tile of 32 sizes, per 128-angle block (3 split products x 2 GEMMs,
+    padded)."""
+    nang, nbin, inst = counts["nang"], counts["nbin"], counts["instances"]
+    return {"k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * inst) * nang,
+            "k_tab_coeffs": 12.0 * counts["sum_nmx"] + 89.0 * counts["sum_nmax"],
+            "k_tab_coeffs_mixed": 15.0 * counts["sum_warm"] + 32.0 * counts["sum_nmax"],
+            "k_tab_s12_tc": counts["sum_kc16_half"] * 6 * 2 * 128 * 64 * 16 * (-(-nang // 128))}
+
+
+ON_FP64_PIPE = ("k_tab_s12_plain", "k_tab_coeffs")
+
+
+def roofline_of(ktimes, counts, peaks, fp64_peak):
+    """Per-kernel rates and the roofline of the dominant kernel.
+
+    ktimes: {kernel: (launches, total ms)} from CUDA events on the launching
+    stream; peaks: MEASURED_PEAKS-style dict (bf16_tflops); fp64_peak:
+    measured DFMA GFLOP/s.  achieved = algorithmic flop per launch / mean
+    launch time; the executed flop (what the pipe ran) is reported beside
+    it.  Returns (kernels, roof)."""
+    alg = algorithmic_flop(counts)
+    exe = executed_flop(counts)
+    kernels = {}
+    tot = max(1e-9, sum(v[1] for v in ktimes.values()))
+    for name, (nl_, tms) in ktimes.items():
+        sec = tms / max(nl_, 1) * 1e-3
+        k = {"launches": nl_, "ms_per_launch": tms / max(nl_, 1), "share": tms / tot}
+        if name in ON_FP64_PIPE:
+            k["algorithmic_gflops"] = alg[name] / sec / 1e9
+            k["fp64_gflops"] = exe[name] / sec / 1e9
+            k["fp64_pipe_frac"] = exe[name] / sec / 1e9 / fp64_peak
+        elif name == "k_tab_coeffs_mixed":
+            k["algorithmic_gflops"] = alg[name] / sec / 1e9
+            k["fp64_equivalent_gflops_as_fp32_pairs"] = exe[name] / sec / 1e9
+        elif name == "k_tab_s12_tc":
+            k["algorithmic_tflops"] = alg[name] / sec / 1e12
+            k["executed_mma_tflops"] = exe[name] / sec / 1e12
+            k["epilogue_algorithmic_tflops"] = alg["k_tab_s12_tc_epilogue"] / sec / 1e12
+            k["tensor_peak_tflops"] = peaks.get("bf16_tflops")
+        kernels[name] = k
+    roof = None
+    top = max(ktimes.items(), key=lambda kv: kv[1][1])[0] if ktimes else None
+    if top in ON_FP64_PIPE:
+        nl_, tms = ktimes[top]
+        sec = tms / max(nl_, 1) * 1e-3
+        ach = alg[top] / sec / 1e9
+        tb = NCU_BYTES_PER_UNIT.get(top)
+        roof = {"bound": "fp64", "kernel": top, "achieved": ach, "peak": fp64_peak, "unit": "GFLOP/s",
+                "frac": ach / fp64_peak, "traffic": tb * counts["units"] if tb else None,
+                "traffic_unit": "bytes per launch (ncu capture scaled by units)",
+                "peak_source": "DFMA throughput measured in this run (gbmie_measure_fp64_peak); "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "algorithmic_flop_per_launch": alg[top], "executed_flop_per_launch": exe[top],
+                "executed_frac": exe[top] / sec / 1e9 / fp64_peak}
+    elif top == "k_tab_s12_tc":
+        nl_, tms = ktimes[top]
+        sec = tms / max(nl_, 1) * 1e-3
+        peak = peaks.get("bf16_tflops")
+        roof = {"bound": "tensor", "kernel": top, "achieved": alg[top] / sec / 1e12,
+                "peak": peak, "unit": "TFLOP/s", "frac": alg[top] / sec / 1e12 / peak,
+                "traffic": NCU_BYTES_PER_UNIT[top] * counts["units"],
+                "traffic_unit": "bytes per launch (ncu capture scaled by units)",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                "algorithmic_flop_per_launch": alg[top], "executed_mma_flop_per_launch": exe[top],
+                "executed_frac": exe[top] / sec / 1e12 / peak,
+                "note": "achieved = the angular sums' algorithmic flop (16 per order and angle); the "
+                        "tensor cores execute executed_mma_flop (3 split products x 2 GEMMs on padded "
+                        "tiles). The tensor pipe is not this kernel's limit: the fused Mueller/PSD "
+                        "epilogue is (latency-bound FP32 work of 8 warps)"}
+    return kernels, roof
+
+
 class Clocks(object):
     """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
 
@@ -316,72 +413,12 @@ def main():
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws, device="cuda:%d" % dev)
     e2e_value = replica_value(counts["instances"], ws, n_done, e2e_s)
 
-    # ---- roofline of the dominant kernel (FP64 pipe) ----
-    top = max(ktimes.items(), key=lambda kv: kv[1][1]) if ktimes else (None, (0, 0.0))
-    nang, nbin = counts["nang"], counts["nbin"]
-    coef_flop = 12.0 * counts["sum_nmx"] + 89.0 * counts["sum_nmax"]
-    flops = {
-        # S+/S- sums (4 DFMA per order and angle), Mueller elements (14 flop),
-        # number-weighted accumulation (4 FMA per bin)
-        "k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * counts["instances"]) * nang,
-        # D_n steps (12 flop), a_n/b_n and efficiency sums (89 flop per order)
-        "k_tab_coeffs": coef_flop,
-        # the extended-precision part of the mixed recurrences as FP64 flop of the
-        # same algorithm: 15 per warm-up D_n step, 32 per order (D_n, its
-        # reciprocal, Re of the a_n/b_n numerators and denominators); run as
-        # FP32 pairs (double-float), not on the FP64 pipe
-        "k_tab_coeffs_mixed": 15.0 * counts["sum_warm"] + 32.0 * counts["sum_nmax"],
-    }
-    on_fp64_pipe = {"k_tab_s12_plain", "k_tab_coeffs"}
+    # ---- roofline of the dominant kernel ----
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         peaks = {"bf16_tflops": 1900.0, "hbm_gbs": 6800.0, "fallback": True}
-
-    def kernel_table(kt):
-        out = {}
-        tot = max(1e-9, sum(v[1] for v in kt.values()))
-        for name, (nl_, tms) in kt.items():
-            out[name] = {"launches": nl_, "ms_per_launch": tms / max(nl_, 1), "share": tms / tot}
-            if name in flops:
-                key = "fp64_gflops" if name in on_fp64_pipe else "fp64_equivalent_gflops_as_fp32_pairs"
-                out[name][key] = flops[name] / (tms / nl_ * 1e-3) / 1e9
-        return out
-    kernels = kernel_table(ktimes)
-    roof = None
-    if top[0] in on_fp64_pipe:
-        nl_, tms = top[1]
-        ach = flops[top[0]] / (tms / nl_ * 1e-3) / 1e9
-        tb = NCU_BYTES_PER_UNIT.get(top[0])
-        roof = {"bound": "fp64", "kernel": top[0], "achieved": ach, "peak": fp64_peak, "unit": "GFLOP/s",
-                "frac": ach / fp64_peak, "traffic": tb * counts["units"] if tb else None,
-                "traffic_unit": "bytes per launch (ncu capture scaled by units)",
-                "peak_source": "DFMA throughput measured in this run (gbmie_measure_fp64_peak); "
-                               "MEASURED_PEAKS.json has no FP64 figure",
-                "algorithmic_flop_per_launch": flops[top[0]]}
-    # tensor-core contraction: executed MMA flop (3 split products x 2 GEMMs,
-    # padded K and N) and algorithmic flop (8 per order and angle, S+/S- form)
-    if "k_tab_s12_tc" in ktimes:
-        nl_, tms = ktimes["k_tab_s12_tc"]
-        sec = tms / nl_ * 1e-3
-        alg = 8.0 * counts["sum_nmax"] * nang
-        # 6 MMAs (M 128 angles x N 64 (32 sizes, Re/Im) x K 16) per 16-order chunk
-        # of a half tile, per 128-angle block
-        exe = counts["sum_kc16_half"] * 6 * 2 * 128 * 64 * 16 * (-(-nang // 128))
-        kernels["k_tab_s12_tc"]["algorithmic_tflops"] = alg / sec / 1e12
-        kernels["k_tab_s12_tc"]["executed_mma_tflops"] = exe / sec / 1e12
-        kernels["k_tab_s12_tc"]["tensor_peak_tflops"] = peaks.get("bf16_tflops")
-        if top[0] == "k_tab_s12_tc":
-            roof = {"bound": "tensor", "kernel": "k_tab_s12_tc", "achieved": exe / sec / 1e12,
-                    "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-                    "frac": exe / sec / 1e12 / peaks.get("bf16_tflops"),
-                    "traffic": NCU_BYTES_PER_UNIT["k_tab_s12_tc"] * counts["units"],
-                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
-                    "algorithmic_flop_per_launch": alg, "executed_mma_flop_per_launch": exe,
-                    "note": "executed = 3 split products x 2 GEMMs on padded tiles; algorithmic = 8 flop "
-                            "per (order, angle) of the S+/S- sums; the tensor pipe is not this kernel's "
-                            "limit: the fused Mueller/PSD epilogue is (latency-bound FP32 work of 8 "
-                            "warps, about 1400 of its ~3300 cycles per 32-size item in the packed FMAs)"}
+    kernels, roof = roofline_of(ktimes, counts, peaks, fp64_peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and not args.small:
@@ -404,7 +441,7 @@ def main():
                          "plain_fp64": ms_plain / args.steps},
         "mixed_vs_plain_speedup": ms_plain / ms,
         "plain_fp64": {"value": replica_value(counts["instances"], ws, args.steps, ms_plain * 1e-3), "unit": UNIT,
-                       "kernels": kernel_table(kt_plain)},
+                       "kernels": roofline_of(kt_plain, counts, peaks, fp64_peak)[0]},
         "accuracy_mixed_vs_fp64": acc,
         "roofline": roof,
         "kernels": kernels,
