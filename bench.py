@@ -233,7 +233,8 @@ def roofline_of(ktimes, counts, peaks, fp64_peak):
                 "peak": peak, "unit": "TFLOP/s", "frac": alg[top] / sec / 1e12 / peak,
                 "traffic": NCU_BYTES_PER_UNIT[top] * counts["units"],
                 "traffic_unit": "bytes per launch (ncu capture scaled by units)",
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                "peak_source": ("fallback bf16 burst figure (MEASURED_PEAKS.json absent), of fallback"
+                                if peaks.get("fallback") else "MEASURED_PEAKS.json bf16_tflops (burst), of measured"),
                 "algorithmic_flop_per_launch": alg[top], "executed_mma_flop_per_launch": exe[top],
                 "executed_frac": exe[top] / sec / 1e12 / peak,
                 "note": "achieved = the angular sums' algorithmic flop (16 per order and angle); the "

@@ -59,5 +59,13 @@ def test_plain_roofline_is_fp64_pipe(counts):
     assert kernels["k_tab_coeffs"]["algorithmic_gflops"] == pytest.approx(w / 5e-3 / 1e9)
 
 
+def test_fallback_peak_is_named(counts):
+    kt = {"k_tab_s12_tc": (1, 1.0)}
+    _, roof = bench.roofline_of(kt, counts, {"bf16_tflops": 1900.0, "fallback": True}, 3000.0)
+    assert "of fallback" in roof["peak_source"] and roof["peak"] == 1900.0
+    _, roof = bench.roofline_of(kt, counts, PEAKS, 3000.0)
+    assert "of measured" in roof["peak_source"]
+
+
 def test_no_kernels_no_roofline(counts):
     assert bench.roofline_of({}, counts, PEAKS, 3000.0) == ({}, None)
