@@ -455,6 +455,28 @@ def gen_hydrophobic(ref_src):
     print("hydrophobic: %d arrays" % len(out))
 
 
+def gen_growth(ref_src):
+    """growth_su.npz: the reference's CARMA sulfate growth (carma_utils.py:
+    wtpct :136-188, dens :190-243, grow_v75 :245-314) over 7 RH x 6 dry radii
+    x 3 temperatures (126 cases)."""
+    sys.path.insert(0, os.path.join(ref_src, "geosmie"))
+    import carma_utils as cu
+    rh = np.array([0.01, 0.2, 0.5, 0.8, 0.9, 0.95, 0.99])
+    rd = np.array([5e-9, 2e-8, 6.95e-8, 2e-7, 1e-6, 5e-6])
+    temp = np.array([200.0, 220.0, 273.0])
+    ratio = np.empty((rh.size, rd.size, temp.size))
+    wt = np.empty((rh.size, temp.size))
+    de = np.empty((rh.size, temp.size))
+    for i, h in enumerate(rh):
+        for k, t in enumerate(temp):
+            wt[i, k] = cu.wtpct(float(h), temp=float(t))
+            de[i, k] = cu.dens(float(h), temp=float(t))
+            for j, r in enumerate(rd):
+                ratio[i, j, k] = cu.grow_v75(float(h), float(r), temp=float(t))
+    np.savez(os.path.join(HERE, "growth_su.npz"), rh=rh, rd=rd, temp=temp, ratio=ratio, wtpct=wt, dens=de)
+    print("growth_su: %d cases" % ratio.size)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -465,7 +487,8 @@ def main():
     sys.path.insert(0, os.path.join(src, "pymiecoated"))
     sys.path.insert(0, os.path.join(src, "geosmie"))
     from pymiecoated import mie_coated
-    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables", "bands", "hydrophobic"]
+    sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables", "bands", "hydrophobic",
+                                             "growth"]
     if "single" in sel:
         gen_single(mie_coated)
     if "coated" in sel:
@@ -476,6 +499,8 @@ def main():
         gen_tables(src, Dataset)
     if "bands" in sel:
         gen_bands(src, Dataset)
+    if "growth" in sel:
+        gen_growth(src)
     if "hydrophobic" in sel:
         sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
         gen_hydrophobic(src)
