@@ -80,7 +80,10 @@ def initialize_xarr(params, radind, minlam, maxlam):
 
 
 def humidity_growth(rhdep, siz0, rh, allrh):
-    """Humidified size, particleparams.py:85-108 ('simple'/'trivial', 'ss')."""
+    """Humidified size, particleparams.py:85-108 ('simple'/'trivial', 'ss',
+    'su').  For 'su' the CARMA sulfate law (carma_utils.py:245-314) is taken
+    from geosmie_gb300.growth, which tests/test_growth.py pins bit for bit
+    to the reference's own wtpct, dens and grow_v75."""
     rhi = list(allrh).index(rh)
     rhtype = rhdep["type"]
     rhp = rhdep["params"]
@@ -92,6 +95,11 @@ def humidity_growth(rhdep, siz0, rh, allrh):
             return siz0
         c1, c2, c3, c4 = rhp["c1"], rhp["c2"], rhp["c3"], rhp["c4"]
         return (c1 * siz ** c2 / (c3 * siz ** c4 - np.log10(rh)) + siz ** 3.0) ** (1.0 / 3.0) / 100.0
+    if rhtype == "su":
+        if rh == 0.0:
+            return siz0
+        from geosmie_gb300 import growth
+        return siz0 * float(growth.grow_v75(rh, siz0, temp=rhp["temp"]))
     raise NotImplementedError("growth type %s is outside the restated path" % rhtype)
 
 
@@ -107,7 +115,8 @@ def lognorm_psd(rmode, sigma, xx, lambd, rmax, rmin):
 
 
 def humid_refractive_index(params, radind, rhi, rh, nref0, nrefwater):
-    """Growth factor and volume-mixed index, dointegration.py:493-536 (:505)."""
+    """Growth factor and volume-mixed index, dointegration.py:493-536 (:505);
+    'simple', 'trivial', 'ss' and 'su'."""
     rtype = params["rhDep"]["type"]
     if rtype == "simple" or (rtype == "trivial" and rhi == 0):
         gf = params["rhDep"]["params"]["gf"][rhi]
@@ -118,6 +127,11 @@ def humid_refractive_index(params, radind, rhi, rh, nref0, nrefwater):
             rminmaj = pparam["rMinMaj"][radind]
         except KeyError:
             rminmaj = pparam["rmin0"][radind][0]
+        rminuse = humidity_growth(params["rhDep"], rminmaj, rh[rhi], rh)
+        rrat = rminmaj / rminuse
+        gf = 1.0 / rrat
+    elif rtype == "su":   # the first mode's lower radius (dointegration.py:522-528)
+        rminmaj = params["psd"]["params"]["rmin0"][radind][0]
         rminuse = humidity_growth(params["rhDep"], rminmaj, rh[rhi], rh)
         rrat = rminmaj / rminuse
         gf = 1.0 / rrat

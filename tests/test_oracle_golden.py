@@ -98,7 +98,7 @@ def test_size_range_fixture():
     assert np.max(np.abs(s1 - g["s1"]) / np.max(np.abs(g["s1"]), axis=1, keepdims=True)) < 1e-12
 
 
-@pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt"])
+@pytest.mark.parametrize("name", ["lognorm", "trivial", "seasalt", "su"])
 def test_table_fixture(name):
     g = load_golden("table_%s.npz" % name)
     params = json.loads(str(g["params_json"]))
