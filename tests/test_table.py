@@ -66,9 +66,11 @@ def test_bin_spec_host_fields_match_reference_cpu(name):
 def test_host_grid_and_weights_match_oracle_cpu(name):
     """The size-parameter grid and its widths (initializeXarr,
     dointegration.py:425-463) equal the oracle's bit for bit (the oracle's
-    grid equals the reference's own on these definitions); the Gong sea-salt
-    weights (dointegration.py:585-624), which the table driver passes to the
-    GPU as explicit weights, agree to the last bits."""
+    grid equals the reference's own on these definitions).  The weights the
+    table driver passes to the GPU explicitly agree with the oracle's: the
+    lognormal modes grown by the CARMA 'su' law (dointegration.py:549-583) bit
+    for bit, the Gong sea-salt weights (dointegration.py:585-624) to the last
+    bits."""
     from geosmie_gb300 import table
     from oracle import integration as oi
     g = load_golden("table_%s.npz" % name)
@@ -80,6 +82,14 @@ def test_host_grid_and_weights_match_oracle_cpu(name):
         xo, dxo = oi.initialize_xarr(params, b, lam[0], lam[-1])
         np.testing.assert_array_equal(x, xo)
         np.testing.assert_array_equal(dx, dxo)
+        if params["psd"]["type"] == "lognorm" and params["rhDep"]["type"] == "su":
+            # CARMA growth of every mode radius at its own dry size: host weights
+            w = table._lognorm_weights(params, b, rh, x, dx, lam)
+            for li, l_ in enumerate(lam):
+                for ri, r in enumerate(rh):
+                    ref = oi.calculate_psd(params, b, r, rh, xo, dxo, None, l_)[0]
+                    for k in range(len(ref)):
+                        np.testing.assert_array_equal(w[li, ri, k], ref[k])
         if params["psd"]["type"] != "ss":
             continue
         w = table._ss_weights(params, b, rh, x, lam)
