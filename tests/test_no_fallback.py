@@ -51,3 +51,25 @@ def test_package_never_imports_the_oracle():
                 elif isinstance(node, ast.ImportFrom):
                     names = [node.module or ""]
                 assert not any(n == "oracle" or n.startswith("oracle.") for n in names), (f, names)
+
+
+def test_bench_uses_the_oracle_only_in_its_cpu_legs():
+    """bench.py reaches the oracle only from the CPU baseline and the
+    reference arm (_oracle_unit, cpu_sample, run_reference)."""
+    tree = ast.parse(open(os.path.join(ROOT, "bench.py")).read())
+    allowed = {"_oracle_unit", "cpu_sample", "run_reference"}
+    seen = []
+
+    def visit(node, fn):
+        for child in ast.iter_child_nodes(node):
+            name = child.name if isinstance(child, ast.FunctionDef) else fn
+            mods = []
+            if isinstance(child, ast.Import):
+                mods = [a.name for a in child.names]
+            elif isinstance(child, ast.ImportFrom):
+                mods = [child.module or ""]
+            if any(m == "oracle" or m.startswith("oracle.") for m in mods):
+                seen.append(fn)
+            visit(child, name)
+    visit(tree, None)
+    assert seen and set(seen) <= allowed, seen
