@@ -32,3 +32,20 @@ def test_status_strings_without_gpu():
     lib.gbmie_status_string.restype = ctypes.c_char_p
     assert lib.gbmie_status_string(0) == b"ok"
     assert b"invalid" in lib.gbmie_status_string(1)
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/gbmie.h compiles as strict C99 and as C++17 (what a cgo, JNI
+    or ctypes binding includes), with no warnings."""
+    import shutil
+    import subprocess
+    import pytest
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "gbmie.h"\nint main(void) { return 0; }\n')
+    inc = os.path.join(ROOT, "include")
+    for cc, flags in (("gcc", ["-std=c99", "-pedantic"]), ("g++", ["-std=c++17", "-x", "c++"])):
+        if shutil.which(cc) is None:
+            pytest.skip("%s not found" % cc)
+        r = subprocess.run([cc] + flags + ["-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc, str(src)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, (cc, r.stderr)
