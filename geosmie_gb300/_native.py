@@ -48,6 +48,7 @@ SIGNATURES = {
     "gbmie_pitau": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _P]),
     "gbmie_s12": (ctypes.c_int, [_P, _I64, _P, _P, _P, _I32, _P, _P, _P]),
     "gbmie_size_range": (ctypes.c_int, [_P, _I64, _P, _D, _D, _I32, _P, _P, _P, _P]),
+    "gbmie_s12_pt": (ctypes.c_int, [_P, _I64, _P, _P, _P, _I32, _I32, _P, _P, _P, _P]),
     "gbmie_s12_noalloc": (ctypes.c_int, [_P, _I64, _P, _P, _P, _I32, _I32, _P, _P, _P]),
     "gbmie_table_plan_create": (ctypes.c_int, [_P, _P, ctypes.POINTER(_P), ctypes.POINTER(_I64)]),
     "gbmie_table_plan_destroy": (ctypes.c_int, [_P]),

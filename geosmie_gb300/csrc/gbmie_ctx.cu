@@ -279,7 +279,9 @@ int gbmie_ctx_synchronize(gbmie_ctx *ctx)
         cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), ctx->stream);
         cudaStreamSynchronize(ctx->stream);
         if (f & GBMIE_FLAG_TIMEOUT) return ctx_fail(ctx, GBMIE_ERR_TIMEOUT, "device wait hit its iteration limit");
-        if (f & GBMIE_FLAG_NMAX) return ctx_fail(ctx, GBMIE_ERR_NMAX, "nmax above %d", GBMIE_MAX_NMAX);
+        if (f & GBMIE_FLAG_NMAX)
+            return ctx_fail(ctx, GBMIE_ERR_NMAX, "an instance needs more partial waves than the call allows "
+                                                 "(GBMIE_MAX_NMAX = %d, or the given row length)", GBMIE_MAX_NMAX);
         return ctx_fail(ctx, GBMIE_ERR_INVALID, "invalid instance parameters (x < 0, y < x, NaN, "
                                                "or coated with mu != 1)");
     }

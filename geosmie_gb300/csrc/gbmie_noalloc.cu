@@ -1,10 +1,11 @@
 // gbmie_s12_noalloc: S1/S2 from Mie coefficients without any device
 // allocation, for callers that cannot call cudaMalloc -- code that runs
 // inside another framework's memory pool or allocator-owned region (which
-// forbids foreign cudaMalloc/cudaFree), code recorded into a CUDA graph by
-// someone else, and embedded callers that must not grow the device footprint
-// after start-up.  They pass their own inputs and outputs; the only other
-// device memory used is the fixed array below.
+// forbids foreign cudaMalloc/cudaFree), and embedded callers that must not
+// grow the device footprint after start-up.  They pass their own inputs and
+// outputs; the only other device memory used is the fixed array below.  The
+// call returns after its stream has finished (it reads the status word back
+// into host memory).
 //
 // The angular table (pi~_n + tau~_n, pi~_n - tau~_n) lives in the
 // file-scope array g_noalloc_pq of GBMIE_NOALLOC_PQ_BYTES (4 MiB), which

@@ -176,6 +176,67 @@ extern "C" int gbmie_s12(gbmie_ctx *ctx, int64_t n, const int64_t *offsets, cons
                           (double2 *)s1, (double2 *)s2);
 }
 
+// S1, S2 from caller-supplied pi~/tau~ rows (mie_props.py:115-149): one warp
+// per (instance, angle), lanes over orders, FP64 sums reduced across the warp.
+// An instance with more orders than a row holds is flagged and skipped.
+__global__ void k_s12_pt(int64_t n, const int64_t *__restrict__ off, const double2 *__restrict__ an,
+                         const double2 *__restrict__ bn, int nang, int ld, const double *__restrict__ pin,
+                         const double *__restrict__ tin, double2 *__restrict__ s1, double2 *__restrict__ s2,
+                         int *__restrict__ flags)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarp = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n * nang; w += nwarp) {
+        const int64_t i = w / nang;
+        const int a = (int)(w - i * nang);
+        const int64_t o = off[i];
+        const int64_t nm = off[i + 1] - o;
+        if (nm < 0 || nm > ld) {
+            if (lane == 0) atomicOr(flags, GBMIE_FLAG_NMAX);
+            continue;   // uniform across the warp
+        }
+        const double *pr = pin + (int64_t)a * ld, *tr = tin + (int64_t)a * ld;
+        double r1 = 0.0, i1 = 0.0, r2 = 0.0, i2 = 0.0;
+        for (int64_t k = lane; k < nm; k += 32) {
+            const double2 av = an[o + k], bv = bn[o + k];
+            const double p = pr[k], t = tr[k];
+            r1 = fma(av.x, p, fma(bv.x, t, r1));
+            i1 = fma(av.y, p, fma(bv.y, t, i1));
+            r2 = fma(av.x, t, fma(bv.x, p, r2));
+            i2 = fma(av.y, t, fma(bv.y, p, i2));
+        }
+        for (int m = 16; m > 0; m >>= 1) {
+            r1 += __shfl_xor_sync(0xffffffffu, r1, m);
+            i1 += __shfl_xor_sync(0xffffffffu, i1, m);
+            r2 += __shfl_xor_sync(0xffffffffu, r2, m);
+            i2 += __shfl_xor_sync(0xffffffffu, i2, m);
+        }
+        if (lane == 0) {
+            s1[i * nang + a] = make_double2(r1, i1);
+            s2[i * nang + a] = make_double2(r2, i2);
+        }
+    }
+}
+
+extern "C" int gbmie_s12_pt(gbmie_ctx *ctx, int64_t n, const int64_t *offsets, const gbmie_complex *an,
+                            const gbmie_complex *bn, int32_t nang, int32_t ld, const double *pi_rows,
+                            const double *tau_rows, gbmie_complex *s1, gbmie_complex *s2)
+{
+    if (!ctx) return GBMIE_ERR_INVALID;
+    if (n < 0 || nang < 0 || ld < 1 ||
+        (n > 0 && nang > 0 && (!offsets || !an || !bn || !pi_rows || !tau_rows || !s1 || !s2)))
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "gbmie_s12_pt: bad arguments");
+    if (n == 0 || nang == 0) return GBMIE_OK;
+    cudaSetDevice(ctx->device);
+    const int64_t warps = n * nang;
+    const int64_t blocks = ceil_div64(warps, 8);
+    ctx_pre_launch(ctx);
+    k_s12_pt<<<(unsigned)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, ctx->stream>>>(
+        n, offsets, (const double2 *)an, (const double2 *)bn, nang, ld, pi_rows, tau_rows, (double2 *)s1,
+        (double2 *)s2, ctx->d_flags);
+    return ctx_check_launch(ctx, "k_s12_pt");
+}
+
 int launch_coeffs_uniform(gbmie_ctx *ctx, int64_t n, const double *x, double2 eps, const int64_t *off,
                           double2 *an, double2 *bn, double *eff);
 

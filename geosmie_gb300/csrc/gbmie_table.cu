@@ -327,10 +327,10 @@ struct KSum {
     __device__ __forceinline__ double val() const { return (double)s - (double)c; }
 };
 
-// (FP32 sums: at most 128 registers, two blocks per SM; the FP64 form keeps
-// its registers)
+// (launch bounds match the launches: 64 threads for the FP32 sums of the
+// mixed path, 256 for the FP64 sums)
 template <int NB, typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_tab_scalars(TabView v)
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 64 : 256) k_tab_scalars(TabView v)
 {
     __shared__ double sR[NB][15];
     __shared__ double sRed[8][NB * 9];

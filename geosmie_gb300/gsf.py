@@ -39,14 +39,22 @@ def expand(ang_deg, F, nnodes=129, precision=_native.GBMIE_PLAIN_FP64, device=0)
     return coef.cpu().numpy(), cnorm.cpu().numpy()
 
 
+def pygeos_pmom(coef, num_expand=129):
+    """pmom[..., p, m] from expansion coefficients [..., 6, L] in
+    spher_expan's order (alpha1 alpha2 alpha3 alpha4 beta1 beta2): the output
+    remap [0, 4, 2, 5, 1, 3] of convertncdf.py:381-394 (p order P11 P12 P33
+    P34 P22 P44) and the zero padding (or truncation) to num_expand moments."""
+    coef = np.asarray(coef, np.float64)
+    pmom = np.zeros(coef.shape[:-2] + (6, num_expand))
+    n = min(num_expand, coef.shape[-1])
+    for ii, npol in enumerate(PYGEOS_REMAP):
+        pmom[..., npol, :n] = coef[..., ii, :n]
+    return pmom
+
+
 def pmom_from_table(table, ang_deg, num_expand=129, nnodes=129, device=0):
     """pmom[bin, wavelength, rh, p, m] of a table (rungsf, pygeos mode)."""
     F = np.stack([table[k] for k in ELEMENTS_IN], axis=3)   # [bin, wl, rh, 6, nang]
     shp = F.shape
     coef, _ = expand(ang_deg, F.reshape(-1, 6, shp[-1]), nnodes, device=device)
-    coef = coef.reshape(shp[0], shp[1], shp[2], 6, nnodes)
-    pmom = np.zeros(shp[:3] + (6, num_expand))
-    n = min(num_expand, nnodes)
-    for ii, npol in enumerate(PYGEOS_REMAP):
-        pmom[:, :, :, npol, :n] = coef[:, :, :, ii, :n]
-    return pmom
+    return pygeos_pmom(coef.reshape(shp[0], shp[1], shp[2], 6, nnodes), num_expand)

@@ -104,6 +104,50 @@ def s12(off, an, bn, cos_theta, device=0):
     return s1, s2
 
 
+def pitau(cos_theta, nmax, device=0):
+    """Scaled angular functions pi~_n, tau~_n [nang, nmax] (CUDA float64) at
+    the given cosines (pymiecoated/mie_props.py:166-231, the rows of
+    MultipleMie.preCalculatePT, mie_coated.py:160-179)."""
+    ctx = _native.context(device)
+    cost = _dev(np.atleast_1d(np.asarray(cos_theta, np.float64)), torch.float64, ctx.device)
+    nmax = max(int(nmax), 2)
+    pin = torch.empty((cost.numel(), nmax), dtype=torch.float64, device=ctx.device)
+    tin = torch.empty_like(pin)
+    ctx.call("gbmie_pitau", _native._I32(cost.numel()), _native.ptr(cost), _native._I32(nmax), _native.ptr(pin),
+             _native.ptr(tin))
+    ctx.sync()
+    return pin, tin
+
+
+def s12_pt(off, an, bn, pin, tin, device=0):
+    """S1, S2 [n, nang] complex128 (CUDA) from CSR coefficients and
+    caller-supplied scaled pi~/tau~ rows [nang, ld] with ld >= every
+    instance's nmax (mie_props.py:115-149); ValueError if a row is shorter
+    than an instance's nmax."""
+    ctx = _native.context(device)
+    dv = ctx.device
+    pin = torch.as_tensor(np.asarray(pin, np.float64) if not torch.is_tensor(pin) else pin,
+                          dtype=torch.float64).to(dv)
+    tin = torch.as_tensor(np.asarray(tin, np.float64) if not torch.is_tensor(tin) else tin,
+                          dtype=torch.float64).to(dv)
+    if pin.dim() == 1:
+        pin = pin[None, :]
+        tin = tin[None, :]
+    if pin.shape != tin.shape:
+        raise ValueError("pin and tin must have the same shape")
+    pin = pin.contiguous()
+    tin = tin.contiguous()
+    n = off.numel() - 1
+    nang, ld = pin.shape
+    s1 = torch.empty((n, nang), dtype=torch.complex128, device=dv)
+    s2 = torch.empty_like(s1)
+    ctx.call("gbmie_s12_pt", _native._I64(n), _native.ptr(off), _native.ptr(an), _native.ptr(bn),
+             _native._I32(nang), _native._I32(ld), _native.ptr(pin), _native.ptr(tin), _native.ptr(s1),
+             _native.ptr(s2))
+    ctx.sync()
+    return s1, s2
+
+
 class MieScatterProps(object):
     """Coefficients of one parameter set and their properties
     (pymiecoated/mie_coated.py:181-211)."""
@@ -140,18 +184,11 @@ class MieScatterProps(object):
         return complex(s1[0, 0].item()), complex(s2[0, 0].item())
 
     def S12_pt(self, pin, tin):
-        """S1, S2 from caller-supplied scaled pi/tau arrays (mie_props.py:116-117).
-
-        The sums run on the device: the caller's arrays are copied up and
-        combined with the device-resident coefficients in FP64.
-        """
-        pin = torch.as_tensor(np.asarray(pin, np.float64), device=self.an.device)
-        tin = torch.as_tensor(np.asarray(tin, np.float64), device=self.an.device)
-        k = self.nmax
-        a, b = self.an[:k], self.bn[:k]
-        s1 = (a * pin[:k]).sum() + (b * tin[:k]).sum()
-        s2 = (a * tin[:k]).sum() + (b * pin[:k]).sum()
-        return complex(s1.item()), complex(s2.item())
+        """S1, S2 from caller-supplied scaled pi/tau arrays of at least nmax
+        entries (mie_props.py:115-117), summed on the device by
+        gbmie_s12_pt."""
+        s1, s2 = s12_pt(self.off, self.an, self.bn, pin, tin, self.device)
+        return complex(s1[0, 0].item()), complex(s2[0, 0].item())
 
 
 class Mie(object):
@@ -307,6 +344,35 @@ class MultipleMie(object):
         ctx = _native.context(self.device)
         self._dx = _dev(self.xArr, torch.float64, ctx.device)
         self._dcost = _dev(self.costarr, torch.float64, ctx.device)
+
+    def calculateS12(self, xx, eps, mu, jvarr=(), yvarr=()):
+        """(S1, S2) at every cosine of costarr for one size parameter xx and
+        permittivity/permeability eps, mu (mie_coated.py:51-53): a [nang, 2]
+        complex array whose row k unpacks as (S1, S2).  jvarr/yvarr are
+        accepted and ignored (Bessel functions are computed on the device)."""
+        off, an, bn, _ = coefficients([float(xx)], complex(eps), None if mu is None else complex(mu),
+                                      device=self.device, with_eff=False)
+        s1, s2 = s12(off, an, bn, self.costarr, self.device)
+        return np.stack([s1[0].cpu().numpy(), s2[0].cpu().numpy()], axis=-1)
+
+    def calculateS12WithParams(self, xx, jvarr, yvarr, params):
+        """(S1, S2) at every cosine of costarr from given coefficients
+        params = (an, bn, nmax), as returned by pymiecoated's
+        single_mie_coeff_numba (mie_coated.py:55-59): the scaled pi/tau rows
+        of nmax at costarr (the reference's parr/tarr) are built on the
+        device and the sums run there (gbmie_s12_pt)."""
+        an, bn, nmax = params
+        nmax = int(nmax)
+        an = np.asarray(an, np.complex128)[:nmax]
+        bn = np.asarray(bn, np.complex128)[:nmax]
+        if an.size != nmax or bn.size != nmax:
+            raise ValueError("params must hold nmax coefficients a_n and b_n")
+        dv = _native.context(self.device).device
+        off = torch.tensor([0, nmax], dtype=torch.int64, device=dv)
+        pin, tin = pitau(self.costarr, nmax, self.device)
+        s1, s2 = s12_pt(off, _dev(an, torch.complex128, dv), _dev(bn, torch.complex128, dv), pin, tin,
+                        self.device)
+        return np.stack([s1[0].cpu().numpy(), s2[0].cpu().numpy()], axis=-1)
 
     def calculateS12SizeRange(self, mr, mi):
         """S1/S2 at every cosine and the six efficiencies for every size,

@@ -119,6 +119,21 @@ def seasalt_large(n_lambda=20, n_radii=4000, n_nodes=4000, n_moments=1000):
     return spec, desc, n_moments, n_nodes
 
 
+def gsf_smooth(n_nodes=64):
+    """Small particles (x <= 1.8, nmax <= 10) on n_nodes Gauss-node angles:
+    2 wavelengths x 2 RH x 1 lognormal bin x 120 radii 0.01-0.15 um,
+    m = 1.45 + 0.01i.  S1/S2 are polynomials of degree <= nmax in cos(theta),
+    so the phase matrix is a polynomial of degree <= 20 and an expansion in
+    n_nodes >= 21 generalized spherical functions on n_nodes Gauss nodes
+    reproduces it to rounding: the workload on which the expansion can be
+    checked against a reconstruction."""
+    lam = np.array([0.55e-6, 1.02e-6])
+    r = np.logspace(np.log10(0.01e-6), np.log10(0.15e-6), 120)
+    m = np.full((2, 2, 1), 1.45 + 0.01j)
+    spec = _lognormal_spec(lam, r, m, [1.0, 1.15], [0.05e-6], 1.8, 1700.0, gauss_angles(n_nodes))
+    return spec, "smooth small-particle table on %d Gauss nodes" % n_nodes
+
+
 def coated_bc(n_lambda=30, n_radii=2000, n_rh=20, n_frac=10, nang=181):
     """Black-carbon core in an organic shell swollen by humidity.
 

@@ -118,10 +118,24 @@ int gbmie_s12(gbmie_ctx *ctx, int64_t n, const int64_t *offsets,
               const gbmie_complex *an, const gbmie_complex *bn, int32_t nang,
               const double *cos_theta, gbmie_complex *s1, gbmie_complex *s2);
 
-/* gbmie_s12 for callers that cannot allocate device memory (code running in
- * another framework's memory pool, or recorded into someone else's CUDA
- * graph, or that must not grow the device footprint after start-up).  No
- * counterpart in the reference.  Allocates nothing: no context, no scratch;
+/* Amplitude functions S1, S2 [n][nang] of n instances from their
+ * coefficients (CSR by offsets) and caller-supplied scaled angular functions
+ * pi~_n, tau~_n (times (2n+1)/(n(n+1))) given as rows pi[nang][ld],
+ * tau[nang][ld], order n at column n-1; every instance's nmax must be <= ld
+ * (else GBMIE_ERR_NMAX).  S1 = sum a_n pi~_n + b_n tau~_n, S2 = sum a_n
+ * tau~_n + b_n pi~_n over the instance's own orders.  Replaces
+ * pymiecoated/mie_props.py:115-149 (mie_S12_pt, Mie.S12_pt) and
+ * mie_coated.py:51-59 (MultipleMie.calculateS12WithParams over its
+ * precomputed parr/tarr rows).  Allocates nothing. */
+int gbmie_s12_pt(gbmie_ctx *ctx, int64_t n, const int64_t *offsets, const gbmie_complex *an,
+                 const gbmie_complex *bn, int32_t nang, int32_t ld, const double *pi_rows,
+                 const double *tau_rows, gbmie_complex *s1, gbmie_complex *s2);
+
+/* gbmie_s12 for callers that cannot allocate device memory: code running
+ * inside another framework's memory pool or allocator-owned region (which
+ * forbids foreign cudaMalloc/cudaFree), and embedded callers that must not
+ * grow the device footprint after start-up.  No counterpart in the
+ * reference.  Allocates nothing: no context, no scratch;
  * the angular table lives in a fixed 4 MiB device array inside the library
  * (held by every GPU that loads it until exit), so nmax_max * nang must not
  * exceed 262144 (e.g. nmax 700 with 371 angles), else GBMIE_ERR_CAPACITY.
@@ -174,9 +188,9 @@ typedef struct {
     int32_t grid_kind;          /* GBMIE_GRID_* */
     int32_t psd_kind;           /* GBMIE_PSD_* */
     int32_t precision;          /* GBMIE_PLAIN_FP64 or GBMIE_MIXED */
-    int32_t n_gsf;              /* moments of the GSF expansion (reference
-                                   129 = its Gauss node count); 0 = none
-                                   (reference 129); 0 = no expansion */
+    int32_t n_gsf;              /* moments of the GSF expansion; the
+                                   reference keeps 129 (its Gauss node
+                                   count); 0 = no expansion */
     const double *lambda;       /* [n_lambda] m */
     const double *grid;         /* [n_size] ascending, see grid_kind */
     const double *dgrid;        /* [n_size] PSD widths (drarr), same unit */

@@ -2,7 +2,9 @@
 
 Run in a container where the GEOSmie sources are present:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref /root/reference
+
+(or with the reference tree named by the GEOSMIE_REF environment variable).
 
 It imports the reference's own Python code -- pymiecoated (mie_coated.Mie,
 MultipleMie, mie_coeffs, mie_props) and geosmie/dointegration.fun -- with
@@ -26,6 +28,14 @@ Outputs (small .npz files, committed):
   hydrophobic.npz  hydrophobic.doConversion on the one-bin tables above
                    (table_trivial, table_seasalt), non-legacy and legacy
                    layout, from files laid out by geosmie_gb300.lutfile.
+  gsf_reconstruct.npz  utils/eval_gsfun.py's reconstruction of the phase
+                   matrix (OPTICS.calcP11/P12/P22_P33/P34, d_mn) from the
+                   oracle's pmom of a smooth Gauss-node table; eval_gsfun
+                   imports xarray, replaced by a small named-array stand-in.
+  rungsf_pygeos.npz  gsf/convertncdf.processFileRaw (pygeos mode) on
+                   table_lognorm's reference phase matrix, with a stand-in
+                   ./spher_expan.x (the oracle's C restatement writing the
+                   Fortran program's text layout).
 """
 import argparse
 import contextlib
@@ -477,18 +487,247 @@ def gen_growth(ref_src):
     print("growth_su: %d cases" % ratio.size)
 
 
+# --------------------------------------------------------------------------
+# GSF pins: the reference's own reconstruction (utils/eval_gsfun.py) and its
+# own rungsf glue (gsf/convertncdf.py processFileRaw, pygeos mode)
+# --------------------------------------------------------------------------
+class _DA(object):
+    """The few xarray.DataArray features eval_gsfun's reconstructions use
+    (named dimensions, isel, dict indexing, name-aligned arithmetic,
+    ufuncs); eval_gsfun imports xarray, which this image lacks."""
+
+    def __init__(self, data=None, dims=(), coords=None):
+        self.dims = tuple(dims)
+        if data is None:
+            shape = tuple(np.asarray(getattr(coords[d], "data", coords[d])).size for d in self.dims)
+            data = np.full(shape, np.nan)
+        self.data = np.array(data, dtype=np.float64)
+
+    @property
+    def values(self):
+        return self.data
+
+    @property
+    def sizes(self):
+        return dict(zip(self.dims, self.data.shape))
+
+    def isel(self, **kw):
+        x, dims = self.data, []
+        ax = 0
+        for d in self.dims:
+            if d in kw and np.ndim(kw[d]) == 0:
+                x = np.take(x, int(kw[d]), axis=ax)
+            else:
+                if d in kw:
+                    x = np.take(x, np.asarray(kw[d]), axis=ax)
+                dims.append(d)
+                ax += 1
+        return _DA(x, dims)
+
+    def _on(self, dims):
+        x = np.transpose(self.data, [self.dims.index(d) for d in dims if d in self.dims])
+        return x.reshape([self.data.shape[self.dims.index(d)] if d in self.dims else 1 for d in dims])
+
+    def _op(self, other, f, swap=False):
+        if isinstance(other, _DA):
+            dims = list(self.dims) + [d for d in other.dims if d not in self.dims]
+            a, b = self._on(dims), other._on(dims)
+            return _DA(f(b, a) if swap else f(a, b), dims)
+        return _DA(f(other, self.data) if swap else f(self.data, other), self.dims)
+
+    def __add__(self, o):
+        return self._op(o, np.add)
+
+    def __radd__(self, o):
+        return self._op(o, np.add, True)
+
+    def __sub__(self, o):
+        return self._op(o, np.subtract)
+
+    def __rsub__(self, o):
+        return self._op(o, np.subtract, True)
+
+    def __mul__(self, o):
+        return self._op(o, np.multiply)
+
+    def __rmul__(self, o):
+        return self._op(o, np.multiply, True)
+
+    def __iadd__(self, o):
+        r = self._op(o, np.add)
+        assert set(r.dims) == set(self.dims)
+        self.data = np.broadcast_to(r._on(self.dims), self.data.shape).copy()
+        return self
+
+    def __getitem__(self, key):
+        return self.isel(**key)
+
+    def __setitem__(self, key, val):
+        if isinstance(key, slice):
+            self.data[key] = val
+            return
+        idx = tuple(key.get(d, slice(None)) for d in self.dims)
+        rest = [d for d in self.dims if d not in key]
+        self.data[idx] = val._on(rest) if isinstance(val, _DA) else val
+
+    def __iter__(self):
+        for v in self.data:
+            yield float(v)
+
+    def __array_ufunc__(self, ufunc, method, *inputs, **kw):
+        dims = next(x.dims for x in inputs if isinstance(x, _DA))
+        args = [x.data if isinstance(x, _DA) else x for x in inputs]
+        return _DA(getattr(ufunc, method)(*args, **kw), dims)
+
+
+def gen_gsf_reconstruct(src):
+    """The reference's own reconstruction of the six phase-matrix elements
+    from pmom (eval_gsfun.OPTICS.calcP11/calcP12/calcP22_P33/calcP34, with
+    its d_mn Wigner recurrences and scipy eval_legendre), applied to the
+    oracle's pmom of a smooth workload whose expansion is exact."""
+    xr = types.ModuleType("xarray")
+    xr.DataArray = _DA
+    sys.modules["xarray"] = xr
+    sys.path.insert(0, os.path.join(src, "utils"))
+    import eval_gsfun
+    root = os.path.dirname(os.path.dirname(HERE))
+    sys.path.insert(0, root)
+    from geosmie_gb300 import workloads
+    from oracle import integration
+    spec, _ = workloads.gsf_smooth()
+    n = spec["ang"].size
+    tab = integration.run_spec(spec, n_gsf=n)
+    pm = tab["pmom"]                                  # [bin, wl, rh, 6, m]
+    nb, nl, nr = pm.shape[:3]
+
+    class _Optics(object):
+        p = _DA([11, 12, 33, 34, 22, 44], ("p",))
+
+        def __getitem__(self, k):
+            return {"pmom": _DA(pm, ("bin", "wavelength", "rh", "p", "m"))}[k]
+    o = eval_gsfun.OPTICS.__new__(eval_gsfun.OPTICS)
+    o.optics = _Optics()
+    o.nMom = n
+    o.theta = _DA(np.radians(spec["ang"]), ("ang",))
+    o.irh, o.ibin, o.iwav = np.arange(nr), np.arange(nb), np.arange(nl)
+    o.dims = ("bin", "wavelength", "rh", "ang")
+    o.coords = {"rh": np.arange(nr), "wavelength": np.arange(nl), "bin": np.arange(nb), "ang": spec["ang"]}
+    o.getPmatrix()
+    out = {"recon_" + k: getattr(o, k).data for k in ["p11", "p12", "p22", "p33", "p34", "p44"]}
+    np.savez(os.path.join(HERE, "gsf_reconstruct.npz"), ang=spec["ang"], pmom=pm,
+             **{"phase_" + k: tab[k] for k in ["p11", "p12", "p22", "p33", "p34", "p44"]}, **out)
+    print("gsf_reconstruct: %d entries x %d nodes" % (nb * nl * nr, n))
+
+
+def gen_rungsf(src):
+    """convertncdf.processFileRaw in pygeos mode (the rungsf pass) on the
+    reference's own lognormal table (table_lognorm.npz), with a stand-in
+    ./spher_expan.x that runs the oracle's C restatement on each text file and
+    writes its .expan_coeff in the Fortran program's layout (a header, then
+    L and AL1 AL2 AL3 AL4 BET1 BET2 at F17.10, spher_expan.f:93-107).  What
+    is recorded is the pmom the reference's glue writes: element remap,
+    zero padding to 129 moments, F17.10 quantisation."""
+    root = os.path.dirname(os.path.dirname(HERE))
+    g = np.load(os.path.join(HERE, "table_lognorm.npz"))
+    nc = types.ModuleType("netCDF4")
+    prepared = {}
+
+    class Var(object):
+        def __init__(self, data, dims):
+            self.data = np.array(data, dtype=np.float64)
+            self.dims = dims
+
+        def __getitem__(self, k):
+            return self.data[k]
+
+        def __setitem__(self, k, v):
+            self.data[k] = v
+
+        def __len__(self):
+            return self.data.shape[0]
+
+        def __setattr__(self, k, v):
+            object.__setattr__(self, k, v)
+
+    class Dataset(object):
+        def __init__(self, path, mode="r"):
+            d = prepared[os.path.basename(path).replace("nomom.", "")]
+            self.dims, self.variables = d
+
+        def createDimension(self, name, size):
+            self.dims[name] = size
+
+        def createVariable(self, name, dtype, dims, **kw):
+            dims = (dims,) if isinstance(dims, str) else tuple(dims)
+            v = Var(np.zeros([self.dims[d] for d in dims]), dims)
+            self.variables[name] = v
+            return v
+
+        def close(self):
+            pass
+    nc.Dataset = Dataset
+    sys.modules["netCDF4"] = nc
+    sys.path.insert(0, os.path.join(src, "gsf"))
+    import convertncdf
+    ang = g["out_ang"]
+    dims = {"rh": g["out_rh"].size, "wavelength": g["out_wavelength"].size, "bin": g["out_bin"].size, "p": 6,
+            "ang": ang.size}
+    vars_ = {"wavelength": Var(g["out_wavelength"], ("wavelength",)), "rh": Var(g["out_rh"], ("rh",)),
+             "bin": Var(g["out_bin"], ("bin",)), "p": Var([11, 12, 33, 34, 22, 44], ("p",)),
+             "ang": Var(ang, ("ang",))}
+    for k in ["p11", "p12", "p22", "p33", "p34", "p44"]:
+        vars_[k] = Var(g["out_" + k], ("bin", "wavelength", "rh", "ang"))
+    name = "integ-lognorm-raw.nomom.nc4"
+    prepared[name.replace("nomom.", "")] = (dims, vars_)
+    old = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:
+        os.chdir(tmp)
+        try:
+            open(name, "w").close()
+            exe = os.path.join(tmp, "spher_expan.x")
+            with open(exe, "w") as fp:
+                fp.write(_SPHER_STANDIN.replace("@PYTHON@", sys.executable).replace("@ROOT@", repr(root)))
+            os.chmod(exe, 0o755)
+            with contextlib.redirect_stdout(io.StringIO()):
+                convertncdf.processFileRaw(name, ".", 0, None, "pygeos", False)
+        finally:
+            os.chdir(old)
+    pmom = vars_["pmom"].data
+    np.savez(os.path.join(HERE, "rungsf_pygeos.npz"), pmom=pmom, ang=ang)
+    print("rungsf_pygeos: pmom %s" % (pmom.shape,))
+
+
+_SPHER_STANDIN = r"""#!@PYTHON@
+# stand-in for spher_expan.x: the oracle's C restatement on one text file,
+# coefficients written in the Fortran program's layout (spher_expan.f:93-107)
+import sys
+sys.path.insert(0, @ROOT@)
+import numpy as np
+from oracle import gsf
+t = np.loadtxt(sys.argv[1])
+coef, cnorm = gsf.expand(t[:, 0], t[:, 1:7].T[None], 129)
+with open(sys.argv[1] + ".expan_coeff", "w") as fp:
+    fp.write(" %5d%17.10f\n" % (128, cnorm[0]))
+    for l in range(129):
+        fp.write(" %5d" % l + "".join("%17.10f" % v for v in coef[0, :, l]) + "\n")
+"""
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GEOSMIE_REF"),
+                    help="root of the GEOSmie reference tree (default: $GEOSMIE_REF)")
     ap.add_argument("--only", default="")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref (or set GEOSMIE_REF) to the root of the GEOSmie reference tree")
     src = os.path.join(a.ref, "src")
     Dataset = _install_shims()
     sys.path.insert(0, os.path.join(src, "pymiecoated"))
     sys.path.insert(0, os.path.join(src, "geosmie"))
     from pymiecoated import mie_coated
     sel = a.only.split(",") if a.only else ["single", "coated", "size_range", "tables", "bands", "hydrophobic",
-                                             "growth"]
+                                             "growth", "gsf_reconstruct", "rungsf"]
     if "single" in sel:
         gen_single(mie_coated)
     if "coated" in sel:
@@ -501,6 +740,10 @@ def main():
         gen_bands(src, Dataset)
     if "growth" in sel:
         gen_growth(src)
+    if "gsf_reconstruct" in sel:
+        gen_gsf_reconstruct(src)
+    if "rungsf" in sel:
+        gen_rungsf(src)
     if "hydrophobic" in sel:
         sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
         gen_hydrophobic(src)

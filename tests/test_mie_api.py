@@ -165,6 +165,53 @@ def test_size_range_fixture_gpu():
 
 
 @pytest.mark.gpu
+def test_calculate_s12_methods_gpu():
+    """MultipleMie.calculateS12 and calculateS12WithParams (mie_coated.py:51-59)
+    against the reference's own sweep and coefficients: calculateS12 per size
+    against the size_range fixture, calculateS12WithParams with the
+    reference's a_n/b_n (mie_single fixture) against the reference's S1/S2,
+    1e-9 of the instance's largest |S|."""
+    g = load_golden("size_range.npz")
+    mm = MultipleMie(g["x"], None, g["cost"])
+    mm.preCalculate()
+    eps = complex(float(g["mr"]), float(g["mi"])) ** 2
+    sc = np.max(np.abs(g["s1"]), axis=1)
+    for i in [0, 17, 40, 79]:
+        row = mm.calculateS12(float(g["x"][i]), eps, 1.0, (), ())
+        assert row.shape == (g["cost"].size, 2)
+        assert np.max(np.abs(row[:, 0] - g["s1"][i])) / sc[i] < 1e-9
+        assert np.max(np.abs(row[:, 1] - g["s2"][i])) / sc[i] < 1e-9
+    s = load_golden("mie_single.npz")
+    mm = MultipleMie(s["x"], None, s["u"])
+    off = s["offsets"]
+    for i in range(0, len(s["x"]), 7):
+        sl = slice(off[i], off[i + 1])
+        row = mm.calculateS12WithParams(float(s["x"][i]), (), (), (s["an"][sl], s["bn"][sl], off[i + 1] - off[i]))
+        scale = max(np.max(np.abs(s["s1"][i])), np.max(np.abs(s["s2"][i])))
+        assert np.max(np.abs(row[:, 0] - s["s1"][i])) / scale < 1e-9, i
+        assert np.max(np.abs(row[:, 1] - s["s2"][i])) / scale < 1e-9, i
+
+
+@pytest.mark.gpu
+def test_s12_pt_gpu():
+    """Mie.S12_pt with the scaled pi/tau rows of gbmie_pitau equals Mie.S12
+    at the same cosine (the reference's known answer, test_mie.py:45-53);
+    rows longer than nmax are accepted, shorter ones raise ValueError."""
+    from geosmie_gb300.mie import pitau
+    mie = Mie(m=complex(1.5, 0.5), x=2.5)
+    ref = KAT[0][2]
+    for extra in (0, 9):
+        nmax = mie._get().nmax
+        pin, tin = pitau([-0.6], nmax + extra)
+        s1, s2 = mie.S12_pt(pin[0].cpu().numpy(), tin[0].cpu().numpy())
+        assert abs(s1 - ref[0]) / abs(ref[0]) < KAT_EPS
+        assert abs(s2 - ref[1]) / abs(ref[1]) < KAT_EPS
+    pin, tin = pitau([-0.6], mie._get().nmax - 1)
+    with pytest.raises(ValueError):
+        mie.S12_pt(pin[0].cpu().numpy(), tin[0].cpu().numpy())
+
+
+@pytest.mark.gpu
 def test_large_and_edge_sizes_gpu():
     from geosmie_gb300.mie import coefficients
     from oracle import pymie
