@@ -174,6 +174,8 @@ def work_counts(spec):
     lam = np.asarray(spec["lambda"])
     grid = np.asarray(spec["grid"])
     m = np.asarray(spec["m"])
+    mcore = spec.get("m_core")
+    mabs = np.abs(m) if mcore is None else np.maximum(np.abs(m), np.abs(np.asarray(mcore)).reshape(m.shape))
     nl, nrh, ncomp = m.shape
     x = 2 * np.pi * grid[None, :] / lam[:, None] if int(spec["grid_kind"]) == 1 else np.tile(grid, (1, 1))
     nm = nmax_of(x)                                   # [nle, ns]
@@ -186,7 +188,7 @@ def work_counts(spec):
         nmi = nm[le[li]]
         for ri in range(nrh):
             for c in range(ncomp):
-                z = np.abs(m[li, ri, c]) * xs
+                z = mabs[li, ri, c] * xs   # coated: max(|m_core|, |m_shell|) y (mie_coated.py:131,166)
                 nmx = np.rint(np.maximum(nmi, z) + 16.0)
                 sum_nmax += int(nmi.sum())
                 sum_nmx += int(nmx.sum())
@@ -210,4 +212,4 @@ def work_counts(spec):
             "sum_nmax": sum_nmax, "sum_nmx": sum_nmx, "sum_warm": sum_warm,
             "sum_kc16": sum_kc16, "sum_kc16_half": sum_kc16_half,
             "rows": int(x.shape[0] * grid.size), "nbin": int(np.asarray(spec["frac"]).shape[0]),
-            "nang": int(np.asarray(spec["ang"]).size)}
+            "nang": int(np.asarray(spec["ang"]).size), "coated": mcore is not None}

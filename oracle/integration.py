@@ -410,7 +410,19 @@ def run_table(params, mlist, waterm, ang=None, batch=True, lambdas=None):
     return out
 
 
-def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
+def psd_volume(xxarr, lam, psd, fracs):
+    """The 'volume' that integrate_psd accumulates over the PSD components
+    (4/3 pi sum r^3 psd / sum psd, weighted by frac), in its order of
+    operations; it needs no Mie results."""
+    rr = xxarr * lam / (2.0 * np.pi)
+    vol = 0.0
+    for fi, frac in enumerate(fracs):
+        w_psd = psd[fi]
+        vol = vol + frac * (4.0 / 3.0 * np.pi * np.sum(rr ** 3.0 * w_psd) / np.sum(w_psd))
+    return vol
+
+
+def run_spec(spec, n_gsf=0, n_gsf_nodes=0, units=None, batch=True):
     """CPU evaluation of a table spec (the arrays of geosmie_gb300's
     TablePlan / gbmie_table_desc) with the restated reference formulas:
     raw_mie, lognormal / r^-4 / given PSD weights, integrate_psd,
@@ -422,6 +434,10 @@ def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
     Returns arrays shaped like the GPU results: scatkeys [nbin, nl, nrh,
     nang], scalar keys [nbin, nl, nrh], pback [nbin, nl, nrh, 6], 'nl_<key>'
     [nbin, nl, nrh], pmom [nbin, nl, nrh, 6, n_gsf] in the pygeos p order.
+    units: None for every (wavelength, RH) unit, or a list of (wavelength
+    index, RH index) pairs to evaluate (the others stay zero).  batch=False
+    evaluates homogeneous spheres size by size as pymiecoated's MultipleMie
+    does (raw_mie's per-size path) instead of vectorised over sizes.
     """
     from . import gsf as ogsf
     lam = np.asarray(spec["lambda"], np.float64)
@@ -457,20 +473,26 @@ def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
             w[r > pp[1]] = 0.0
         return w / np.sum(w)
 
-    for li in range(nl):
+    todo = {}
+    for li, ri in (units if units is not None else [(li, ri) for li in range(nl) for ri in range(nrh)]):
+        todo.setdefault(int(li), []).append(int(ri))
+    for li in sorted(todo):
         x = 2 * np.pi * grid / lam[li] if radius_grid else grid
         rr = x * lam[li] / (2 * np.pi)
         reff0 = [[np.sum(rr ** 4 * weights(li, rh0, b, c, x)) / np.sum(rr ** 3 * weights(li, rh0, b, c, x))
                   for c in range(ncomp)] for b in range(nbin)]
-        mass0 = [None] * nbin
-        for ri in range(nrh):
+        # dry mass from RH index 0 (dointegration.py:992-993): the PSD alone
+        mass0 = [psd_volume(x, lam[li], [weights(li, 0, b, c, x) for c in range(ncomp)], frac[b]) *
+                 float(np.asarray(spec["rhop0"])[b]) for b in range(nbin)]
+        for ri in sorted(set(todo[li])):
             if spec.get("m_core") is not None:
                 mcore = np.asarray(spec["m_core"], np.complex128)
                 cr = float(np.asarray(spec["core_ratio"])[ri])
                 raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag, m_core=mcore[li, ri, c],
                                 core_ratio=cr) for c in range(ncomp)]
             else:
-                raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag) for c in range(ncomp)]
+                raws = [raw_mie(x, cost, lam[li], m[li, ri, c].real, m[li, ri, c].imag, batch=batch)
+                        for c in range(ncomp)]
             for b in range(nbin):
                 psd = [weights(li, ri, b, c, x) for c in range(ncomp)]
                 rhop = float(np.asarray(spec["rhop"])[b, ri])
@@ -479,8 +501,6 @@ def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
                 fin = finalize_unit(ret, ang, float(np.asarray(spec["gf"])[ri]), rhop, [m[li, ri, 0].real],
                                     [m[li, ri, 0].imag], float(np.asarray(spec["rlow"])[b]),
                                     float(np.asarray(spec["rup"])[b]))
-                if ri == 0:
-                    mass0[b] = fin["volume"] * rhop0
                 fin["area"] = fin["area"] / mass0[b]
                 fin["volume"] = fin["volume"] / mass0[b]
                 for k in SCATKEYS:
@@ -493,7 +513,12 @@ def run_spec(spec, n_gsf=0, n_gsf_nodes=0):
     if n_gsf:
         F = np.stack([out[k] for k in ["p11", "p22", "p33", "p44", "p12", "p34"]], axis=3)
         ng = max(n_gsf, n_gsf_nodes)
-        coef, _ = ogsf.expand(ang, F.reshape(-1, 6, ang.size), ng)
-        coef = coef.reshape(nbin, nl, nrh, 6, ng)[..., :n_gsf]
-        out["pmom"] = coef[:, :, :, [0, 4, 2, 5, 1, 3], :]
+        done = np.zeros((nl, nrh), bool)
+        for li in todo:
+            done[li, todo[li]] = True
+        sel = np.broadcast_to(done[None], (nbin, nl, nrh))
+        coef, _ = ogsf.expand(ang, F[sel].reshape(-1, 6, ang.size), ng)
+        pm = np.zeros((nbin, nl, nrh, 6, n_gsf))
+        pm[sel] = coef[..., :n_gsf][:, [0, 4, 2, 5, 1, 3], :]
+        out["pmom"] = pm
     return out

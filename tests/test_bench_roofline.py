@@ -69,3 +69,50 @@ def test_fallback_peak_is_named(counts):
 
 def test_no_kernels_no_roofline(counts):
     assert bench.roofline_of({}, counts, PEAKS, 3000.0) == ({}, None)
+
+
+def test_accuracy_summaries():
+    """bench.accuracy: phase errors relative to P11 at the same angle, qabs
+    relative to itself for the mixed path and to qext for FP64, moments
+    relative to the entry's largest alpha1; oracle_accuracy compares a
+    table's sample units with per-unit oracle results."""
+    import numpy as np
+    rng = np.random.default_rng(1)
+    shp = (2, 3, 4)
+    ref = {k: rng.uniform(1.0, 2.0, shp + (7,)) for k in bench.SCAT}
+    ref.update({k: rng.uniform(1.0, 2.0, shp) for k in bench.SCALARS + ["qabs"]})
+    ref["pback"] = rng.uniform(1.0, 2.0, shp + (6,))
+    ref["pmom"] = rng.uniform(1.0, 2.0, shp + (6, 5))
+    ref.update({"nl_" + k: rng.uniform(1.0, 2.0, shp) for k in bench.NLKEYS})
+    got = {k: v.copy() for k, v in ref.items()}
+    got["p34"][1, 2, 3, 4] += 1e-7 * ref["p11"][1, 2, 3, 4]
+    got["qabs"][0, 0, 0] *= 1 + 3e-7
+    got["pmom"][1, 1, 1, 2, 3] += 2e-7 * np.max(ref["pmom"][1, 1, 1, 0, :])
+    a = bench.accuracy(got, ref, mixed=True)
+    assert abs(a["phase_over_p11"] - 1e-7) < 1e-12
+    assert abs(a["qabs_rel"] - 3e-7) < 1e-10 and "qabs_over_qext" not in a
+    assert abs(a["pmom_over_alpha1"] - 2e-7) < 1e-12
+    assert a["scalars_rel"] == 0.0 and a["nl_rel"] == 0.0
+    b = bench.accuracy(got, ref)
+    assert "qabs_over_qext" in b and b["qabs_over_qext"] <= 3e-7 * 2.0
+    units = [(0, 1, 2), (0, 2, 3)]
+    orc = {u: {k: v[:, u[1], u[2]] for k, v in ref.items()} for u in units}
+    acc = bench.oracle_accuracy(units, [got], [ref], orc)
+    assert acc["units"] == 2 and acc["mixed"]["phase_over_p11"] == 0.0
+    assert abs(acc["fp64"]["phase_over_p11"] - 1e-7) < 1e-12
+    assert bench.sig({"a": [1.23456789, 2]}, 3) == {"a": [1.23, 2]}
+
+
+def test_config_sample_units_in_range():
+    """Every oracle sample unit of the five workloads indexes an existing
+    (table, wavelength, RH) unit; the headline sulfate units are timed size by
+    size, the others vectorised."""
+    for cfg in (1, 2, 3, 4):
+        specs = bench.build_config(cfg)[0]
+        for t in bench.unit_tasks(cfg):
+            c, si, li, ri, batch = t
+            m = specs[si]["m"]
+            assert c == cfg and 0 <= li < m.shape[0] and 0 <= ri < m.shape[1]
+            assert batch == (cfg != 3)
+    tot, per = bench.config_counts(2)
+    assert tot["instances"] == 5 * 40 * 1000 and per["instances"] == 40 * 1000

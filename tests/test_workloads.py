@@ -112,6 +112,41 @@ def test_seasalt_large_gauss_nodes_gpu():
     assert np.allclose(a["pmom"][..., 0, 0], 1.0, atol=1e-12)
 
 
+def _check_units(a, ref, units, n_gsf):
+    """The FP64 GPU table against the oracle at the given (wavelength, RH)
+    units, all bins: the tolerances of _check_table (phase 1e-9 of P11,
+    qext/qsca/g 1e-10, other scalars 1e-9, qabs 1e-10 of qext), GSF moments
+    1e-9 absolute."""
+    li = np.array([u[0] for u in units])
+    ri = np.array([u[1] for u in units])
+    sub = lambda d: {k: v[:, li, ri] for k, v in d.items() if isinstance(v, np.ndarray) and v.ndim >= 3}
+    _check_table(sub(a), sub(ref))
+    if n_gsf:
+        assert np.max(np.abs(a["pmom"][:, li, ri] - ref["pmom"][:, li, ri])) < 1e-9
+
+
+@pytest.mark.gpu
+def test_sulfate_table_full_gpu():
+    """The benchmark's headline table in full -- 36 RH x 60 wavelengths x 5
+    bins x 2000 radii x 181 angles + 64 GSF moments: the mixed-precision
+    table against the FP64 table on every output (phase elements 1e-6 of
+    P11, every scalar 1e-6 relative, qabs 1e-6 of itself, GSF moments 1e-6
+    of the entry's largest alpha1), and the FP64 table against the oracle on
+    stratified (wavelength, RH) units spanning the wavelength and RH range
+    (dointegration.py:786-1031)."""
+    from oracle import integration
+    spec, _ = workloads.sulfate_table()
+    a, b = _mixed_plain(spec, n_gsf=64)
+    _check_mixed(a, b, 64)
+    pb = np.max(np.abs(b["pback"] - a["pback"]) / np.abs(a["pback"][..., :1]))
+    assert pb < 1e-6, pb
+    for k in ["nl_" + k for k in ["mass", "volume", "area", "rEff", "rMass", "rhop", "growth_factor"]]:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, k
+    units = [(0, 0), (0, 35), (29, 18), (59, 0), (59, 35)]
+    ref = integration.run_spec(spec, n_gsf=64, units=units)
+    _check_units(a, ref, units, 64)
+
+
 def test_coated_workload_spec_cpu():
     spec, _ = workloads.coated_bc()
     assert spec["m"].shape == (30, 200, 1) and spec["m_core"].shape == (30, 200, 1)
