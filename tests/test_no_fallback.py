@@ -54,10 +54,11 @@ def test_package_never_imports_the_oracle():
 
 
 def test_bench_uses_the_oracle_only_in_its_cpu_legs():
-    """bench.py reaches the oracle only from the CPU baseline and the
-    reference arm (_oracle_unit, cpu_sample, run_reference)."""
+    """bench.py reaches the oracle only from its CPU legs: the per-unit CPU
+    task (_unit_task: the 1-core baseline and the accuracy check) and the
+    reference arm (run_reference)."""
     tree = ast.parse(open(os.path.join(ROOT, "bench.py")).read())
-    allowed = {"_oracle_unit", "cpu_sample", "run_reference"}
+    allowed = {"_unit_task", "run_reference"}
     seen = []
 
     def visit(node, fn):
