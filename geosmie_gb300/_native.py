@@ -16,6 +16,7 @@ from . import build as _build
 GBMIE_OK = 0
 GBMIE_ERR_INVALID = 1
 GBMIE_ERR_NMAX = 2
+GBMIE_ERR_TIMEOUT = 4
 GBMIE_PLAIN_FP64 = 0
 GBMIE_MIXED = 1
 GRID_X = 0
@@ -56,6 +57,7 @@ SIGNATURES = {
     "gbmie_table_run_graph": (ctypes.c_int, [_P, _P, _P]),
     "gbmie_table_plan_autotune": (ctypes.c_int, [_P, _P, _P]),
     "gbmie_table_plan_tuning": (ctypes.c_int, [_P, _P]),
+    "gbmie_table_plan_set_wait_limit": (ctypes.c_int, [_P, _I64]),
     "gbmie_gsf": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32, _P, _P, _I32]),
     "gbmie_band_average": (ctypes.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P]),
     "gbmie_measure_fp64_peak": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
@@ -67,6 +69,11 @@ _lock = threading.Lock()
 
 class GbmieError(RuntimeError):
     """A failure reported by the CUDA library."""
+
+
+class DeviceTimeout(GbmieError):
+    """A device-side wait ran out of tries (GBMIE_ERR_TIMEOUT): the kernel gave
+    up and returned; the context stays usable."""
 
 
 def library_path():
@@ -129,6 +136,8 @@ class Context:
                                (self.lib.gbmie_last_error(self.h) or b"").decode())
         if st in (GBMIE_ERR_INVALID, GBMIE_ERR_NMAX):
             raise ValueError(msg)
+        if st == GBMIE_ERR_TIMEOUT:
+            raise DeviceTimeout(msg)
         raise GbmieError(msg)
 
     def call(self, name, *args):

@@ -742,6 +742,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
     if (!p) return GBMIE_ERR_NOMEM;
     p->ctx = ctx;
     p->d = d;
+    p->wait_limit = GBMIE_WAIT_LIMIT_DEFAULT;
     p->n_le = d.grid_kind == GBMIE_GRID_X ? 1 : d.n_lambda;
     p->n_units = (int64_t)d.n_lambda * d.n_rh * d.n_comp;
     p->n_inst = p->n_units * d.n_size;
@@ -1301,6 +1302,20 @@ extern "C" int gbmie_table_plan_autotune(gbmie_ctx *ctx, gbmie_table_plan *p, co
     ctx->timing = save_timing;
     ctx->launches = save_launches;
     return st;
+}
+
+extern "C" int gbmie_table_plan_set_wait_limit(gbmie_table_plan *p, int64_t tries)
+{
+    if (!p || tries > (int64_t)GBMIE_WAIT_LIMIT_DEFAULT) return GBMIE_ERR_INVALID;
+    const uint32_t lim = tries < 0 ? GBMIE_WAIT_LIMIT_DEFAULT : (uint32_t)tries;
+    if (lim == p->wait_limit) return GBMIE_OK;
+    if (p->gexec) {   // a captured graph holds the old limit; none of its replays may be in flight
+        GBMIE_TRY(ctx_cuda(p->ctx, cudaStreamSynchronize(p->ctx->stream), "set_wait_limit"));
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+    }
+    p->wait_limit = lim;
+    return GBMIE_OK;
 }
 
 extern "C" int gbmie_table_plan_tuning(const gbmie_table_plan *p, int32_t *params)

@@ -580,6 +580,7 @@ struct TcArgs {
     const int64_t *unit_cbase;   // [n_units]
     int ntiles;
     int win;                     // accumulation window (16-order chunks, <= TC_NS)
+    uint32_t wait_limit;         // tries of every pipeline wait (gbmie_table_plan_set_wait_limit)
     int *flags;
 };
 
@@ -695,7 +696,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             uint32_t it = 0, ii = 0, wc = 0, b0_loads = 0;   // chunks, items, own windows
             bool ok = true, have_b0 = false;
             if (!reload) {   // every block's resident chunk, loaded once
-                ok = mbar_wait_or_abort(b0_full, 0, s_abort);
+                ok = mbar_wait_or_abort(b0_full, 0, s_abort, 0, g.wait_limit);
                 b0_loads = 1;
             }
             for (int k = 0; ok; ++k) {
@@ -707,7 +708,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 for (int ab = 0; ab < nblocks && ok; ++ab) {
                     if (reload) {   // the producer reloads the resident slot
                         if (have_b0) mma_commit(b0_empty);
-                        if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort, TC_SLEEP_NS)) {
+                        if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort, TC_SLEEP_NS, g.wait_limit)) {
                             ok = false;
                             break;
                         }
@@ -734,14 +735,14 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                             for (int w0 = 0; w0 < nc && ok; w0 += g.win) {
                                 const int nj = min(g.win, nc - w0);
                                 const uint32_t set = 2 * p + (wc & 1u), use = wc >> 1;
-                                if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort)) {
+                                if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, 0, g.wait_limit)) {
                                     ok = false;
                                     break;
                                 }
                                 for (int j = 0; j < nj && ok; ++j) {
                                     const uint32_t c = it + j, st = c % TC_NS, par = (c / TC_NS) & 1u;
                                     ok = false;
-                                    for (uint32_t tr = 0; tr < (1u << 26); ++tr) {
+                                    for (uint32_t tr = 0; tr < g.wait_limit; ++tr) {
                                         if (s_chunk[st] == (int)c) {
                                             if (mbar_try(full + st, par)) {
                                                 ok = true;
@@ -798,16 +799,18 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         // ================= producer: bulk copies (one thread) =================
         if (lane == 0) {
             uint32_t it = 0, b0_loads = 0;
-            uint64_t *last_tx = nullptr;   // barrier of the last bulk copy, and its phase
-            uint32_t last_tx_phase = 0;
+            // the phase of the latest bulk copy into each ring stage (bit
+            // TC_NS + st: stage st has one) and into the resident slot, so
+            // that an abort can wait for every copy still in flight
+            uint32_t st_phase = 0, tx_used = 0, b0_phase = 0;
             bool ok = true;
             if (!reload) {
                 mbar_arrive_expect_tx(b0_full, (uint32_t)(nblocks * TC_A_BYTES));
                 for (int b = 0; b < nblocks; ++b)
                     bulk_g2s(sB0 + b * TC_A_BYTES, (const uint8_t *)g.bt + (size_t)b * nkc * TC_A_BYTES, TC_A_BYTES,
                              b0_full);
-                last_tx = b0_full;
-                last_tx_phase = 0;
+                tx_used |= 1u << (2 * TC_NS);
+                b0_phase = 0;
             }
             for (int k = 0; ok; ++k) {
                 const int64_t uidx = tc_unit_index(k, cta, G);
@@ -823,14 +826,14 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     const uint8_t *gA = (const uint8_t *)g.bt + (size_t)ab * nkc * TC_A_BYTES;
                     if (reload) {
                         if (b0_loads > 0 &&
-                            !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort, TC_SLEEP_NS)) {
+                            !mbar_wait_or_abort(b0_empty, (b0_loads - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit)) {
                             ok = false;
                             break;
                         }
                         mbar_arrive_expect_tx(b0_full, TC_A_BYTES);
                         bulk_g2s(sB0, gA, TC_A_BYTES, b0_full);
-                        last_tx = b0_full;
-                        last_tx_phase = b0_loads & 1u;
+                        tx_used |= 1u << (2 * TC_NS);
+                        b0_phase = b0_loads & 1u;
                         ++b0_loads;
                     }
                     // chunk bases tcb[tile], tcb[tile + 1], loaded one tile ahead
@@ -865,7 +868,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 const int st = (int)(c % TC_NS);
                                 uint8_t *sS = sStage + st * TC_STAGE_BYTES;
                                 if (c >= TC_NS &&
-                                    !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort, TC_SLEEP_NS)) {
+                                    !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit)) {
                                     ok = false;
                                     break;
                                 }
@@ -873,19 +876,27 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 mbar_arrive_expect_tx(full + st, TC_B_BYTES + (j > 0 ? TC_A_BYTES : 0));
                                 bulk_g2s(sS, ua + ((size_t)(base + j) * 2 + h) * TC_B_BYTES, TC_B_BYTES, full + st);
                                 if (j > 0) bulk_g2s(sS + TC_B_BYTES, gA + (size_t)j * TC_A_BYTES, TC_A_BYTES, full + st);
-                                last_tx = full + st;
-                                last_tx_phase = (c / TC_NS) & 1u;
+                                tx_used |= 1u << (TC_NS + st);
+                                st_phase = (st_phase & ~(1u << st)) | (((c / TC_NS) & 1u) << st);
                             }
                         }
                     }
                 }
             }
-            if (!ok || *s_abort) {
+            if (!ok) {
                 *s_abort = 1;
                 atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
-                // a bulk copy still in flight must land before shared memory is released
-                if (last_tx) mbar_wait(last_tx, last_tx_phase, 1u << 20);
             }
+            // every bulk copy must land before shared memory is released, also
+            // when another role gave up and left copies unconsumed: wait for
+            // the latest phase of every stage that received one (an earlier
+            // phase of a stage completed before its next copy was issued); in
+            // a run without timeouts these have all completed already
+            for (int st = 0; st < TC_NS; ++st)
+                if ((tx_used >> (TC_NS + st)) & 1u && !mbar_wait(full + st, (st_phase >> st) & 1u, 1u << 20))
+                    atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
+            if ((tx_used >> (2 * TC_NS)) & 1u && !mbar_wait(b0_full, b0_phase, 1u << 20))
+                atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
         }
         __syncwarp();
     } else if (warp == 11) {
@@ -965,7 +976,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             const uint32_t slot = iw % TC_NW;
             int go = 1;
             if (lane == 0 && iw >= TC_NW)
-                go = mbar_wait_or_abort(w_empty + slot, (iw / TC_NW - 1) & 1u, s_abort, TC_SLEEP_NS) ? 1 : 0;
+                go = mbar_wait_or_abort(w_empty + slot, (iw / TC_NW - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit) ? 1 : 0;
             go = __shfl_sync(0xffffffffu, go, 0);
             if (!go) {
                 ok = false;
@@ -1049,7 +1060,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             const uint32_t wsl = ie % TC_NW;
             {
                 int go = 1;
-                if (lane == 0) go = mbar_wait_or_abort(w_full + wsl, (ie / TC_NW) & 1u, s_abort) ? 1 : 0;
+                if (lane == 0) go = mbar_wait_or_abort(w_full + wsl, (ie / TC_NW) & 1u, s_abort, 0, g.wait_limit) ? 1 : 0;
                 go = __shfl_sync(0xffffffffu, go, 0);
                 if (!go) {
                     ok = false;
@@ -1069,7 +1080,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 const uint32_t wi = ip ? wce[1] : wce[0];
                 const uint32_t set = 2 * ip + (wi & 1u), use = wi >> 1;
                 int go = 1;
-                if (lane == 0) go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort) ? 1 : 0;
+                if (lane == 0) go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort, 0, g.wait_limit) ? 1 : 0;
                 go = __shfl_sync(0xffffffffu, go, 0);
                 if (!go) {
                     ok = false;
@@ -1289,6 +1300,7 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     a.unit_cbase = p->unit_cbase;
     a.ntiles = p->ntiles;
     a.win = p->tc_win < 1 ? 1 : (p->tc_win > TC_WIN_MAX ? TC_WIN_MAX : p->tc_win);
+    a.wait_limit = p->wait_limit;
     a.flags = ctx->d_flags;
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);

@@ -59,7 +59,12 @@ struct gbmie_table_plan {
     int coef_block;         // block size of k_tab_coeffs_mixed
     int tc_win;             // accumulation window of k_tab_s12_tc (16-order chunks)
     int tuned;
+    // tries of every pipeline wait of k_tab_s12_tc before it gives up and
+    // flags a timeout (default GBMIE_WAIT_LIMIT_DEFAULT;
+    // gbmie_table_plan_set_wait_limit)
+    uint32_t wait_limit;
 };
+#define GBMIE_WAIT_LIMIT_DEFAULT (1u << 26)
 
 // ---------------------------------------------------------------------------
 // block reduction of K doubles (all threads receive the totals)

@@ -190,6 +190,14 @@ class TablePlan(object):
         self.ctx.call("gbmie_table_plan_autotune", self.h, ctypes.byref(self.out))
         return self.tuning()
 
+    def set_wait_limit(self, tries):
+        """Tries of every pipeline wait of the mixed path's tensor-core
+        contraction before it gives up and reports a device timeout (raised
+        by the next sync()); None restores the default.  0 makes every wait
+        give up at once: a way to test timeout handling without a hang."""
+        self.ctx.check(self.ctx.lib.gbmie_table_plan_set_wait_limit(self.h, -1 if tries is None else int(tries)),
+                       "gbmie_table_plan_set_wait_limit")
+
     def tuning(self):
         """{'tuned', 'plain_per_bucket', 'plain_chunk' [5], 'plain_threads'
         [5], 'coef_block', 'tc_window'}: the plan's launch parameters (nmax

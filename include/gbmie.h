@@ -281,6 +281,16 @@ int gbmie_table_run_graph(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_ta
  * shape take it at creation.  Ends with a run of the tuned table into out.
  * No counterpart in the reference (its loops run in Python). */
 int gbmie_table_plan_autotune(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_out *out);
+/* Tries of every pipeline wait (mbarrier waits between the roles of the
+ * tensor-core contraction of mixed plans) before the kernel gives up: it
+ * then raises GBMIE_FLAG_TIMEOUT, lets its in-flight copies and MMAs finish,
+ * frees its tensor memory and returns, and the next gbmie_ctx_synchronize
+ * reports GBMIE_ERR_TIMEOUT.  tries < 0 restores the default (2^26); 0 makes
+ * every wait give up at once, so that callers can test their handling of a
+ * device timeout without a hang (the context stays usable).  Drops a
+ * captured graph of the plan (synchronising the context stream first).  No
+ * counterpart in the reference (its loops run in Python). */
+int gbmie_table_plan_set_wait_limit(gbmie_table_plan *plan, int64_t tries);
 /* params[16]: [0] 1 when tuned (or taken from the cache); [1] 1 = the plain
  * angular kernel runs one launch per nmax bucket, 0 = one launch over the
  * whole grid; [2..6] sizes per block and [7..11] angles per pass of the four

@@ -215,6 +215,53 @@ def test_mixed_precision_within_1e6_gpu(n_gsf):
 
 
 @pytest.mark.gpu
+def test_device_wait_timeout_reported_and_context_usable_gpu():
+    """Every pipeline wait of the tensor-core contraction is bounded.  With
+    0 tries every wait gives up at once: the kernel flags a timeout, lets its
+    copies and MMAs finish, frees its tensor memory and returns, and the next
+    synchronisation raises DeviceTimeout.  With a few tries a wait may or may
+    not run out in mid-pipeline; the run ends either way, with OK or a
+    timeout.  The same context and plan then build the table normally, eager
+    and as a captured graph, within the mixed path's 1e-6 of the FP64
+    table."""
+    from geosmie_gb300._native import DeviceTimeout
+    spec = synthetic_spec(nl=3, nrh=3, ns=400, nbin=5, nang=181)
+    from geosmie_gb300.table import TablePlan
+    ref = TablePlan(spec, precision=0, n_gsf=16)
+    ref.run()
+    a = ref.results()
+    ref.close()
+    plan = TablePlan(spec, precision=1, n_gsf=16)
+    plan.set_wait_limit(0)
+    plan.run()
+    with pytest.raises(DeviceTimeout):
+        plan.sync()
+    for tries in (4, 64, 1024):
+        plan.set_wait_limit(tries)
+        plan.run()
+        try:
+            plan.sync()
+        except DeviceTimeout:
+            pass
+    plan.set_wait_limit(0)
+    plan.run(graph=True)
+    with pytest.raises(DeviceTimeout):
+        plan.sync()
+    plan.set_wait_limit(None)
+    for graph in (False, True):
+        plan.run(graph=graph)
+        b = plan.results()
+        p11 = np.abs(a["p11"])
+        for k in SCAT:
+            assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, (graph, k)
+        for k in TIGHT:
+            assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, (graph, k)
+        scale = np.max(np.abs(a["pmom"][..., 0, :]), axis=-1)[..., None, None]
+        assert np.max(np.abs(b["pmom"] - a["pmom"]) / scale) < 1e-6
+    plan.close()
+
+
+@pytest.mark.gpu
 def test_mixed_reference_layout_and_many_angles_gpu():
     """The reference's own layout (one x grid per bin, 371 angles in two
     column blocks, two-mode bin) through the mixed path, against the
