@@ -568,6 +568,19 @@ def main():
         ms_eager, _, ktimes, _ = timed(plans, steps, warmup)
         ms, launches, _, clk = timed(plans, steps, warmup, graph=True, with_clocks=headline)
         r["mixed"] = [p.results() for p in plans]
+        if headline and specs[0].get("m_core") is None:
+            # the same table with the D_n recurrence in FP64 from the
+            # reference's start (the cost of that precision plan on this GPU)
+            for p in plans:
+                p.set_dn_fp64(True)
+            ms_dn, _, kt_dn, _ = timed(plans, steps, warmup)
+            dn = [p.results() for p in plans]
+            for p in plans:
+                p.set_dn_fp64(False)
+            r["dn64"] = {"ms": ms_dn / steps, "coeff_kernel_ms": kt_dn.get("k_tab_coeffs_mixed_dn64", (1, None))[1],
+                         "acc_vs_fp64": worst([accuracy(b, a, mixed=True) for a, b in zip(r["plain"], dn)])}
+            if r["dn64"]["coeff_kernel_ms"] is not None:
+                r["dn64"]["coeff_kernel_ms"] /= steps
         for p in plans:
             p.close()
         del plans
@@ -683,6 +696,8 @@ def main():
                                    "plan creation and the copy back overlap the neighbouring tables' runs"),
         "gpu_launches": h["launches"],
         "clocks": h["clocks"],
+        "dn_fp64_variant": sig(dict(h["dn64"], coeff_kernel_ms_default=h["kernels"].get("k_tab_coeffs_mixed", {}).get(
+            "ms_per_launch")), 3) if h.get("dn64") else None,
         "table_gen_ms": sig({"mixed": h["ms"], "mixed_eager_launches": h["ms_eager"], "plain_fp64": h["ms_plain"]}),
         "mixed_vs_plain_speedup": sig(h["ms_plain"] / h["ms"]),
         "plain_fp64_value": sig(h["plain_value"]),

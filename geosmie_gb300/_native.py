@@ -58,6 +58,7 @@ SIGNATURES = {
     "gbmie_table_plan_autotune": (ctypes.c_int, [_P, _P, _P]),
     "gbmie_table_plan_tuning": (ctypes.c_int, [_P, _P]),
     "gbmie_table_plan_set_wait_limit": (ctypes.c_int, [_P, _I64]),
+    "gbmie_table_plan_set_dn_fp64": (ctypes.c_int, [_P, _I32]),
     "gbmie_gsf": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32, _P, _P, _I32]),
     "gbmie_band_average": (ctypes.c_int, [_P, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P]),
     "gbmie_measure_fp64_peak": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),

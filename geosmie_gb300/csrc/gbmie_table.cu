@@ -573,6 +573,10 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.rowc = (double4 *)(scr + p->o_rowc);
     v.hidx = (HomogIndex *)(scr + p->o_hidx);
     v.pcd = p->d.precision == GBMIE_MIXED ? (float4 *)(scr + p->o_pcf) : nullptr;
+    v.ngrp = p->ngrp;
+    v.grel = p->grp;
+    v.grow = p->grp ? p->grp + (size_t)p->n_le * (p->ngrp + 1) : nullptr;
+    v.gunit = p->grp ? v.grow + p->n_le : nullptr;
     v.hdf = p->d.precision == GBMIE_MIXED ? (float4 *)(scr + p->o_hdf) : nullptr;
     v.rowcd = p->d.precision == GBMIE_MIXED ? (float4 *)(scr + p->o_rowcd) : nullptr;
     return v;
@@ -694,6 +698,7 @@ static void plan_free(gbmie_table_plan *p)
     free(p->hcos);
     if (p->brange) cudaFreeAsync(p->brange, s);
     if (p->unit_cbase) cudaFreeAsync(p->unit_cbase, s);
+    if (p->grp) cudaFreeAsync(p->grp, s);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
     if (p->has_gsf && p->gsf_entry >= 0) table_gsf_release(p->ctx, p->gsf_entry);
@@ -867,6 +872,50 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
                               "unit chunks copy");
             free(tcb);
             free(ucb);
+            // order-major layout of the mixed recurrences' rows and
+            // coefficients in groups of 32 sizes: order k of size 32 g + l at
+            // [group base + 32 (k - 1) + l], so that a warp (one group) reads
+            // and writes one contiguous 512-byte segment per order.  A group
+            // holds 32 x its largest nmax entries.  grp = [n_le][ng + 1]
+            // bases within a wavelength's block, [n_le] block bases of the
+            // rows, [n_units] block bases of the coefficients.
+            p->ngrp = (d.n_size + 31) / 32;
+            const size_t ngl = (size_t)p->n_le * (p->ngrp + 1);
+            const size_t ngrp_all = ngl + p->n_le + p->n_units;
+            int64_t *hg = st == GBMIE_OK ? (int64_t *)malloc(sizeof(int64_t) * ngrp_all) : nullptr;
+            if (st == GBMIE_OK && !hg) st = GBMIE_ERR_NOMEM;
+            if (st == GBMIE_OK) {
+                int64_t rows_acc = 0;
+                for (int le = 0; le < p->n_le; ++le) {
+                    int64_t acc_g = 0;
+                    for (int g = 0; g < p->ngrp; ++g) {
+                        hg[(size_t)le * (p->ngrp + 1) + g] = acc_g;
+                        int64_t gm = 0;
+                        for (int i = 32 * g; i < d.n_size && i < 32 * g + 32; ++i) {
+                            const int64_t r = (int64_t)le * d.n_size + i;
+                            if (hoff[r + 1] - hoff[r] > gm) gm = hoff[r + 1] - hoff[r];
+                        }
+                        acc_g += 32 * gm;
+                    }
+                    hg[(size_t)le * (p->ngrp + 1) + p->ngrp] = acc_g;
+                    hg[ngl + le] = rows_acc;
+                    rows_acc += acc_g;
+                }
+                p->pcg_total = rows_acc;
+                int64_t cf_acc = 0;
+                for (int64_t u = 0; u < p->n_units; ++u) {
+                    const int lam = (int)(u / ((int64_t)d.n_rh * d.n_comp));
+                    const int le = d.grid_kind == GBMIE_GRID_X ? 0 : lam;
+                    hg[ngl + p->n_le + u] = cf_acc;
+                    cf_acc += hg[(size_t)le * (p->ngrp + 1) + p->ngrp];
+                }
+                p->cfg_total = cf_acc;
+                st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->grp, sizeof(int64_t) * ngrp_all, ctx->stream), "size groups");
+            }
+            if (st == GBMIE_OK)
+                st = ctx_cuda(ctx, cudaMemcpyAsync(p->grp, hg, sizeof(int64_t) * ngrp_all, cudaMemcpyHostToDevice, ctx->stream),
+                              "size groups copy");
+            free(hg);
             if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->unit_order, sizeof(int) * p->n_units, ctx->stream), "unit order");
             if (st == GBMIE_OK)
                 st = ctx_cuda(ctx, cudaMemcpyAsync(p->unit_order, ord, sizeof(int) * p->n_units, cudaMemcpyHostToDevice, ctx->stream),
@@ -939,11 +988,11 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_reff0 = carve(sizeof(double) * (size_t)d.n_lambda * d.n_bin * d.n_comp);
         p->o_pacc = carve(sizeof(double) * (size_t)p->n_entries * 4 * d.n_ang);
         p->o_pq = carve(mixed ? 16 : sizeof(double2) * (size_t)p->nmax_max * d.n_ang);
-        p->o_cf = carve(mixed ? sizeof(float4) * (size_t)p->ab_total : 16);
+        p->o_cf = carve(mixed ? sizeof(float4) * (size_t)(p->ab_total > p->cfg_total ? p->ab_total : p->cfg_total) : 16);
         p->o_eexp = carve(mixed ? sizeof(int) * (size_t)p->n_inst : 16);
         p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
         p->o_asplit = carve(mixed ? (size_t)16384 * (size_t)p->n_chunks : 16);
-        p->o_pcf = carve(mixed ? sizeof(float4) * (size_t)p->pc_total : 16);
+        p->o_pcf = carve(mixed ? sizeof(float4) * (size_t)p->pcg_total : 16);
         p->o_hdf = carve(mixed ? 4 * sizeof(float4) * (size_t)p->n_units : 16);
         p->o_rowcd = carve(mixed ? 2 * sizeof(float4) * (size_t)p->n_le * d.n_size : 16);
         p->o_dscr = carve(d.m_core ? 5 * sizeof(double2) * (size_t)p->ab_total : 16);
@@ -1315,6 +1364,19 @@ extern "C" int gbmie_table_plan_set_wait_limit(gbmie_table_plan *p, int64_t trie
         p->gexec = nullptr;
     }
     p->wait_limit = lim;
+    return GBMIE_OK;
+}
+
+extern "C" int gbmie_table_plan_set_dn_fp64(gbmie_table_plan *p, int32_t enable)
+{
+    if (!p || (enable != 0 && enable != 1)) return GBMIE_ERR_INVALID;
+    if (enable == p->dn_fp64) return GBMIE_OK;
+    if (p->gexec) {   // a captured graph holds the other kernel; none of its replays may be in flight
+        GBMIE_TRY(ctx_cuda(p->ctx, cudaStreamSynchronize(p->ctx->stream), "set_dn_fp64"));
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+    }
+    p->dn_fp64 = enable;
     return GBMIE_OK;
 }
 

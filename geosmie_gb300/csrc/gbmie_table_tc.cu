@@ -122,7 +122,7 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 // and the rest in FP32: D~ imaginary parts, the products N.im, M.im and the
 // ratio a = N / (N - i M).  Coefficients go to emit(k, a, b, t) from k = nmax
 // down to 1.  rowd: psi_n, chi_n of x as pairs (psi hi, lo, chi hi, lo) at
-// [n - 1].  GB300's FP64 pipe issues a small fraction of the FP32 rate, so
+// [(n - 1) rs].  GB300's FP64 pipe issues a small fraction of the FP32 rate, so
 // the pairs (a few FP32 operations per FP64 one) run these recurrences
 // several times faster than FP64 did; the precision they keep (2^-46 against
 // 2^-53) is far below the FP32 coefficients this path emits: the largest
@@ -140,9 +140,16 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float v)
 //
 // hd: the unit's constants as pairs (k_mixed_consts): m, 1/m, x/z, (|z|/x);
 // r0 = (sin x, cos x) = (psi_0, chi_0) and xi = 1/x as pairs, xf = x.
-template <class Emit>
+//
+// DN64 (a measurement variant, gbmie_table_plan_set_dn_fp64): the downward
+// D_n recurrence in FP64 from the reference's start, zero at
+// nmx = round(max(nmax, |m x|) + 16) (mie_coeffs.py:101,119-121), with
+// z = m x formed in FP64 from m64 and x64; D_k is then rounded to pairs for
+// the numerators, which are as above.
+template <bool DN64, class Emit>
 __device__ __forceinline__ void homog_core_mixed(const float4 *__restrict__ hd, float4 r0, df xi, float xf,
-                                                 const float4 *__restrict__ rowd, int nmax, Emit &emit)
+                                                 const float4 *__restrict__ rowd, int rs, int nmax, Emit &emit,
+                                                 double2 m64 = make_double2(0.0, 0.0), double x64 = 0.0)
 {
     const float4 hm = hd[0], hmi = hd[1], hz = hd[2];
     const float azm = hd[3].x;
@@ -158,33 +165,52 @@ __device__ __forceinline__ void homog_core_mixed(const float4 *__restrict__ hd, 
     // asks for 1e-17); emulated for x in [1e-3, 650]: the same coefficients
     // to 2.2e-7 with 24% fewer steps on the sulfate-like table.
     int warm = nmx - 1 - nmax;
-    if (az < (float)(nmax + 1)) {
+    if (!DN64 && az < (float)(nmax + 1)) {
         const float q = 2.f * logf((2.f * (float)(nmax + 1) + 1.f) / az);
         const int need = (int)ceilf(23.0f / q) + 2;
         if (need < warm) warm = need;
     }
     cdf D = cdf{df{0.f, 0.f}, df{0.f, 0.f}};
-    for (int k = nmax + warm; k > nmax; --k) {
-        const cdf r = cdf_mul_f(zinv, (float)(k + 1));   // (k+1)/z
-        const cdf w = cdf_add(D, r);
-        const df iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
-        D = cdf{df_fma(df_neg(w.re), iw, r.re), df_fma(w.im, iw, r.im)};   // r - 1/w
+    cdf rk, w;
+    df iw;
+    cplx D64 = cx(0.0, 0.0), zi64 = cx(0.0, 0.0);
+    if (DN64) {
+        const cplx z64 = cx(m64.x * x64, m64.y * x64);
+        const int nmx64 = (int)rint(fmax((double)nmax, cabs(z64)) + 16.0);
+        zi64 = 1.0 / z64;
+        for (int k = nmx64 - 1; k > nmax; --k) {
+            const cplx r = zi64 * (double)(k + 1);
+            D64 = r - cinv(D64 + r);
+        }
+    } else {
+        for (int k = nmax + warm; k > nmax; --k) {
+            const cdf r = cdf_mul_f(zinv, (float)(k + 1));   // (k+1)/z
+            const cdf w1 = cdf_add(D, r);
+            const df iw1 = df_rcp(df_fma(w1.re, w1.re, df_mul(w1.im, w1.im)));
+            D = cdf{df_fma(df_neg(w1.re), iw1, r.re), df_fma(w1.im, iw1, r.im)};   // r - 1/w
+        }
+        rk = cdf_mul_f(zinv, (float)(nmax + 1));   // r_nmax = (nmax+1)/z
+        w = cdf_add(D, rk);                         // D_{nmax+1} + r_nmax
+        iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
     }
-    cdf rk = cdf_mul_f(zinv, (float)(nmax + 1));   // r_nmax = (nmax+1)/z
-    cdf w = cdf_add(D, rk);                         // D_{nmax+1} + r_nmax
-    df iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
     // psi_k, chi_k (pn) and psi_{k-1}, chi_{k-1} (pm); the row entry of the
     // next order is loaded one order ahead (its latency overlaps an order's
     // arithmetic)
-    float4 pn = rowd[nmax - 1];
-    float4 pm = nmax > 1 ? rowd[nmax - 2] : r0;
+    float4 pn = rowd[(nmax - 1) * rs];
+    float4 pm = nmax > 1 ? rowd[(nmax - 2) * rs] : r0;
     for (int k = nmax; k >= 1; --k) {
-        const float4 pnext = k > 2 ? rowd[k - 3] : r0;
-        D = cdf{df_fma(df_neg(w.re), iw, rk.re), df_fma(w.im, iw, rk.im)};   // D_k
-        if (k > 1) {
-            rk = cdf_mul_f(zinv, (float)k);   // r_{k-1} = k/z
-            w = cdf_add(D, rk);
-            iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
+        const float4 pnext = k > 2 ? rowd[(k - 3) * rs] : r0;
+        if (DN64) {
+            const cplx r = zi64 * (double)(k + 1);
+            D64 = r - cinv(D64 + r);   // D_k
+            D = cdf{df_from_f64(D64.re), df_from_f64(D64.im)};
+        } else {
+            D = cdf{df_fma(df_neg(w.re), iw, rk.re), df_fma(w.im, iw, rk.im)};   // D_k
+            if (k > 1) {
+                rk = cdf_mul_f(zinv, (float)k);   // r_{k-1} = k/z
+                w = cdf_add(D, rk);
+                iw = df_rcp(df_fma(w.re, w.re, df_mul(w.im, w.im)));
+            }
         }
         const df nx = df_mul_f(xi, (float)k);   // k/x
         const df dar = df_fma(D.re, mi_re, df_fma(df_neg(D.im), mi_im, nx));   // Re(D/m) + k/x
@@ -372,22 +398,29 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int6
     split_rows(v, i, ex, nmax, cf + c, 1, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
 }
 
-__global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_inst, float4 *__restrict__ cf,
+// One thread per instance; the threads of a unit are padded to whole warps
+// (n_pad = 32 ngrp per unit) so that a warp is one group of 32 sizes and its
+// row loads and coefficient stores are one contiguous segment per order.
+template <bool DN64>
+__global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_threads, float4 *__restrict__ cf,
                                                           int *__restrict__ eexp, int *__restrict__ eunit,
                                                           int *flags, const int *__restrict__ tile_cbase,
                                                           const int64_t *__restrict__ unit_cbase, int ntiles,
                                                           uint8_t *__restrict__ asplit)
 {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_inst) return;
-    const int i = (int)(t % v.n_size);
-    const int64_t unit = t / v.n_size;
+    const int64_t tp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tp >= n_threads) return;
+    const int n_pad = 32 * v.ngrp;
+    const int i = (int)(tp % n_pad);
+    const int64_t unit = tp / n_pad;
+    if (i >= v.n_size) return;
+    const int64_t t = unit * v.n_size + i;   // the instance
     const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
     const int le = v.le(lam);
     const int64_t row = (int64_t)le * v.n_size + i;
     const int64_t o = v.off[row];
     const int nmax = (int)(v.off[row + 1] - o);
-    const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
+    const int64_t gb = v.grel[(int64_t)le * (v.ngrp + 1) + (i >> 5)] + (i & 31);   // order 1 within the block
     const float4 rc0 = v.rowcd[2 * row], rc1 = v.rowcd[2 * row + 1];
     const df xi = df{rc1.x, rc1.y};
     // an instance of one 16-order chunk keeps its coefficients in this
@@ -396,14 +429,16 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
     extern __shared__ float4 cf_stage[];
     const bool staged = nmax <= TC_KC16;
     EmitMixed emit;
-    emit.cf = staged ? cf_stage + threadIdx.x : cf + c;
-    emit.cs = staged ? (int)blockDim.x : 1;
+    emit.cf = staged ? cf_stage + threadIdx.x : cf + v.gunit[unit] + gb;
+    emit.cs = staged ? (int)blockDim.x : 32;
     emit.amax = 0.f;
     emit.ab = emit.sca = emit.asy = emit.qbr = emit.qbi = 0.f;
     emit.ab_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
     emit.pa = emit.pb = make_float2(0.f, 0.f);
     emit.inv_n1 = __frcp_rn((float)(nmax + 1));
-    homog_core_mixed(v.hdf + 4 * unit, rc0, xi, rc1.z, v.pcd + o, nmax, emit);
+    const float4 *rowd = v.pcd + v.grow[le] + gb;
+    if (DN64) homog_core_mixed<true>(v.hdf + 4 * unit, rc0, xi, rc1.z, rowd, 32, nmax, emit, v.m[unit], v.xg[row]);
+    else homog_core_mixed<false>(v.hdf + 4 * unit, rc0, xi, rc1.z, rowd, 32, nmax, emit);
     // efficiencies from the compensated sums (value = sum - compensation), in
     // pairs; one FP64 addition per output
     const df iy2 = df_mul(xi, xi);   // 1 / x^2
@@ -427,14 +462,26 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_i
 }
 
 // The psi/chi rows as FP32 pairs (psi hi, lo, chi hi, lo) for the mixed
-// recurrences.
-__global__ void k_rows_df(int64_t n, const double2 *__restrict__ src, float4 *__restrict__ dst)
+// recurrences, from the CSR rows pc to the order-major groups of 32 sizes
+// (TabView::pcd); one thread per size row, the threads of a wavelength block
+// padded to whole groups, so that a warp's stores of an order are one
+// contiguous segment.
+__global__ void k_rows_df(TabView v, int64_t n_threads, const double2 *__restrict__ src, float4 *__restrict__ dst)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        const double2 v = src[i];
-        const df p = df_from_f64(v.x), c = df_from_f64(v.y);
-        dst[i] = make_float4(p.hi, p.lo, c.hi, c.lo);
+    const int64_t tp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tp >= n_threads) return;
+    const int n_pad = 32 * v.ngrp;
+    const int i = (int)(tp % n_pad);
+    const int le = (int)(tp / n_pad);
+    if (i >= v.n_size) return;
+    const int64_t row = (int64_t)le * v.n_size + i;
+    const int64_t o = v.off[row];
+    const int nmax = (int)(v.off[row + 1] - o);
+    float4 *d = dst + v.grow[le] + v.grel[(int64_t)le * (v.ngrp + 1) + (i >> 5)] + (i & 31);
+    for (int k = 0; k < nmax; ++k) {
+        const double2 w = src[o + k];
+        const df p = df_from_f64(w.x), c = df_from_f64(w.y);
+        d[32 * k] = make_float4(p.hi, p.lo, c.hi, c.lo);
     }
 }
 
@@ -1244,9 +1291,13 @@ static int coef_stage_attr(gbmie_ctx *ctx)
     static volatile bool done[64];
     const int dev = ctx->device;
     if (dev >= 0 && dev < 64 && done[dev]) return GBMIE_OK;
-    const int st = ctx_cuda(ctx, cudaFuncSetAttribute(k_tab_coeffs_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      (int)coef_stage_bytes(256)),
-                            "k_tab_coeffs_mixed shared memory");
+    int st = ctx_cuda(ctx, cudaFuncSetAttribute(k_tab_coeffs_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)coef_stage_bytes(256)),
+                      "k_tab_coeffs_mixed shared memory");
+    if (st == GBMIE_OK)
+        st = ctx_cuda(ctx, cudaFuncSetAttribute(k_tab_coeffs_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)coef_stage_bytes(256)),
+                      "k_tab_coeffs_mixed shared memory");
     if (st == GBMIE_OK && dev >= 0 && dev < 64) done[dev] = true;
     return st;
 }
@@ -1259,7 +1310,8 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     int *eexp = (int *)(scr + p->o_eexp);
     int *eunit = (int *)(scr + p->o_eunit);
     ctx_pre_launch(ctx);
-    k_rows_df<<<(unsigned)ceil_div64(p->pc_total, 256), 256, 0, st>>>(p->pc_total, v.pc, v.pcd);
+    const int64_t n_rows_pad = (int64_t)p->n_le * 32 * p->ngrp;
+    k_rows_df<<<(unsigned)ceil_div64(n_rows_pad, 256), 256, 0, st>>>(v, n_rows_pad, v.pc, v.pcd);
     GBMIE_TRY(ctx_check_launch(ctx, "k_rows_df"));
     {
         const int64_t nrows = (int64_t)p->n_le * v.n_size;
@@ -1280,10 +1332,11 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed_coated"));
     } else {
         GBMIE_TRY(coef_stage_attr(ctx));
-        k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, p->coef_block), p->coef_block,
-                             coef_stage_bytes(p->coef_block), st>>>(v, p->n_inst, cf, eexp, eunit, ctx->d_flags,
-                                                                   p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
-        GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed"));
+        auto kern = p->dn_fp64 ? k_tab_coeffs_mixed<true> : k_tab_coeffs_mixed<false>;
+        const int64_t nthr = p->n_units * 32 * p->ngrp;
+        kern<<<(unsigned)ceil_div64(nthr, p->coef_block), p->coef_block, coef_stage_bytes(p->coef_block), st>>>(
+            v, nthr, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
+        GBMIE_TRY(ctx_check_launch(ctx, p->dn_fp64 ? "k_tab_coeffs_mixed_dn64" : "k_tab_coeffs_mixed"));
     }
     GBMIE_TRY(ctx_cuda(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0), "join"));   // the PSD weights
     TcArgs a;
@@ -1365,8 +1418,10 @@ int tune_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr,
             for (int rep = 0; rep < 2; ++rep) {
                 const int bs = blocks[c];
                 cudaEventRecord(e0, st);
-                k_tab_coeffs_mixed<<<(unsigned)ceil_div64(p->n_inst, bs), bs, coef_stage_bytes(bs), st>>>(
-                    v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles,
+                auto kern = p->dn_fp64 ? k_tab_coeffs_mixed<true> : k_tab_coeffs_mixed<false>;
+                const int64_t nthr = p->n_units * 32 * p->ngrp;
+                kern<<<(unsigned)ceil_div64(nthr, bs), bs, coef_stage_bytes(bs), st>>>(
+                    v, nthr, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles,
                     (uint8_t *)(scr + p->o_asplit));
                 cudaEventRecord(e1, st);
                 GBMIE_TRY(ctx_cuda(ctx, cudaEventSynchronize(e1), "tune coefficients"));

@@ -38,6 +38,11 @@ struct gbmie_table_plan {
     int64_t *unit_cbase; // [n_units] first chunk of a unit (plan-owned)
     int64_t n_chunks;    // chunks of the whole table
     size_t o_asplit;
+    // order-major size groups of the mixed recurrences (TabView grel, grow,
+    // gunit: one plan-owned block)
+    int ngrp;
+    int64_t *grp;
+    int64_t pcg_total, cfg_total;
     GsfTables gsf;
     int has_gsf;
     int gsf_entry;       // its context cache entry, or -1 when plan-owned
@@ -63,6 +68,9 @@ struct gbmie_table_plan {
     // flags a timeout (default GBMIE_WAIT_LIMIT_DEFAULT;
     // gbmie_table_plan_set_wait_limit)
     uint32_t wait_limit;
+    // mixed path: D_n recurrence in FP64 from the reference's start
+    // (gbmie_table_plan_set_dn_fp64; a measurement variant)
+    int dn_fp64;
 };
 #define GBMIE_WAIT_LIMIT_DEFAULT (1u << 26)
 
@@ -113,7 +121,15 @@ struct TabView {
     double4 *rowc;      // per size row: sin x, cos x, 1/x
     HomogIndex *hidx;   // per unit: medium constants of the recurrences
     const double2 *pq;
-    float4 *pcd;        // pc as FP32 pairs: psi hi, lo, chi hi, lo (mixed path)
+    // pc as FP32 pairs (psi hi, lo, chi hi, lo; mixed path) in order-major
+    // groups of 32 sizes: order k of size i = 32 g + l of wavelength block le
+    // at pcd[grow[le] + grel[le][g] + 32 (k - 1) + l]; the mixed
+    // coefficients (cf) of unit u in the same layout from gunit[u]
+    float4 *pcd;
+    int ngrp;                   // groups per wavelength block, (n_size + 31) / 32
+    const int64_t *grel;        // [n_le][ngrp + 1] group bases within a block
+    const int64_t *grow;        // [n_le] block bases of pcd
+    const int64_t *gunit;       // [n_units] block bases of cf
     float4 *hdf;        // per unit, FP32 pairs: m, 1/m, x/z, (|z|/x) (mixed path)
     float4 *rowcd;      // per size row, FP32 pairs: (sin x, cos x), (1/x, x) (mixed path)
     // PSD weights, their radius moments and reff0 do not depend on the

@@ -198,6 +198,13 @@ class TablePlan(object):
         self.ctx.check(self.ctx.lib.gbmie_table_plan_set_wait_limit(self.h, -1 if tries is None else int(tries)),
                        "gbmie_table_plan_set_wait_limit")
 
+    def set_dn_fp64(self, enable):
+        """Mixed plans of homogeneous spheres: run the D_n recurrence in FP64
+        from the reference's start (True) or in double-float pairs with the
+        shortened warm-up (False, the default)."""
+        self.ctx.check(self.ctx.lib.gbmie_table_plan_set_dn_fp64(self.h, int(bool(enable))),
+                       "gbmie_table_plan_set_dn_fp64")
+
     def tuning(self):
         """{'tuned', 'plain_per_bucket', 'plain_chunk' [5], 'plain_threads'
         [5], 'coef_block', 'tc_window'}: the plan's launch parameters (nmax

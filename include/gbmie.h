@@ -291,6 +291,13 @@ int gbmie_table_plan_autotune(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmi
  * captured graph of the plan (synchronising the context stream first).  No
  * counterpart in the reference (its loops run in Python). */
 int gbmie_table_plan_set_wait_limit(gbmie_table_plan *plan, int64_t tries);
+/* Mixed plans of homogeneous spheres: enable = 1 runs the downward D_n
+ * recurrence of the coefficient kernel in FP64 from the reference's start
+ * (zero at round(max(nmax, |m x|) + 16), pymiecoated/mie_coeffs.py:101,
+ * 119-121) instead of double-float pairs with a warm-up shortened to an
+ * e^-23 damping; 0 restores the default.  A measurement variant (the cost of
+ * keeping D_n in FP64 on this GPU); drops a captured graph of the plan. */
+int gbmie_table_plan_set_dn_fp64(gbmie_table_plan *plan, int32_t enable);
 /* params[16]: [0] 1 when tuned (or taken from the cache); [1] 1 = the plain
  * angular kernel runs one launch per nmax bucket, 0 = one launch over the
  * whole grid; [2..6] sizes per block and [7..11] angles per pass of the four

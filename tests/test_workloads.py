@@ -147,6 +147,32 @@ def test_sulfate_table_full_gpu():
     _check_units(a, ref, units, 64)
 
 
+@pytest.mark.gpu
+def test_dn_fp64_variant_gpu():
+    """The mixed path with its D_n recurrence in FP64 from the reference's
+    start (gbmie_table_plan_set_dn_fp64) against the FP64 table, on reduced
+    dust-like bins (Im m 1e-4..1e-2, x up to 314) and a reduced sulfate-like
+    table: every output within the mixed path's 1e-6; the default
+    double-float form stays within 1e-6 of it too."""
+    from geosmie_gb300.table import TablePlan
+    small, _ = workloads.dust_bins(n_lambda=4, n_sub=200)
+    sul, _ = workloads.sulfate_table(n_rh=4, n_lambda=5, n_radii=300)
+    for spec in small[3:] + [sul]:
+        a, b = _mixed_plain(spec, n_gsf=16)
+        plan = TablePlan(spec, precision=1, n_gsf=16)
+        plan.set_dn_fp64(True)
+        plan.run()
+        c = plan.results()
+        plan.set_dn_fp64(False)
+        plan.run()
+        d = plan.results()
+        plan.close()
+        _check_mixed(a, c, 16)
+        for k in SCAT:
+            assert np.max(np.abs(d[k] - b[k]) / np.abs(a["p11"])) < 1e-10, k   # the default form is unchanged
+        assert np.max(np.abs(c["p11"] - b["p11"]) / np.abs(a["p11"])) < 1e-6
+
+
 def test_coated_workload_spec_cpu():
     spec, _ = workloads.coated_bc()
     assert spec["m"].shape == (30, 200, 1) and spec["m_core"].shape == (30, 200, 1)
