@@ -478,8 +478,12 @@ def main():
     ap.add_argument("--other-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="reduced sulfate table (quick check, not a bench line)")
+    ap.add_argument("--lambdas", type=int, default=60, help="wavelengths of the sulfate table (profiling subsets)")
+    ap.add_argument("--rh", type=int, default=36, help="RH values of the sulfate table (profiling subsets)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.lambdas != 60 or args.rh != 36:
+        args.small = True   # a profiling subset, not a bench line
     if args.impl == "reference":
         return run_reference(args)
 
@@ -547,8 +551,13 @@ def main():
         mixed-vs-FP64 errors, the end-to-end rate through run_tables, the
         roofline of the dominant mixed kernel; keeps both tables' results."""
         if args.small and cfg == 3:
-            specs = [workloads.sulfate_table(n_rh=6, n_lambda=10, n_radii=500)[0]]
-            desc, n_gsf, nodes = "reduced sulfate table (quick check)", 64, 0
+            if args.lambdas != 60 or args.rh != 36:
+                specs = [workloads.sulfate_table(n_rh=args.rh, n_lambda=args.lambdas)[0]]
+                desc = "sulfate table subset: %d RH x %d wavelengths (profiling)" % (args.rh, args.lambdas)
+            else:
+                specs = [workloads.sulfate_table(n_rh=6, n_lambda=10, n_radii=500)[0]]
+                desc = "reduced sulfate table (quick check)"
+            n_gsf, nodes = 64, 0
         else:
             specs, desc, n_gsf, nodes, _ = build_config(cfg)
         tot, per = config_counts(cfg) if not args.small else (workloads.work_counts(specs[0]),) * 2
@@ -661,6 +670,8 @@ def main():
                     "mixed_vs_plain_speedup": r["ms_plain"] / r["ms"],
                     "e2e": r["e2e"]["value"],
                     "roofline": {k: roof.get(k) for k in ("kernel", "bound", "achieved", "unit", "frac")},
+                    "top_kernels_ms": {k: v["ms_per_launch"] for k, v in
+                                       sorted(r["kernels"].items(), key=lambda kv: -kv[1]["share"])[:3]},
                     "cpu_baseline": r["cpu_baseline"]["value"] if r["cpu_baseline"] else None,
                     "mixed_vs_fp64": r["acc_mixed_vs_fp64"],
                     "vs_oracle": {k: (r["acc_vs_oracle"][k] if r["acc_vs_oracle"] else None)
