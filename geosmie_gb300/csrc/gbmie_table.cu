@@ -44,15 +44,23 @@ __global__ void k_tab_make_x(int n_le, int n_size, int grid_kind, const double *
 // ---------------------------------------------------------------------------
 // run kernels
 // ---------------------------------------------------------------------------
+// psi/chi rows per (wavelength block, size) in FP64 (CSR, pc) and, for
+// homogeneous mixed plans (pairs = 1), also as FP32 pairs in the order-major
+// groups of 32 sizes the mixed recurrences read (TabView::pcd).
 __global__ void __launch_bounds__(128) k_tab_psi_chi(int64_t nrows, const double *__restrict__ xg,
                                                      const int64_t *__restrict__ off, double2 *__restrict__ pc,
-                                                     double4 *__restrict__ rowc)
+                                                     double4 *__restrict__ rowc, TabView v, int pairs)
 {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nrows) return;
     const int64_t o = off[j];
     const double x = xg[j];
-    psi_chi_row(x, (int)(off[j + 1] - o), pc + o);
+    float4 *pr = nullptr;
+    if (pairs) {
+        const int le = (int)(j / v.n_size), i = (int)(j - (int64_t)le * v.n_size);
+        pr = v.pcd + v.grow[le] + v.grel[(int64_t)le * (v.ngrp + 1) + (i >> 5)] + (i & 31);
+    }
+    psi_chi_row(x, (int)(off[j + 1] - o), pc + o, pr, 32);
     double s, c;
     sincos(x, &s, &c);
     rowc[j] = make_double4(s, c, 1.0 / x, 0.0);
@@ -1094,7 +1102,8 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     cudaStream_t st = ctx->stream;
     const int64_t nrows = (int64_t)p->n_le * d.n_size;
     ctx_pre_launch(ctx);
-    k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc, v.rowc);
+    k_tab_psi_chi<<<(unsigned)ceil_div64(nrows, 128), 128, 0, st>>>(nrows, p->xg, p->off, v.pc, v.rowc, v,
+                                                                    d.precision == GBMIE_MIXED && !d.m_core);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_psi_chi"));
     ctx_pre_launch(ctx);
     k_tab_index<<<(unsigned)ceil_div64(p->n_units, 128), 128, 0, st>>>(p->n_units, v.m, v.hidx, ctx->d_flags);

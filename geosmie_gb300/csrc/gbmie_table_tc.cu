@@ -461,30 +461,6 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_t
     split_rows(v, i, ex, nmax, emit.cf, emit.cs, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
 }
 
-// The psi/chi rows as FP32 pairs (psi hi, lo, chi hi, lo) for the mixed
-// recurrences, from the CSR rows pc to the order-major groups of 32 sizes
-// (TabView::pcd); one thread per size row, the threads of a wavelength block
-// padded to whole groups, so that a warp's stores of an order are one
-// contiguous segment.
-__global__ void k_rows_df(TabView v, int64_t n_threads, const double2 *__restrict__ src, float4 *__restrict__ dst)
-{
-    const int64_t tp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tp >= n_threads) return;
-    const int n_pad = 32 * v.ngrp;
-    const int i = (int)(tp % n_pad);
-    const int le = (int)(tp / n_pad);
-    if (i >= v.n_size) return;
-    const int64_t row = (int64_t)le * v.n_size + i;
-    const int64_t o = v.off[row];
-    const int nmax = (int)(v.off[row + 1] - o);
-    float4 *d = dst + v.grow[le] + v.grel[(int64_t)le * (v.ngrp + 1) + (i >> 5)] + (i & 31);
-    for (int k = 0; k < nmax; ++k) {
-        const double2 w = src[o + k];
-        const df p = df_from_f64(w.x), c = df_from_f64(w.y);
-        d[32 * k] = make_float4(p.hi, p.lo, c.hi, c.lo);
-    }
-}
-
 // Per-unit and per-row constants of the mixed recurrences as FP32 pairs:
 // hdf[4 u] = m, 1/m, x/z (1/z = (x/z)(1/x)), (|z|/x); rowcd[2 j] = (sin x, cos x),
 // (1/x, x).
@@ -1309,10 +1285,6 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     float4 *cf = (float4 *)(scr + p->o_cf);
     int *eexp = (int *)(scr + p->o_eexp);
     int *eunit = (int *)(scr + p->o_eunit);
-    ctx_pre_launch(ctx);
-    const int64_t n_rows_pad = (int64_t)p->n_le * 32 * p->ngrp;
-    k_rows_df<<<(unsigned)ceil_div64(n_rows_pad, 256), 256, 0, st>>>(v, n_rows_pad, v.pc, v.pcd);
-    GBMIE_TRY(ctx_check_launch(ctx, "k_rows_df"));
     {
         const int64_t nrows = (int64_t)p->n_le * v.n_size;
         const int64_t nc = nrows > p->n_units ? nrows : p->n_units;

@@ -30,7 +30,9 @@ __device__ __forceinline__ int miller_start(double az, int nmax)
 // upward recurrence from chi_0 = cos x, chi_{-1} = -sin x (stable: chi is
 // the dominant solution).  row1 may alias the coefficient output (the
 // homogeneous kernels overwrite it in place).
-__device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1)
+// pair (or NULL): the same rows also as FP32 pairs (psi hi, lo, chi hi, lo)
+// at pair[(n - 1) * pstride], for the mixed recurrences.
+__device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1, float4 *pair = nullptr, int pstride = 1)
 {
     const int N = miller_start(x, nmax);
     const double xinv = 1.0 / x;
@@ -55,7 +57,13 @@ __device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1)
         const double chin = (double)(2 * n - 1) * xinv * chi - chim1;
         chim1 = chi;
         chi = chin;
-        row1[n - 1] = make_double2(scale * row1[n - 1].x, chi);
+        const double psi = scale * row1[n - 1].x;
+        row1[n - 1] = make_double2(psi, chi);
+        if (pair) {
+            const float ph = __double2float_rn(psi), ch = __double2float_rn(chi);
+            pair[(size_t)(n - 1) * pstride] = make_float4(ph, __double2float_rn(psi - (double)ph), ch,
+                                                          __double2float_rn(chi - (double)ch));
+        }
     }
 }
 
