@@ -707,6 +707,7 @@ static void plan_free(gbmie_table_plan *p)
     if (p->brange) cudaFreeAsync(p->brange, s);
     if (p->unit_cbase) cudaFreeAsync(p->unit_cbase, s);
     if (p->grp) cudaFreeAsync(p->grp, s);
+    if (p->ctasks) cudaFreeAsync(p->ctasks, s);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
     if (p->has_gsf && p->gsf_entry >= 0) table_gsf_release(p->ctx, p->gsf_entry);
@@ -923,6 +924,44 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
             if (st == GBMIE_OK)
                 st = ctx_cuda(ctx, cudaMemcpyAsync(p->grp, hg, sizeof(int64_t) * ngrp_all, cudaMemcpyHostToDevice, ctx->stream),
                               "size groups copy");
+            // tasks of the persistent coefficient kernel: (wavelength block,
+            // group) by decreasing largest nmax (stable), each with every
+            // unit of that block
+            if (st == GBMIE_OK) {
+                const int nlg = p->n_le * p->ngrp;
+                struct G { int64_t gm; int lg; };
+                G *gs = (G *)malloc(sizeof(G) * (size_t)nlg);
+                const int64_t upl = d.grid_kind == GBMIE_GRID_X ? p->n_units : (int64_t)d.n_rh * d.n_comp;
+                int2 *ht = (int2 *)malloc(sizeof(int2) * (size_t)nlg * (size_t)upl);
+                if (!gs || !ht) st = GBMIE_ERR_NOMEM;
+                for (int k = 0; st == GBMIE_OK && k < nlg; ++k) {
+                    const int le = k / p->ngrp, g = k % p->ngrp;
+                    const int64_t *rel = hg + (size_t)le * (p->ngrp + 1);
+                    gs[k] = G{(rel[g + 1] - rel[g]) / 32, k};
+                }
+                if (st == GBMIE_OK) {
+                    qsort(gs, (size_t)nlg, sizeof(G), [](const void *a, const void *b) -> int {
+                        const G *x = (const G *)a, *y = (const G *)b;
+                        if (x->gm != y->gm) return x->gm > y->gm ? -1 : 1;
+                        return x->lg - y->lg;
+                    });
+                    int64_t nt = 0;
+                    for (int k = 0; k < nlg; ++k) {
+                        const int le = gs[k].lg / p->ngrp, g = gs[k].lg % p->ngrp;
+                        const int64_t u0 = d.grid_kind == GBMIE_GRID_X ? 0 : (int64_t)le * upl;
+                        for (int64_t u = u0; u < u0 + upl; ++u) ht[nt++] = make_int2((int)u, g);
+                    }
+                    p->n_ctasks = (int)nt;
+                    st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->ctasks, sizeof(int2) * (size_t)nt, ctx->stream),
+                                  "coefficient tasks");
+                    if (st == GBMIE_OK)
+                        st = ctx_cuda(ctx, cudaMemcpyAsync(p->ctasks, ht, sizeof(int2) * (size_t)nt, cudaMemcpyHostToDevice,
+                                                           ctx->stream),
+                                      "coefficient tasks copy");
+                }
+                free(gs);
+                free(ht);
+            }
             free(hg);
             if (st == GBMIE_OK) st = ctx_cuda(ctx, cudaMallocAsync((void **)&p->unit_order, sizeof(int) * p->n_units, ctx->stream), "unit order");
             if (st == GBMIE_OK)
@@ -1000,6 +1039,7 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_eexp = carve(mixed ? sizeof(int) * (size_t)p->n_inst : 16);
         p->o_eunit = carve(mixed ? sizeof(int) * (size_t)p->n_units : 16);
         p->o_asplit = carve(mixed ? (size_t)16384 * (size_t)p->n_chunks : 16);
+        p->o_cnext = carve(16);
         p->o_pcf = carve(mixed ? sizeof(float4) * (size_t)p->pcg_total : 16);
         p->o_hdf = carve(mixed ? 4 * sizeof(float4) * (size_t)p->n_units : 16);
         p->o_rowcd = carve(mixed ? 2 * sizeof(float4) * (size_t)p->n_le * d.n_size : 16);

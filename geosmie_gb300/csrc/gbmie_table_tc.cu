@@ -401,19 +401,19 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int6
 // One thread per instance; the threads of a unit are padded to whole warps
 // (n_pad = 32 ngrp per unit) so that a warp is one group of 32 sizes and its
 // row loads and coefficient stores are one contiguous segment per order.
+// One instance (unit, size i) of the mixed coefficients: the recurrences,
+// the efficiencies, the instance's exponent and its rows of the
+// contraction's split operand.  stage: this thread's column of the block's
+// shared staging (stride stage_stride); an instance of one 16-order chunk
+// keeps its coefficients there until split_rows reads them (no global round
+// trip), longer ones go through cf.
 template <bool DN64>
-__global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_threads, float4 *__restrict__ cf,
-                                                          int *__restrict__ eexp, int *__restrict__ eunit,
-                                                          int *flags, const int *__restrict__ tile_cbase,
-                                                          const int64_t *__restrict__ unit_cbase, int ntiles,
-                                                          uint8_t *__restrict__ asplit)
+__device__ __forceinline__ void coeffs_mixed_instance(const TabView &v, int64_t unit, int i, float4 *__restrict__ cf,
+                                                      float4 *stage, int stage_stride, int *__restrict__ eexp,
+                                                      int *__restrict__ eunit, const int *__restrict__ tile_cbase,
+                                                      const int64_t *__restrict__ unit_cbase, int ntiles,
+                                                      uint8_t *__restrict__ asplit)
 {
-    const int64_t tp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tp >= n_threads) return;
-    const int n_pad = 32 * v.ngrp;
-    const int i = (int)(tp % n_pad);
-    const int64_t unit = tp / n_pad;
-    if (i >= v.n_size) return;
     const int64_t t = unit * v.n_size + i;   // the instance
     const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
     const int le = v.le(lam);
@@ -423,14 +423,10 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_t
     const int64_t gb = v.grel[(int64_t)le * (v.ngrp + 1) + (i >> 5)] + (i & 31);   // order 1 within the block
     const float4 rc0 = v.rowcd[2 * row], rc1 = v.rowcd[2 * row + 1];
     const df xi = df{rc1.x, rc1.y};
-    // an instance of one 16-order chunk keeps its coefficients in this
-    // thread's column of the block's shared staging until split_rows reads
-    // them (no global round trip); longer ones go through cf
-    extern __shared__ float4 cf_stage[];
     const bool staged = nmax <= TC_KC16;
     EmitMixed emit;
-    emit.cf = staged ? cf_stage + threadIdx.x : cf + v.gunit[unit] + gb;
-    emit.cs = staged ? (int)blockDim.x : 32;
+    emit.cf = staged ? stage : cf + v.gunit[unit] + gb;
+    emit.cs = staged ? stage_stride : 32;
     emit.amax = 0.f;
     emit.ab = emit.sca = emit.asy = emit.qbr = emit.qbi = 0.f;
     emit.ab_c = emit.sca_c = emit.asy_c = emit.qbr_c = emit.qbi_c = 0.f;
@@ -459,6 +455,52 @@ __global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, int64_t n_t
     eexp[t] = ex;
     atomicMax(eunit + unit, ex);
     split_rows(v, i, ex, nmax, emit.cf, emit.cs, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
+}
+
+// Persistent: a grid that fills the GPU once (blocks resident per SM x SMs);
+// every warp takes tasks -- one group of 32 sizes of one unit, a lane per
+// size -- from a global counter until none is left.  The task list (plan
+// time) orders the groups by decreasing largest nmax (heavy tasks first, so
+// that the last ones to run are light) and no warp waits for its block's
+// other warps, so that the SMs stay filled to the end: with a thread per
+// instance and one block per 64 or 128 sizes, blocks held their slots until
+// their slowest warp finished and the SMs ran at about 12 of the 20 warps
+// their registers allow.
+template <bool DN64>
+__global__ void __launch_bounds__(256) k_tab_coeffs_mixed(TabView v, const int2 *__restrict__ tasks, int ntasks,
+                                                          int *__restrict__ next, float4 *__restrict__ cf,
+                                                          int *__restrict__ eexp, int *__restrict__ eunit,
+                                                          const int *__restrict__ tile_cbase,
+                                                          const int64_t *__restrict__ unit_cbase, int ntiles,
+                                                          uint8_t *__restrict__ asplit)
+{
+    extern __shared__ float4 cf_stage[];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(next, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntasks) break;
+        const int2 tk = tasks[t];   // (unit, group)
+        const int i = 32 * tk.y + lane;
+        if (i < v.n_size)
+            coeffs_mixed_instance<DN64>(v, tk.x, i, cf, cf_stage + threadIdx.x, (int)blockDim.x, eexp, eunit,
+                                        tile_cbase, unit_cbase, ntiles, asplit);
+        __syncwarp();
+    }
+}
+
+// blocks of k_tab_coeffs_mixed resident per SM at `block` threads, times the SMs
+static int coef_grid(gbmie_ctx *ctx, bool dn64, int block, int *grid)
+{
+    int nb = 0, nsm = 0;
+    GBMIE_TRY(ctx_cuda(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                &nb, dn64 ? k_tab_coeffs_mixed<true> : k_tab_coeffs_mixed<false>, block,
+                                TC_KC16 * sizeof(float4) * (size_t)block),
+                       "coefficient occupancy"));
+    GBMIE_TRY(ctx_cuda(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device), "SM count"));
+    *grid = (nb > 0 ? nb : 1) * nsm;
+    return GBMIE_OK;
 }
 
 // Per-unit and per-row constants of the mixed recurrences as FP32 pairs:
@@ -1305,9 +1347,13 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     } else {
         GBMIE_TRY(coef_stage_attr(ctx));
         auto kern = p->dn_fp64 ? k_tab_coeffs_mixed<true> : k_tab_coeffs_mixed<false>;
-        const int64_t nthr = p->n_units * 32 * p->ngrp;
-        kern<<<(unsigned)ceil_div64(nthr, p->coef_block), p->coef_block, coef_stage_bytes(p->coef_block), st>>>(
-            v, nthr, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
+        int grid = 0;
+        GBMIE_TRY(coef_grid(ctx, p->dn_fp64, p->coef_block, &grid));
+        int *next = (int *)(scr + p->o_cnext);
+        GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(next, 0, sizeof(int), st), "task counter"));
+        ctx_pre_launch(ctx);
+        kern<<<grid, p->coef_block, coef_stage_bytes(p->coef_block), st>>>(
+            v, p->ctasks, p->n_ctasks, next, cf, eexp, eunit, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
         GBMIE_TRY(ctx_check_launch(ctx, p->dn_fp64 ? "k_tab_coeffs_mixed_dn64" : "k_tab_coeffs_mixed"));
     }
     GBMIE_TRY(ctx_cuda(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0), "join"));   // the PSD weights
@@ -1389,12 +1435,15 @@ int tune_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr,
         for (int c = 0; c < 3; ++c)
             for (int rep = 0; rep < 2; ++rep) {
                 const int bs = blocks[c];
-                cudaEventRecord(e0, st);
                 auto kern = p->dn_fp64 ? k_tab_coeffs_mixed<true> : k_tab_coeffs_mixed<false>;
-                const int64_t nthr = p->n_units * 32 * p->ngrp;
-                kern<<<(unsigned)ceil_div64(nthr, bs), bs, coef_stage_bytes(bs), st>>>(
-                    v, nthr, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles,
-                    (uint8_t *)(scr + p->o_asplit));
+                int grid = 0;
+                GBMIE_TRY(coef_grid(ctx, p->dn_fp64, bs, &grid));
+                int *next = (int *)(scr + p->o_cnext);
+                GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(next, 0, sizeof(int), st), "task counter"));
+                cudaEventRecord(e0, st);
+                kern<<<grid, bs, coef_stage_bytes(bs), st>>>(v, p->ctasks, p->n_ctasks, next, cf, eexp, eunit,
+                                                               p->tile_cbase, p->unit_cbase, p->ntiles,
+                                                               (uint8_t *)(scr + p->o_asplit));
                 cudaEventRecord(e1, st);
                 GBMIE_TRY(ctx_cuda(ctx, cudaEventSynchronize(e1), "tune coefficients"));
                 float ms = 0.f;

@@ -43,6 +43,12 @@ struct gbmie_table_plan {
     int ngrp;
     int64_t *grp;
     int64_t pcg_total, cfg_total;
+    // tasks of the persistent mixed coefficient kernel: (unit, group) pairs
+    // by decreasing largest nmax of the group (plan-owned), and the scratch
+    // offset of its task counter
+    int2 *ctasks;
+    int n_ctasks;
+    size_t o_cnext;
     GsfTables gsf;
     int has_gsf;
     int gsf_entry;       // its context cache entry, or -1 when plan-owned
