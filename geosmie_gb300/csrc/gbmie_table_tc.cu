@@ -365,37 +365,51 @@ __device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int 
     }
 }
 
-__global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, int64_t n_inst, float4 *__restrict__ cf,
-                                                                 int *__restrict__ eexp, int *__restrict__ eunit,
-                                                                 int *flags, const int *__restrict__ tile_cbase,
+// Persistent like k_tab_coeffs_mixed: warps take (unit, 32-size group)
+// tasks, heavy groups first, from the plan's task list.
+__global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, const int2 *__restrict__ tasks,
+                                                                 int ntasks, int *__restrict__ next,
+                                                                 float4 *__restrict__ cf, int *__restrict__ eexp,
+                                                                 int *__restrict__ eunit, int *flags,
+                                                                 const int *__restrict__ tile_cbase,
                                                                  const int64_t *__restrict__ unit_cbase, int ntiles,
                                                                  uint8_t *__restrict__ asplit)
 {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_inst) return;
-    const int i = (int)(t % v.n_size);
-    const int64_t unit = t / v.n_size;
-    const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
-    const int le = v.le(lam);
-    const int64_t row = (int64_t)le * v.n_size + i;
-    const int64_t o = v.off[row];
-    const int nmax = (int)(v.off[row + 1] - o);
-    const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
-    const double x = v.xg[row];
-    EmitCf emit{cf + c, 0.f};
-    EffSums es;
-    coated_table_instance(v, unit, c, o, nmax, x, emit, es, flags);
-    double e[6];
-    es.finish(x, e);
-    double *o4 = v.eff4 + t * 4;
-    o4[0] = e[0];
-    o4[1] = e[1];
-    o4[2] = e[3];
-    o4[3] = e[4];
-    const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
-    eexp[t] = ex;
-    atomicMax(eunit + unit, ex);
-    split_rows(v, i, ex, nmax, cf + c, 1, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int tk_i = 0;
+        if (lane == 0) tk_i = atomicAdd(next, 1);
+        tk_i = __shfl_sync(0xffffffffu, tk_i, 0);
+        if (tk_i >= ntasks) break;
+        const int2 tk = tasks[tk_i];   // (unit, group)
+        const int i = 32 * tk.y + lane;
+        const int64_t unit = tk.x;
+        if (i < v.n_size) {
+            const int64_t t = unit * v.n_size + i;
+            const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
+            const int le = v.le(lam);
+            const int64_t row = (int64_t)le * v.n_size + i;
+            const int64_t o = v.off[row];
+            const int nmax = (int)(v.off[row + 1] - o);
+            const int64_t c = v.unit_base[unit] + (o - v.off[(int64_t)le * v.n_size]);
+            const double x = v.xg[row];
+            EmitCf emit{cf + c, 0.f};
+            EffSums es;
+            coated_table_instance(v, unit, c, o, nmax, x, emit, es, flags);
+            double e[6];
+            es.finish(x, e);
+            double *o4 = v.eff4 + t * 4;
+            o4[0] = e[0];
+            o4[1] = e[1];
+            o4[2] = e[3];
+            o4[3] = e[4];
+            const int ex = emit.amax > 0.f ? ilogbf(emit.amax) : -1000;
+            eexp[t] = ex;
+            atomicMax(eunit + unit, ex);
+            split_rows(v, i, ex, nmax, cf + c, 1, split_idx(v, unit, i, tile_cbase, unit_cbase, ntiles), asplit);
+        }
+        __syncwarp();
+    }
 }
 
 // One thread per instance; the threads of a unit are padded to whole warps
@@ -646,6 +660,7 @@ struct TcArgs {
     int ntiles;
     int win;                     // accumulation window (16-order chunks, <= TC_NS)
     uint32_t wait_limit;         // tries of every pipeline wait (gbmie_table_plan_set_wait_limit)
+    int ntr, tpr;                // tile ranges per (unit, angle block) and tiles per range
     int *flags;
 };
 
@@ -684,6 +699,37 @@ static_assert(TC_SMEM_BYTES(5) <= 227 * 1024 && TC_SMEM_BYTES(8) <= 227 * 1024, 
 __device__ __forceinline__ int64_t tc_unit_index(int k, int cta, int G)
 {
     return (int64_t)k * G + ((k & 1) ? (G - 1 - cta) : cta);
+}
+
+// Work items of the contraction: (unit, angle block, range of tpr tiles),
+// units in decreasing-work order (unit_order), the k-th of CTA cta dealt as
+// above.  A (unit, block) split over several items, possibly on several
+// CTAs, is summed by the FP64 additions of the items' partial sums, so that
+// tables with few units (a single wavelength, or 20) still fill every SM.
+struct TcWork {
+    int64_t unit;
+    int ab, t0, t1;
+    bool valid;
+};
+__device__ __forceinline__ TcWork tc_work(const TcArgs &g, int k, int cta, int G, int nblocks, int ntl,
+                                          int64_t n_units)
+{
+    TcWork w;
+    const int64_t per = (int64_t)nblocks * g.ntr;
+    const int64_t widx = tc_unit_index(k, cta, G);
+    w.valid = widx < n_units * per;
+    if (!w.valid) {
+        w.unit = 0;
+        w.ab = w.t0 = w.t1 = 0;
+        return w;
+    }
+    const int64_t r = widx / per;
+    const int rem = (int)(widx - r * per);
+    w.ab = rem / g.ntr;
+    w.t0 = (rem - w.ab * g.ntr) * g.tpr;
+    w.t1 = min(ntl, w.t0 + g.tpr);
+    w.unit = g.unit_order[r];
+    return w;
 }
 
 template <int NB>
@@ -765,12 +811,13 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 b0_loads = 1;
             }
             for (int k = 0; ok; ++k) {
-                const int64_t uidx = tc_unit_index(k, cta, G);
-                if (uidx >= n_units) break;
-                const int64_t unit = g.unit_order[uidx];
+                const TcWork wk = tc_work(g, k, cta, G, nblocks, ntl, n_units);
+                if (!wk.valid) break;
+                const int64_t unit = wk.unit;
                 const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
                 const int64_t *off = v.off + (int64_t)v.le(lam) * v.n_size;
-                for (int ab = 0; ab < nblocks && ok; ++ab) {
+                {
+                    const int ab = wk.ab;
                     if (reload) {   // the producer reloads the resident slot
                         if (have_b0) mma_commit(b0_empty);
                         if (!mbar_wait_or_abort(b0_full, b0_loads & 1u, s_abort, TC_SLEEP_NS, g.wait_limit)) {
@@ -783,11 +830,11 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     const uint32_t aB0 = smem_u32(sB0 + (reload ? 0 : ab) * TC_A_BYTES);
                     // nmax of a tile's last size, loaded one tile ahead
                     auto last_of = [&](int t) { return min(TC_INST * (t + 1), v.n_size); };
-                    long long o1 = ldg_pin_s64(off + last_of(0)), o0 = ldg_pin_s64(off + last_of(0) - 1);
-                    for (int tile = 0; tile < ntl && ok; ++tile) {
+                    long long o1 = ldg_pin_s64(off + last_of(wk.t0)), o0 = ldg_pin_s64(off + last_of(wk.t0) - 1);
+                    for (int tile = wk.t0; tile < wk.t1 && ok; ++tile) {
                         const int t0 = tile * TC_INST, ntile = min(TC_INST, v.n_size - t0);
                         const int kt = (int)(o1 - o0);
-                        if (tile + 1 < ntl) {
+                        if (tile + 1 < wk.t1) {
                             o1 = ldg_pin_s64(off + last_of(tile + 1));
                             o0 = ldg_pin_s64(off + last_of(tile + 1) - 1);
                         }
@@ -878,16 +925,17 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 b0_phase = 0;
             }
             for (int k = 0; ok; ++k) {
-                const int64_t uidx = tc_unit_index(k, cta, G);
-                if (uidx >= n_units) break;
-                const int64_t unit = g.unit_order[uidx];
+                const TcWork wk = tc_work(g, k, cta, G, nblocks, ntl, n_units);
+                if (!wk.valid) break;
+                const int64_t unit = wk.unit;
                 const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
                 const int *tcb = g.tile_cbase + (size_t)v.le(lam) * (ntl + 1);
                 const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * (2 * TC_B_BYTES);
                 const int comp = (int)(unit % v.n_comp), rhi = (int)((unit / v.n_comp) % v.n_rh);
                 const float *uW = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
                 const int *uex = g.eexp + (size_t)unit * v.n_size;
-                for (int ab = 0; ab < nblocks && ok; ++ab) {
+                {
+                    const int ab = wk.ab;
                     const uint8_t *gA = (const uint8_t *)g.bt + (size_t)ab * nkc * TC_A_BYTES;
                     if (reload) {
                         if (b0_loads > 0 &&
@@ -902,11 +950,11 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                         ++b0_loads;
                     }
                     // chunk bases tcb[tile], tcb[tile + 1], loaded one tile ahead
-                    int cb0 = ldg_pin_s32(tcb), cb1 = ldg_pin_s32(tcb + 1);
-                    for (int tile = 0; tile < ntl && ok; ++tile) {
+                    int cb0 = ldg_pin_s32(tcb + wk.t0), cb1 = ldg_pin_s32(tcb + wk.t0 + 1);
+                    for (int tile = wk.t0; tile < wk.t1 && ok; ++tile) {
                         const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
                         const int base = cb0, nc = cb1 - cb0;
-                        if (tile + 1 < ntl) {
+                        if (tile + 1 < wk.t1) {
                             cb0 = cb1;
                             cb1 = ldg_pin_s32(tcb + tile + 2);
                         }
@@ -914,10 +962,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                         // PSD weights and exponents of the tile after it (the
                         // weights warp reads them a few items ahead; they were
                         // evicted by the coefficient operand)
-                        if (ab == 0 && tile + 1 < ntl)
+                        if (tile + 1 < wk.t1)
                             bulk_prefetch_l2(ua + (size_t)cb0 * (2 * TC_B_BYTES), (uint32_t)(cb1 - cb0) * (2 * TC_B_BYTES));
-                        if (tile + 2 < ntl || (tile + 2 - ntl < ntl && ab + 1 < nblocks)) {
-                            const int tp = tile + 2 < ntl ? tile + 2 : tile + 2 - ntl;
+                        if (tile + 2 < wk.t1) {
+                            const int tp = tile + 2;
                             const int t0 = tp * TC_INST, nt = min(TC_INST, v.n_size - t0);
                             auto pf = [&](const void *p, size_t bytes) {
                                 const uintptr_t a0 = (uintptr_t)p & ~(uintptr_t)15, a1 = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
@@ -976,17 +1024,19 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         // wait for item i's slot, so their latency overlaps it.
         struct UnitW {
             bool valid;
-            int comp, lr, E;
+            int comp, lr, E, t0, t1;
             const float *Wb;
             const int *ex;
             const int *tcb;
         };
         auto unit_w = [&](int k) -> UnitW {
             UnitW u;
-            const int64_t uidx = tc_unit_index(k, cta, G);
-            u.valid = uidx < n_units;
+            const TcWork wk = tc_work(g, k, cta, G, nblocks, ntl, n_units);
+            u.valid = wk.valid;
             if (!u.valid) return u;
-            const int unit = g.unit_order[uidx];
+            const int unit = (int)wk.unit;
+            u.t0 = wk.t0;
+            u.t1 = wk.t1;
             u.comp = unit % v.n_comp;
             u.lr = unit / v.n_comp;
             const int lam = u.lr / v.n_rh;
@@ -1017,26 +1067,22 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         };
         bool ok = true;
         uint32_t iw = 0;
-        int kq = 0, ab = 0, tile = 0, h = 0;
+        int kq = 0, h = 0;
         UnitW u = unit_w(0);
+        int tile = u.valid ? u.t0 : 0;
         // One step: issue the loads of the next item into nxt, wait for the
         // current item's slot, store it from cur.  Steps alternate the roles
         // of the two buffers (no register copies: a copy would wait for the
         // loads it copies).
         auto step = [&](const WItem &cur, WItem &nxt) {
             const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
-            int nk = kq, nab = ab, nt = tile, nh = h + 1;
+            int nk = kq, nt = tile, nh = h + 1;
             if (nh == 2 || TC_HALF * nh >= ntile) {
                 nh = 0;
-                if (++nt == ntl) {
-                    nt = 0;
-                    if (++nab == nblocks) {
-                        nab = 0;
-                        ++nk;
-                    }
-                }
+                if (++nt == u.t1) ++nk;   // the next work item
             }
             const UnitW un = nk == kq ? u : unit_w(nk);
+            if (nk != kq && un.valid) nt = un.t0;
             if (un.valid) load_item(un, nt, nh, nxt);
             const uint32_t slot = iw % TC_NW;
             int go = 1;
@@ -1062,12 +1108,11 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             ++iw;
             u = un;
             kq = nk;
-            ab = nab;
             tile = nt;
             h = nh;
         };
         WItem ia, ib;
-        if (u.valid) load_item(u, 0, 0, ia);
+        if (u.valid) load_item(u, u.t0, 0, ia);
         while (ok && u.valid) {
             step(ia, ib);
             if (!ok || !u.valid) break;
@@ -1091,7 +1136,9 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         constexpr int NP = (NB + 1) / 2;   // 16-byte weight loads per size: two bins each
         bool ok = true;
         uint32_t wce[2] = {0u, 0u}, ie = 0;   // windows read per issuer; items
-        int kq = 0, ab = 0, tile = 0, h = 0;
+        int kq = 0, h = 0;
+        TcWork cw = tc_work(g, 0, cta, G, nblocks, ntl, n_units);
+        int tile = cw.t0;
         // Sums over sizes: acc[e][b] (registers) collects a tile's w_b E_e
         // (packed pairs); at the tile's end the running sum H (this thread's
         // column of sSum: [bin][thread] of (E0 pair, E1 pair), 16 bytes per
@@ -1106,19 +1153,18 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             acc[0][b] = acc[1][b] = 0ull;
             sh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
         }
-        while (ok && tc_unit_index(kq, cta, G) < n_units) {
+        while (ok && cw.valid) {
             const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
+            const int ab = cw.ab;
             const bool active = TC_ABLK * ab + 32 * q < v.n_ang;   // this warp has angles in the block
-            // the next item
-            int nk = kq, nab = ab, nt = tile, nh = h + 1;
+            // the next item; wend: this item ends the work item
+            int nk = kq, nt = tile, nh = h + 1;
+            bool wend = false;
             if (nh == 2 || TC_HALF * nh >= ntile) {
                 nh = 0;
-                if (++nt == ntl) {
-                    nt = 0;
-                    if (++nab == nblocks) {
-                        nab = 0;
-                        ++nk;
-                    }
+                if (++nt == cw.t1) {
+                    wend = true;
+                    ++nk;
                 }
             }
             // the item's slot of the weight ring
@@ -1224,8 +1270,8 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     two_sum(Hb.y, acc[1][b]);
                     sh[b * TC_EPI_THREADS] = Hb;
                 }
-                if (nt == 0) {
-                    // end of the (unit, angle block): this thread's share of the unit's
+                if (wend) {
+                    // end of the work item: this thread's share of the (unit, block)'s
                     // sums.  Each sum is the unevaluated pair H + acc; the Mueller
                     // combinations are formed on the pairs in FP32 (two-sum for
                     // E0a +- E0b) and both parts go to the FP64 accumulator, scaled by
@@ -1280,8 +1326,11 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     }
                 }
             }
-            kq = nk;
-            ab = nab;
+            if (nk != kq) {
+                kq = nk;
+                cw = tc_work(g, kq, cta, G, nblocks, ntl, n_units);
+                nt = cw.t0;
+            }
             tile = nt;
             h = nh;
             ++ie;
@@ -1341,8 +1390,16 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     ctx_pre_launch(ctx);
     uint8_t *asplit = (uint8_t *)(scr + p->o_asplit);
     if (d.m_core) {
-        k_tab_coeffs_mixed_coated<<<(unsigned)ceil_div64(p->n_inst, 128), 128, 0, st>>>(
-            v, p->n_inst, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles, asplit);
+        int nb = 0, nsm = 0;
+        GBMIE_TRY(ctx_cuda(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_tab_coeffs_mixed_coated, 128, 0),
+                           "coated occupancy"));
+        GBMIE_TRY(ctx_cuda(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device), "SM count"));
+        int *next = (int *)(scr + p->o_cnext);
+        GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(next, 0, sizeof(int), st), "task counter"));
+        ctx_pre_launch(ctx);
+        k_tab_coeffs_mixed_coated<<<(nb > 0 ? nb : 1) * nsm, 128, 0, st>>>(
+            v, p->ctasks, p->n_ctasks, next, cf, eexp, eunit, ctx->d_flags, p->tile_cbase, p->unit_cbase, p->ntiles,
+            asplit);
         GBMIE_TRY(ctx_check_launch(ctx, "k_tab_coeffs_mixed_coated"));
     } else {
         GBMIE_TRY(coef_stage_attr(ctx));
@@ -1375,7 +1432,19 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     a.flags = ctx->d_flags;
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
-    const int grid = (int)(p->n_units < nsm ? p->n_units : nsm);
+    // work items: (unit, angle block) pairs, each split into tile ranges when
+    // there are fewer than four pairs per SM (tables of few wavelengths)
+    const int nblocks = p->n_pad_total / TC_ABLK;
+    const int64_t pairs = p->n_units * (int64_t)nblocks;
+    int ntr = 1;
+    if (pairs < 4 * (int64_t)nsm) {
+        const int64_t want = ceil_div64(4 * (int64_t)nsm, pairs);
+        ntr = (int)(want < p->ntiles ? want : p->ntiles);
+    }
+    a.tpr = (p->ntiles + ntr - 1) / ntr;
+    a.ntr = (p->ntiles + a.tpr - 1) / a.tpr;
+    const int64_t nwork = pairs * a.ntr;
+    const int grid = (int)(nwork < nsm ? nwork : nsm);
     cudaError_t e = cudaSuccess;
     ctx_pre_launch(ctx);
 #define TC_LAUNCH(NBV)                                                                                   \
