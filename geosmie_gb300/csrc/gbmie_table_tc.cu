@@ -270,9 +270,11 @@ struct EmitMixed {
     }
 };
 
-// Coated units of the mixed table: the FP64 coated recurrences (the
-// Toon-Ackerman ratio chain of mie_coeffs.py:183-251) with FP64 efficiency
-// sums; the coefficients leave as FP32 (c, d) like the homogeneous ones.
+// Coated units of the mixed table: the coated recurrences of
+// mie_coeffs.py:183-251 with the Toon-Ackerman ratio chain, the psi/chi rows
+// and the efficiency sums in FP64 and the three D_n recurrences in
+// double-float; the coefficients leave as FP32 (c, d) like the homogeneous
+// ones.
 struct EmitCf {
     float4 *cf;
     float amax;
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_mixed_coated(TabView v, cons
             const double x = v.xg[row];
             EmitCf emit{cf + c, 0.f};
             EffSums es;
-            coated_table_instance(v, unit, c, o, nmax, x, emit, es, flags);
+            coated_table_instance<EmitCf, true>(v, unit, c, o, nmax, x, emit, es, flags);
             double e[6];
             es.finish(x, e);
             double *o4 = v.eff4 + t * 4;

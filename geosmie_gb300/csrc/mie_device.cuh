@@ -1,6 +1,7 @@
 // Per-instance Mie device functions (FP64): Riccati-Bessel rows, homogeneous
 // and coated coefficients with fused efficiency sums.
 #pragma once
+#include "df.cuh"
 #include "common.cuh"
 
 // ---------------------------------------------------------------------------
@@ -293,7 +294,15 @@ __device__ __forceinline__ void homog_instance(double x, cplx eps, cplx mu, cons
 // Coefficients are emitted n = 1..nmax (ascending).  rowy1: psi/chi of y for
 // orders 1..nmax at rowy1[n-1]; it may alias the emitter's a_n output.
 // ---------------------------------------------------------------------------
-template <class Emit>
+//
+// DFD (the mixed table path): the three downward D_n recurrences in
+// double-float pairs (df.cuh, about 2^-46) instead of FP64, from the same
+// start; the values are widened to FP64 for the ratio chain, which stays in
+// FP64 with everything after it.  On GB300 the FP64 pipe issues a small
+// fraction of the FP32 rate, and these recurrences (three arguments, up to
+// max(|m1 y|, |m2 y|) + 16 steps each) were about half of the FP64 work of a
+// coated instance.
+template <class Emit, bool DFD = false>
 __device__ __forceinline__ void coated_instance(double x, double y, cplx eps1, cplx eps2,
                                                 const double2 *rowy1, int nmax,
                                                 double2 *__restrict__ dscr, Emit &emit, EffSums &es)
@@ -306,17 +315,39 @@ __device__ __forceinline__ void coated_instance(double x, double y, cplx eps1, c
     const double mx = fmax(cabs(m1 * y), cabs(w));
     const int nmx = (int)rint(fmax((double)nmax, mx) + 16.0);
     const cplx uinv = cinv(u), vinv = cinv(v), winv = cinv(w);
-    cplx Du = cx(0, 0), Dv = cx(0, 0), Dw = cx(0, 0);
-    for (int k = nmx - 1; k >= 1; --k) {
-        const double kp = (double)(k + 1);
-        const cplx ru = uinv * kp, rv = vinv * kp, rw = winv * kp;
-        Du = ru - cinv(Du + ru);
-        Dv = rv - cinv(Dv + rv);
-        Dw = rw - cinv(Dw + rw);
-        if (k <= nmax) {
-            dscr[5 * (k - 1) + 0] = d2(Du);
-            dscr[5 * (k - 1) + 1] = d2(Dv);
-            dscr[5 * (k - 1) + 2] = d2(Dw);
+    if (DFD) {
+        const cdf zi[3] = {cdf{df_from_f64(uinv.re), df_from_f64(uinv.im)},
+                           cdf{df_from_f64(vinv.re), df_from_f64(vinv.im)},
+                           cdf{df_from_f64(winv.re), df_from_f64(winv.im)}};
+        cdf D[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) D[j] = cdf{df{0.f, 0.f}, df{0.f, 0.f}};
+        for (int k = nmx - 1; k >= 1; --k) {
+            const float kp = (float)(k + 1);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const cdf r = cdf_mul_f(zi[j], kp);   // (k+1)/z
+                const cdf wv = cdf_add(D[j], r);
+                const df iw = df_rcp(df_fma(wv.re, wv.re, df_mul(wv.im, wv.im)));
+                D[j] = cdf{df_fma(df_neg(wv.re), iw, r.re), df_fma(wv.im, iw, r.im)};   // r - 1/w
+                if (k <= nmax)
+                    dscr[5 * (k - 1) + j] = make_double2((double)D[j].re.hi + (double)D[j].re.lo,
+                                                         (double)D[j].im.hi + (double)D[j].im.lo);
+            }
+        }
+    } else {
+        cplx Du = cx(0, 0), Dv = cx(0, 0), Dw = cx(0, 0);
+        for (int k = nmx - 1; k >= 1; --k) {
+            const double kp = (double)(k + 1);
+            const cplx ru = uinv * kp, rv = vinv * kp, rw = winv * kp;
+            Du = ru - cinv(Du + ru);
+            Dv = rv - cinv(Dv + rv);
+            Dw = rw - cinv(Dw + rw);
+            if (k <= nmax) {
+                dscr[5 * (k - 1) + 0] = d2(Du);
+                dscr[5 * (k - 1) + 1] = d2(Dv);
+                dscr[5 * (k - 1) + 2] = d2(Dw);
+            }
         }
     }
     psi_row_complex(v, nmax, dscr + 3, 5);

@@ -157,8 +157,9 @@ struct TabView {
 
 // Coated units (pymiecoated Mie(m=core, m2=shell, x=core, y=outer)): the
 // reference's dispatch (mie_coeffs.py:62-71) and the FP64 coated recurrences
-// (:183-251), one thread per instance; the grid is the outer size.
-template <class Emit>
+// (:183-251), one thread per instance; the grid is the outer size.  DFD:
+// the D_n recurrences in double-float (coated_instance; the mixed path).
+template <class Emit, bool DFD = false>
 __device__ __forceinline__ void coated_table_instance(const TabView &v, int64_t unit, int64_t c, int64_t o, int nmax,
                                                       double x, Emit &emit, EffSums &es, int *flags)
 {
@@ -170,7 +171,7 @@ __device__ __forceinline__ void coated_table_instance(const TabView &v, int64_t 
     const double xc = ratio * x;
     if (xc == x || (e1.re == e2.re && e1.im == e2.im)) homog_instance(x, e1, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
     else if (xc == 0.0) homog_instance(x, e2, cx(1.0, 0.0), v.pc + o, nmax, emit, es);
-    else coated_instance(xc, x, e1, e2, v.pc + o, nmax, v.dscr + 5 * c, emit, es);
+    else coated_instance<Emit, DFD>(xc, x, e1, e2, v.pc + o, nmax, v.dscr + 5 * c, emit, es);
 }
 
 // Mixed path (gbmie_table_tc.cu): the contraction's B operand tables, built
