@@ -54,16 +54,28 @@ __device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1, f
     const double psi1 = s * xinv - c;
     const double scale = (pn * s + pn1 * psi1) / (pn * pn + pn1 * pn1);
     double chi = c, chim1 = -s;
-    for (int n = 1; n <= nmax; ++n) {
-        const double chin = (double)(2 * n - 1) * xinv * chi - chim1;
-        chim1 = chi;
-        chi = chin;
-        const double psi = scale * row1[n - 1].x;
-        row1[n - 1] = make_double2(psi, chi);
-        if (pair) {
-            const float ph = __double2float_rn(psi), ch = __double2float_rn(chi);
-            pair[(size_t)(n - 1) * pstride] = make_float4(ph, __double2float_rn(psi - (double)ph), ch,
-                                                          __double2float_rn(chi - (double)ch));
+    // the unnormalised psi values are read back in groups of 8 independent
+    // loads ahead of their use: read one at a time, each order waited for a
+    // round trip to L2 (the row was just written), and rows of a few hundred
+    // orders took that many round trips in sequence
+    for (int n0 = 1; n0 <= nmax; n0 += 8) {
+        double pr[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) pr[j] = row1[min(n0 + j, nmax) - 1].x;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = n0 + j;
+            if (n > nmax) continue;
+            const double chin = (double)(2 * n - 1) * xinv * chi - chim1;
+            chim1 = chi;
+            chi = chin;
+            const double psi = scale * pr[j];
+            row1[n - 1] = make_double2(psi, chi);
+            if (pair) {
+                const float ph = __double2float_rn(psi), ch = __double2float_rn(chi);
+                pair[(size_t)(n - 1) * pstride] = make_float4(ph, __double2float_rn(psi - (double)ph), ch,
+                                                              __double2float_rn(chi - (double)ch));
+            }
         }
     }
 }
@@ -92,9 +104,14 @@ __device__ __forceinline__ void psi_row_complex(cplx z, int nmax, double2 *out, 
     const cplx s = csin(z), c = ccos(z);
     const cplx psi1 = s * zinv - c;
     const cplx scale = (conjg(pn) * s + conjg(pn1) * psi1) * (1.0 / (abs2(pn) + abs2(pn1)));
-    for (int n = 1; n <= nmax; ++n) {
-        double2 &o = out[(size_t)(n - 1) * stride];
-        o = d2(scale * cx(o));
+    // read back in groups of 8 independent loads (see psi_chi_row)
+    for (int n0 = 1; n0 <= nmax; n0 += 8) {
+        double2 pr[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) pr[j] = out[(size_t)(min(n0 + j, nmax) - 1) * stride];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (n0 + j <= nmax) out[(size_t)(n0 + j - 1) * stride] = d2(scale * cx(pr[j]));
     }
 }
 
