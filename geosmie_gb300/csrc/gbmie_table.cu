@@ -44,9 +44,11 @@ __global__ void k_tab_make_x(int n_le, int n_size, int grid_kind, const double *
 // ---------------------------------------------------------------------------
 // run kernels
 // ---------------------------------------------------------------------------
-// psi/chi rows per (wavelength block, size) in FP64 (CSR, pc) and, for
-// homogeneous mixed plans (pairs = 1), also as FP32 pairs in the order-major
-// groups of 32 sizes the mixed recurrences read (TabView::pcd).
+// psi/chi rows per (wavelength block, size) in FP64 (CSR, pc) or, for
+// homogeneous mixed plans (pairs = 1), as FP32 pairs only, in the order-major
+// groups of 32 sizes the mixed recurrences read (TabView::pcd; the pair
+// slots also hold the unnormalised psi values meanwhile, so that a warp's
+// stores and loads of an order are one segment).
 __global__ void __launch_bounds__(128) k_tab_psi_chi(int64_t nrows, const double *__restrict__ xg,
                                                      const int64_t *__restrict__ off, double2 *__restrict__ pc,
                                                      double4 *__restrict__ rowc, TabView v, int pairs)
@@ -60,7 +62,7 @@ __global__ void __launch_bounds__(128) k_tab_psi_chi(int64_t nrows, const double
         const int le = (int)(j / v.n_size), i = (int)(j - (int64_t)le * v.n_size);
         pr = v.pcd + v.grow[le] + v.grel[(int64_t)le * (v.ngrp + 1) + (i >> 5)] + (i & 31);
     }
-    psi_chi_row(x, (int)(off[j + 1] - o), pc + o, pr, 32);
+    psi_chi_row(x, (int)(off[j + 1] - o), pairs ? nullptr : pc + o, pr, 32);
     double s, c;
     sincos(x, &s, &c);
     rowc[j] = make_double4(s, c, 1.0 / x, 0.0);

@@ -32,21 +32,27 @@ __device__ __forceinline__ int miller_start(double az, int nmax)
 // the dominant solution).  row1 may alias the coefficient output (the
 // homogeneous kernels overwrite it in place).
 // pair (or NULL): the same rows also as FP32 pairs (psi hi, lo, chi hi, lo)
-// at pair[(n - 1) * pstride], for the mixed recurrences.
+// at pair[(n - 1) * pstride], for the mixed recurrences.  row1 == NULL (with
+// pair): no FP64 rows; the unnormalised psi values are parked in the first
+// 8 bytes of each pair slot instead.
 __device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1, float4 *pair = nullptr, int pstride = 1)
 {
     const int N = miller_start(x, nmax);
     const double xinv = 1.0 / x;
+    // the unnormalised psi of order k (1..nmax)
+    auto park = [&](int k) -> double & {
+        return row1 ? row1[k - 1].x : *(double *)(pair + (size_t)(k - 1) * pstride);
+    };
     double pn1 = 0.0, pn = 1.0;   // psi^_{n+1}, psi^_n
     for (int n = N; n >= 1; --n) {
         const double pm = (double)(2 * n + 1) * xinv * pn - pn1;
         pn1 = pn;
         pn = pm;
-        if (n - 1 >= 1 && n - 1 <= nmax) row1[n - 2].x = pm;
+        if (n - 1 >= 1 && n - 1 <= nmax) park(n - 1) = pm;
         if (fabs(pm) > 1e100) {
             pn *= 1e-100;
             pn1 *= 1e-100;
-            for (int k = (n - 1 >= 1 ? n - 1 : 1); k <= nmax; ++k) row1[k - 1].x *= 1e-100;
+            for (int k = (n - 1 >= 1 ? n - 1 : 1); k <= nmax; ++k) park(k) *= 1e-100;
         }
     }
     double s, c;
@@ -61,7 +67,7 @@ __device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1, f
     for (int n0 = 1; n0 <= nmax; n0 += 8) {
         double pr[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) pr[j] = row1[min(n0 + j, nmax) - 1].x;
+        for (int j = 0; j < 8; ++j) pr[j] = park(min(n0 + j, nmax));
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int n = n0 + j;
@@ -70,7 +76,7 @@ __device__ __forceinline__ void psi_chi_row(double x, int nmax, double2 *row1, f
             chim1 = chi;
             chi = chin;
             const double psi = scale * pr[j];
-            row1[n - 1] = make_double2(psi, chi);
+            if (row1) row1[n - 1] = make_double2(psi, chi);
             if (pair) {
                 const float ph = __double2float_rn(psi), ch = __double2float_rn(chi);
                 pair[(size_t)(n - 1) * pstride] = make_float4(ph, __double2float_rn(psi - (double)ph), ch,
