@@ -47,12 +47,13 @@ SAMPLE_RH = [0, 35]
 # one unit per host core, rotating through the list
 REF_LAMBDA = [0, 8, 17, 25, 34, 42, 51, 59]
 REF_RH = [0, 7, 14, 21, 28, 35]
-# DRAM bytes (read + write) per (wavelength, RH, component) unit from one ncu
-# capture of the 12-wavelength sulfate table (432 units; profiles/
-# k_tab_s12_tc_k_tab_coeffs_mixed_sulfate12.md: dram__bytes.sum.per_second x
-# duration), scaled to a run by its units (sulfate table only)
-NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": 904.567513e9 * 527.776e-6 / 432,
-                      "k_tab_s12_tc": 789.561399e9 * 693.696e-6 / 432}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per (wavelength,
+# RH, component) unit from one ncu capture of each kernel on the 12-wavelength
+# sulfate table (432 units; profiles/k_tab_s12_tc_sulfate12.md,
+# profiles/k_tab_coeffs_mixed_sulfate12.md), scaled to a run by its units
+# (sulfate table only)
+NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": (34.291456e6 + 359.66592e6) / 432,
+                      "k_tab_s12_tc": (335.490048e6 + 10.14016e6) / 432}
 SCAT = ["p11", "p12", "p22", "p33", "p34", "p44"]
 SCALARS = ["qext", "qsca", "qb", "g", "csca", "cext", "ssa", "bsca", "bext", "bbck", "refreal", "refimag",
            "lidar_ratio"]
