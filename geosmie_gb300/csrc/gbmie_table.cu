@@ -218,7 +218,8 @@ __global__ void __launch_bounds__(128) k_tab_coeffs_coated(TabView v, int64_t n_
 // streamed through shared memory as (a+b, a-b).
 #define TAB_CAP 2048
 template <int NB>
-__global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int nchunk, const int2 *__restrict__ brange)
+__global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int nchunk, const int2 *__restrict__ brange,
+                                                       int slot0)
 {
     __shared__ double2 cd[TAB_CAP][2];
     const int64_t unit = blockIdx.x / nchunk;
@@ -229,13 +230,18 @@ __global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int
     const int le = v.le(lam);
     const int2 rg = brange[le];           // this launch's nmax bucket on this x grid
     const int i0 = rg.x + ch * chunk, i1 = min(rg.y, i0 + chunk);
-    if (i0 >= i1) return;
+    const int nang = v.n_ang;
+    // this block's partial-sum plane: slot slot0 + ch of the unit
+    double *part = v.part + ((size_t)unit * v.n_slots + slot0 + ch) * v.n_bin * 4 * nang;
+    if (i0 >= i1) {   // no sizes of this unit in the chunk: its plane is zero
+        for (int e = threadIdx.x; e < v.n_bin * 4 * nang; e += blockDim.x) part[e] = 0.0;
+        return;
+    }
     const int64_t *off = v.off + (int64_t)le * v.n_size;   // off[i] for this x grid
     const int64_t cbase = v.unit_base[unit] - off[0];
     const double2 *A = v.an + cbase, *B = v.bn + cbase;
     const int64_t wstride = v.n_size;
     const double *Wb = v.W + v.wlam(lam) + ((size_t)(lr % v.n_rh) * v.n_bin * v.n_comp + comp) * wstride;
-    const int nang = v.n_ang;
     for (int a0 = 0; a0 < nang; a0 += blockDim.x) {
         const int a = a0 + threadIdx.x;
         const bool act = a < nang;
@@ -302,11 +308,11 @@ __global__ void __launch_bounds__(256) k_tab_s12_plain(TabView v, int chunk, int
             for (int b = 0; b < NB; ++b) {
                 if (b < v.n_bin) {
                     const double f = v.frac[(size_t)b * v.n_comp + comp];
-                    double *dst = v.pacc + (((size_t)lr * v.n_bin + b) * 4) * nang + a;
-                    atomicAdd(dst, f * acc[b][0]);
-                    atomicAdd(dst + nang, f * acc[b][1]);
-                    atomicAdd(dst + 2 * nang, f * acc[b][2]);
-                    atomicAdd(dst + 3 * nang, f * acc[b][3]);
+                    double *dst = part + (size_t)b * 4 * nang + a;
+                    dst[0] = f * acc[b][0];
+                    dst[nang] = f * acc[b][1];
+                    dst[2 * nang] = f * acc[b][2];
+                    dst[3 * nang] = f * acc[b][3];
                 }
             }
         }
@@ -457,17 +463,34 @@ __global__ void k_tab_trapz(int nang, const double *__restrict__ theta, double *
 }
 
 // Phase normalisation and the per-entry outputs (dointegration.py:950-1001).
-__global__ void __launch_bounds__(256) k_tab_finalize(TabView v, gbmie_table_out out)
+// The entry's Mueller sums are first formed from the angular kernels'
+// partial sums: over components c, then slots s < used, in that order (a
+// fixed order, so that repeated runs give the same bits), into pacc.
+__global__ void __launch_bounds__(64) k_tab_finalize(TabView v, gbmie_table_out out, int used)
 {
     const int blk = blockIdx.x;   // (lam * n_rh + rh) * n_bin + bin
     const int bin = blk % v.n_bin;
     const int64_t lr = blk / v.n_bin;
     const int rh = (int)(lr % v.n_rh), lam = (int)(lr / v.n_rh);
     const int nang = v.n_ang;
-    const double *P = v.pacc + (size_t)blk * 4 * nang;
+    double *P = v.pacc + (size_t)blk * 4 * nang;
+    const size_t plane = (size_t)v.n_bin * 4 * nang;
+    const double *src = v.part + (size_t)lr * v.n_comp * v.n_slots * plane + (size_t)bin * 4 * nang;
     // trapz(p11 sin(theta), theta) with the precomputed weights
     double tr[1] = {0.0};
-    for (int a = threadIdx.x; a < nang; a += blockDim.x) tr[0] += P[a] * v.tw[a];
+    const int nsrc = v.n_comp * v.n_slots;
+    for (int a = threadIdx.x; a < nang; a += blockDim.x) {
+        for (int k = 0; k < 4; ++k) {
+            const double *q = src + k * nang + a;
+            double sum = 0.0;
+#pragma unroll 1
+            for (int c = 0; c < nsrc; c += v.n_slots)
+#pragma unroll 1
+                for (int sl = 0; sl < used; ++sl) sum += q[(size_t)(c + sl) * plane];
+            P[k * nang + a] = sum;   // read back below by this thread only
+        }
+        tr[0] += P[a] * v.tw[a];
+    }
     block_sum<1>(tr);
     const double scale = 2.0 / tr[0];   // p11n / p11, the same at every angle
     const size_t e = ((size_t)bin * v.n_lambda + lam) * v.n_rh + rh;   // output entry
@@ -575,6 +598,8 @@ static TabView make_view(const gbmie_table_plan *p, char *scr)
     v.sums = (double *)(scr + p->o_sums);
     v.reff0 = (double *)(scr + p->o_reff0);
     v.pacc = (double *)(scr + p->o_pacc);
+    v.part = (double *)(scr + p->o_part);
+    v.n_slots = p->n_slots;
     v.pq = (const double2 *)(scr + p->o_pq);
     v.sraw = (double *)(scr + p->o_sraw);
     v.nlraw = (double *)(scr + p->o_nlraw);
@@ -1036,6 +1061,33 @@ extern "C" int gbmie_table_plan_create(gbmie_ctx *ctx, const gbmie_table_desc *d
         p->o_sums = carve(sizeof(double) * nW * 4);
         p->o_reff0 = carve(sizeof(double) * (size_t)d.n_lambda * d.n_bin * d.n_comp);
         p->o_pacc = carve(sizeof(double) * (size_t)p->n_entries * 4 * d.n_ang);
+        // partial-sum slots per unit: mixed, two size halves per tile range;
+        // plain, the chunks of the finest chunking the autotuner tries (64
+        // sizes) over the nmax buckets or the whole grid, whichever is more
+        if (mixed) {
+            int nsm = 0;
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+            if (nsm < 1) nsm = 1;
+            // work items of the contraction: (unit, angle block) pairs, each
+            // split into tile ranges when there are fewer than four pairs per SM
+            const int64_t pairs = p->n_units * (int64_t)(p->n_pad_total / 128);
+            int ntr = 1;
+            if (pairs < 4 * (int64_t)nsm) {
+                const int64_t want = ceil_div64(4 * (int64_t)nsm, pairs);
+                ntr = (int)(want < p->ntiles ? want : p->ntiles);
+            }
+            p->tc_tpr = (p->ntiles + ntr - 1) / ntr;
+            p->tc_ntr = (p->ntiles + p->tc_tpr - 1) / p->tc_tpr;
+            p->n_slots = 2 * p->tc_ntr;
+            p->slots_used = p->n_slots;
+        } else {
+            int split = 0;
+            for (int b = 0; b < GBMIE_TUNE_BUCKETS; ++b) split += (p->bmaxlen[b] + 63) / 64;
+            const int whole = (p->bmaxlen[GBMIE_TUNE_BUCKETS] + 63) / 64;
+            p->n_slots = split > whole ? split : whole;
+            p->slots_used = 0;
+        }
+        p->o_part = carve(sizeof(double) * (size_t)p->n_units * p->n_slots * d.n_bin * 4 * d.n_ang);
         p->o_pq = carve(mixed ? 16 : sizeof(double2) * (size_t)p->nmax_max * d.n_ang);
         p->o_cf = carve(mixed ? sizeof(float4) * (size_t)(p->ab_total > p->cfg_total ? p->ab_total : p->cfg_total) : 16);
         p->o_eexp = carve(mixed ? sizeof(int) * (size_t)p->n_inst : 16);
@@ -1100,7 +1152,7 @@ static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, co
     k_tab_trapz<<<1, 256, 0, st>>>(d.n_ang, d.theta, v.tw);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_trapz"));
     ctx_pre_launch(ctx);
-    k_tab_finalize<<<(unsigned)p->n_entries, 64, 0, st>>>(v, *out);   // 2-3 angles per thread
+    k_tab_finalize<<<(unsigned)p->n_entries, 64, 0, st>>>(v, *out, p->slots_used);   // 2-3 angles per thread
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
     if (p->has_gsf) {
         GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
@@ -1115,18 +1167,22 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
 // The plain angular kernel over one nmax bucket (sizes of every unit whose
 // nmax falls in it; bucket GBMIE_TUNE_BUCKETS = the whole grid), `chunk`
 // sizes per block, `threads` angles per pass.
-static int launch_s12_plain(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, int b, int chunk, int threads)
+static int launch_s12_plain(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, int b, int chunk, int threads,
+                            int slot0 = 0)
 {
     if (p->bmaxlen[b] == 0) return GBMIE_OK;
     const int nchunk = (p->bmaxlen[b] + chunk - 1) / chunk;
+    if (slot0 + nchunk > p->n_slots)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "k_tab_s12_plain: %d partial-sum slots needed, %d held",
+                        slot0 + nchunk, p->n_slots);
     const unsigned grid = (unsigned)(p->n_units * nchunk);
     const int2 *br = p->brange + (size_t)b * p->n_le;
     cudaStream_t st = ctx->stream;
     ctx_pre_launch(ctx);
-    if (p->d.n_bin <= 1) k_tab_s12_plain<1><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
-    else if (p->d.n_bin <= 2) k_tab_s12_plain<2><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
-    else if (p->d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
-    else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk, br);
+    if (p->d.n_bin <= 1) k_tab_s12_plain<1><<<grid, threads, 0, st>>>(v, chunk, nchunk, br, slot0);
+    else if (p->d.n_bin <= 2) k_tab_s12_plain<2><<<grid, threads, 0, st>>>(v, chunk, nchunk, br, slot0);
+    else if (p->d.n_bin <= 4) k_tab_s12_plain<4><<<grid, threads, 0, st>>>(v, chunk, nchunk, br, slot0);
+    else k_tab_s12_plain<8><<<grid, threads, 0, st>>>(v, chunk, nchunk, br, slot0);
     return ctx_check_launch(ctx, "k_tab_s12_plain");
 }
 
@@ -1164,8 +1220,6 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     GBMIE_TRY(ctx_cuda(ctx, cudaEventRecord(ctx->ev_join, ctx->side), "join"));
     ctx_pre_launch(ctx);
     if (d.precision == GBMIE_MIXED) {
-        GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
-                           "pacc clear"));
         GBMIE_TRY(launch_table_mixed(ctx, p, v, scr));
         return launch_table_tail(ctx, p, v, out);
     }
@@ -1178,15 +1232,19 @@ extern "C" int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *p, const gbmie_
     }
     GBMIE_TRY(ctx_cuda(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0), "join"));   // the PSD weights
     GBMIE_TRY(launch_pq_table(ctx, d.n_ang, d.cos_theta, p->nmax_max, (double2 *)(scr + p->o_pq)));
-    GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(v.pacc, 0, sizeof(double) * p->n_entries * 4 * d.n_ang, st),
-                       "pacc clear"));
+    // the buckets' chunks take consecutive partial-sum slots
+    int slot = 0;
     if (p->plain_split) {
-        for (int b = 0; b < GBMIE_TUNE_BUCKETS; ++b)
-            GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b]));
+        for (int b = 0; b < GBMIE_TUNE_BUCKETS; ++b) {
+            GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b], slot));
+            if (p->bmaxlen[b] > 0) slot += (p->bmaxlen[b] + p->plain_chunk[b] - 1) / p->plain_chunk[b];
+        }
     } else {
         const int b = GBMIE_TUNE_BUCKETS;
-        GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b]));
+        GBMIE_TRY(launch_s12_plain(ctx, p, v, b, p->plain_chunk[b], p->plain_threads[b], 0));
+        slot = (p->bmaxlen[b] + p->plain_chunk[b] - 1) / p->plain_chunk[b];
     }
+    p->slots_used = slot;
     return launch_table_tail(ctx, p, v, out);
 }
 

@@ -1276,10 +1276,13 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     // end of the work item: this thread's share of the (unit, block)'s
                     // sums.  Each sum is the unevaluated pair H + acc; the Mueller
                     // combinations are formed on the pairs in FP32 (two-sum for
-                    // E0a +- E0b) and both parts go to the FP64 accumulator, scaled by
-                    // 2^(2 (E - 13)) exactly in the integer domain.
+                    // E0a +- E0b), both parts are scaled by 2^(2 (E - 13)) exactly
+                    // in the integer domain and their FP64 sum is stored in the
+                    // partial-sum slot of (tile range, size half) of the unit.
                     const int ang = TC_ABLK * ab + 32 * q + lane;
                     if (ang < v.n_ang) {
+                        double *part = v.part + ((size_t)cw.unit * v.n_slots + 2 * (cw.t0 / g.tpr) + wh) *
+                                                    v.n_bin * 4 * v.n_ang;
                         const int k2 = 2 * (hdr.y - SHIFT_BITS);
 #pragma unroll
                         for (int b = 0; b < NB; ++b) {
@@ -1314,9 +1317,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                         a *= fr;
                                         c *= fr;
                                     }
-                                    double *dst = v.pacc + (((size_t)hdr.z * v.n_bin + b) * 4 + k) * v.n_ang + ang;
-                                    atomicAdd(dst, a);
-                                    atomicAdd(dst, c);
+                                    part[((size_t)b * 4 + k) * v.n_ang + ang] = a + c;
                                 }
                             }
                         }
@@ -1435,16 +1436,16 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
     // work items: (unit, angle block) pairs, each split into tile ranges when
-    // there are fewer than four pairs per SM (tables of few wavelengths)
+    // there are fewer than four pairs per SM (tables of few wavelengths); the
+    // plan fixed the split with its partial-sum slots (two per range)
     const int nblocks = p->n_pad_total / TC_ABLK;
     const int64_t pairs = p->n_units * (int64_t)nblocks;
-    int ntr = 1;
-    if (pairs < 4 * (int64_t)nsm) {
-        const int64_t want = ceil_div64(4 * (int64_t)nsm, pairs);
-        ntr = (int)(want < p->ntiles ? want : p->ntiles);
-    }
-    a.tpr = (p->ntiles + ntr - 1) / ntr;
-    a.ntr = (p->ntiles + a.tpr - 1) / a.tpr;
+    a.tpr = p->tc_tpr;
+    a.ntr = p->tc_ntr;
+    if (2 * a.ntr > p->n_slots)
+        return ctx_fail(ctx, GBMIE_ERR_INVALID, "k_tab_s12_tc: %d partial-sum slots needed, %d held", 2 * a.ntr,
+                        p->n_slots);
+    p->slots_used = 2 * a.ntr;
     const int64_t nwork = pairs * a.ntr;
     const int grid = (int)(nwork < nsm ? nwork : nsm);
     cudaError_t e = cudaSuccess;

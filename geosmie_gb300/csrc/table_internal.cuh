@@ -23,6 +23,15 @@ struct gbmie_table_plan {
     int64_t pc_total, ab_total;
     int nmax_max;
     size_t o_pc, o_an, o_bn, o_eff, o_w, o_sums, o_reff0, o_pacc, o_pq, o_sraw, o_nlraw, bytes;
+    // Partial Mueller sums of the angular kernels, one plane [bin][4][ang]
+    // per (unit, slot): a slot is a block's share of a unit's sizes (plain:
+    // a size chunk of an nmax bucket; mixed: a tile range and a size half),
+    // written with plain stores and summed in a fixed order into pacc, so
+    // that a table's bits do not depend on the order in which blocks finish
+    size_t o_part;
+    int n_slots;     // slots per unit the buffer holds
+    int slots_used;  // slots per unit the last launch layout wrote
+    int tc_ntr, tc_tpr;   // mixed: tile ranges per (unit, angle block), tiles per range
     // mixed precision (tensor-core) path
     size_t o_cf, o_eexp, o_eunit, o_wf, o_tw, o_rowc, o_hidx, o_pcf, o_dscr, o_hdf, o_rowcd;
     __half *bt;          // angle-function operand of the contraction (built once per key, see ctx angle_ops)
@@ -122,6 +131,8 @@ struct TabView {
     const int64_t *off, *unit_base;
     double2 *pc, *an, *bn;
     double *eff4, *W, *sums, *reff0, *pacc, *sraw, *nlraw;
+    double *part;   // [n_units][n_slots][bin][4][ang] partial Mueller sums
+    int n_slots;
     float *Wf;   // FP32 copy of W (mixed path), or NULL
     double *tw;  // trapz weights of the angle grid [n_ang]
     double4 *rowc;      // per size row: sin x, cos x, 1/x

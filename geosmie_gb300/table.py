@@ -57,6 +57,33 @@ def angmie():
                            np.linspace(10.0, 180.0, 171, endpoint=True)])
 
 
+def check_spec(spec):
+    """Raise ValueError unless every array of a TablePlan spec has the size
+    its dimensions (nl, nrh, ncomp from m; nbin from frac; ns from grid) ask
+    for: the C plan takes plain pointers and cannot check them."""
+    m = np.asarray(spec["m"])
+    if m.ndim != 3:
+        raise ValueError("spec['m']: [nl, nrh, ncomp] expected, got shape %s" % (m.shape,))
+    nl, nrh, ncomp = m.shape
+    frac = np.asarray(spec["frac"])
+    if frac.ndim != 2 or frac.shape[1] != ncomp:
+        raise ValueError("spec['frac']: [nbin, %d] expected, got shape %s" % (ncomp, frac.shape))
+    nbin = frac.shape[0]
+    ns = np.asarray(spec["grid"]).size
+    need = [("lambda", (nl,)), ("dgrid", (ns,)), ("rhop", (nbin, nrh)), ("rhop0", (nbin,)), ("gf", (nrh,)),
+            ("rlow", (nbin,)), ("rup", (nbin,))]
+    if int(spec["psd_kind"]) == PSD_WEIGHTS:
+        need.append(("weights", (nl, nrh, nbin, ncomp, ns)))
+    else:
+        need += [("psd_param", (nbin, ncomp, 4)), ("gf_psd", (nrh,))]
+    if spec.get("m_core") is not None:
+        need += [("m_core", (nl, nrh, ncomp)), ("core_ratio", (nrh,))]
+    for k, shape in need:
+        n = np.asarray(spec[k]).size
+        if n != int(np.prod(shape)):
+            raise ValueError("spec[%r]: %d values, %s = %d expected" % (k, n, list(shape), int(np.prod(shape))))
+
+
 class TablePlan(object):
     """One planned table on the GPU (a C ``gbmie_table_plan``).
 
@@ -78,6 +105,7 @@ class TablePlan(object):
         """setup_stream: a torch CUDA stream for the plan's own setup (input
         copy, layout kernels, operand tables), so that creating a plan does not
         wait for tables in flight on the caller's stream (run_tables)."""
+        check_spec(spec)
         self.ctx = _native.context(device)
         dv = self.ctx.device
         self._run_stream = None

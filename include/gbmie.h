@@ -265,8 +265,9 @@ int gbmie_table_run(gbmie_ctx *ctx, gbmie_table_plan *plan, const gbmie_table_ou
  * output pointers differ from the captured ones, or after the context's
  * scratch block was reallocated by a larger plan) captures gbmie_table_run
  * on a private stream and instantiates it; every call then launches the
- * graph on the context stream.  Results equal gbmie_table_run's up to the
- * order of the FP64 atomic additions of the angular sums.  With timing
+ * graph on the context stream.  Results equal gbmie_table_run's bit for
+ * bit (the angular kernels' partial sums are added in a fixed order, so a
+ * table's bits do not depend on block timing).  With timing
  * enabled the whole graph is timed as one record, "gbmie_table_graph".  No
  * counterpart in the reference (its table loop is Python,
  * geosmie/dointegration.py:786-1031). */
