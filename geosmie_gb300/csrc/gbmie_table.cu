@@ -485,8 +485,8 @@ __global__ void __launch_bounds__(64) k_tab_finalize(TabView v, gbmie_table_out 
             double sum = 0.0;
 #pragma unroll 1
             for (int c = 0; c < nsrc; c += v.n_slots)
-#pragma unroll 1
-                for (int sl = 0; sl < used; ++sl) sum += q[(size_t)(c + sl) * plane];
+#pragma unroll 8
+                for (int sl = 0; sl < used; ++sl) sum += q[(size_t)(c + sl) * plane];   // loads issued ahead, adds in order
             P[k * nang + a] = sum;   // read back below by this thread only
         }
         tr[0] += P[a] * v.tw[a];

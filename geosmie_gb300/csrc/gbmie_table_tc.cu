@@ -611,7 +611,7 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 // of MMAs into one accumulator therefore loses a fraction of an ulp per
 // product, always in the same direction: at forward angles, where all terms
 // of S+ add coherently, x = 628 gave 1.4e-6 of P11.  Here every tile's
-// orders are split into windows of g.win (<= TC_NS) 16-order chunks; each window
+// orders are split into windows of g.win (<= TC_WIN_MAX) 16-order chunks; each window
 // starts a fresh accumulator, adds the two cross products of its orders
 // (P_hi C_lo, P_lo C_hi, 2^-11 of the result) while the accumulator is small
 // and then the P_hi C_hi products, and the epilogue adds the windows in FP32
@@ -660,17 +660,25 @@ struct TcArgs {
     const int *tile_cbase;       // [n_le][ntiles + 1]
     const int64_t *unit_cbase;   // [n_units]
     int ntiles;
-    int win;                     // accumulation window (16-order chunks, <= TC_NS)
+    int win;                     // accumulation window (16-order chunks, <= TC_WIN_MAX)
     uint32_t wait_limit;         // tries of every pipeline wait (gbmie_table_plan_set_wait_limit)
     int ntr, tpr;                // tile ranges per (unit, angle block) and tiles per range
     int *flags;
 };
 
-#define TC_NS 4                                        // ring stages
-#define TC_WIN_MAX TC_NS                               // longest accumulation window (chunks)
+// ring stages: the copies of a stage's next chunk wait for its MMAs, so the
+// ring's depth bounds the chunks in flight (sulfate-like table: 4 stages
+// 3.15 ms, 5 stages 3.04, 6 stages 3.03)
+#define TC_NS 6
+// longest accumulation window (chunks): the windows the accuracy of the FP32
+// accumulation was checked with (2-4 keep it near 2e-7); a window's chunks
+// sit in the ring together
+#define TC_WIN_MAX 4
+static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
 #define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
-// resident angle-function chunks (angle blocks)
-#define TC_B0_SLOTS(NB) 4
+// resident angle-function chunks (angle blocks; tables of more than 256
+// angles reload one slot per (unit, block))
+#define TC_B0_SLOTS(NB) 2
 #define TC_A_BYTES (4 * TC_MAT_A)                      // P_hi P_lo Q_hi Q_lo of a chunk: 16 KB
 #define TC_B_BYTES (4 * TC_MAT_B)                      // C_hi C_lo D_hi D_lo of a half chunk: 8 KB
 #define TC_STAGE_BYTES (TC_B_BYTES + TC_A_BYTES)       // 24 KB
