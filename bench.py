@@ -53,7 +53,7 @@ REF_RH = [0, 7, 14, 21, 28, 35]
 # profiles/k_tab_coeffs_mixed_sulfate12.md), scaled to a run by its units
 # (sulfate table only)
 NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": (34.291456e6 + 359.66592e6) / 432,
-                      "k_tab_s12_tc": (335.490048e6 + 10.14016e6) / 432}
+                      "k_tab_s12_tc": (323.454976e6 + 16.767744e6) / 432}
 SCAT = ["p11", "p12", "p22", "p33", "p34", "p44"]
 SCALARS = ["qext", "qsca", "qb", "g", "csca", "cext", "ssa", "bsca", "bext", "bbck", "refreal", "refimag",
            "lidar_ratio"]
