@@ -130,12 +130,18 @@ __global__ void __launch_bounds__(128) k_gsf_tc_rows(int ntab, int ng, int nkc, 
     int em[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) em[c] = -1100;
+    // with at most one node per thread its values are kept for the digit
+    // pass below (the same thread takes the same node there)
+    const bool keep = ng <= (int)blockDim.x;
+    double fk[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
         double f[6];
         gt_node_values(Fe, row_stride, map, g, base, frac, w, f);
 #pragma unroll
-        for (int c = 0; c < 6; ++c)
+        for (int c = 0; c < 6; ++c) {
             if (f[c] != 0.0) em[c] = max(em[c], ilogb(f[c]));
+            fk[c] = f[c];
+        }
     }
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -160,7 +166,14 @@ __global__ void __launch_bounds__(128) k_gsf_tc_rows(int ntab, int ng, int nkc, 
     }
     for (int g = threadIdx.x; g < nkc * GT_KC; g += blockDim.x) {
         double f[6] = {0, 0, 0, 0, 0, 0};
-        if (g < ng) gt_node_values(Fe, row_stride, map, g, base, frac, w, f);
+        if (g < ng) {
+            if (keep) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) f[c] = fk[c];
+            } else {
+                gt_node_values(Fe, row_stride, map, g, base, frac, w, f);
+            }
+        }
         const size_t cofs = (size_t)(g / GT_KC) * GT_A_CHUNK;
 #pragma unroll
         for (int c = 0; c < 6; ++c) {

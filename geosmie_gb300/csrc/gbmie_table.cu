@@ -344,9 +344,11 @@ struct KSum {
 };
 
 // (launch bounds match the launches: 64 threads for the FP32 sums of the
-// mixed path, 256 for the FP64 sums)
+// mixed path, 256 for the FP64 sums; one block per SM is enough for the
+// register bound, which lets the sums and the prefetched next size stay in
+// registers: 0.25 -> 0.17 ms on the sulfate-like table)
 template <int NB, typename T>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 64 : 256) k_tab_scalars(TabView v)
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 64 : 256, 1) k_tab_scalars(TabView v)
 {
     __shared__ double sR[NB][15];
     __shared__ double sRed[8][NB * 9];
@@ -366,20 +368,41 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 64 : 256) k_tab_scalars(TabVi
         for (int b = 0; b < NB; ++b)
 #pragma unroll
             for (int j = 0; j < 9; ++j) acc[b][j].zero();
+        // the inputs of a thread's next size are loaded one iteration ahead,
+        // so that their latency overlaps the current size's sums
+        const size_t w0 = v.wlam(lam) + ((size_t)rh * v.n_bin * v.n_comp + comp) * v.n_size;
+        const size_t wstep = (size_t)v.n_comp * v.n_size;   // between bins
+        auto load = [&](int i, double4 &e4, double &rad, T (&wv)[NB]) {
+            if (i < v.n_size) {
+                e4 = make_double4(E[4 * i], E[4 * i + 1], E[4 * i + 2], E[4 * i + 3]);
+                rad = v.radius(lam, i);
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+                    wv[b] = b < v.n_bin ? (sizeof(T) == 8 ? (T)v.W[w0 + b * wstep + i] : (T)v.Wf[w0 + b * wstep + i]) : (T)0;
+            }
+        };
+        double4 e4n = make_double4(0.0, 0.0, 0.0, 0.0);
+        double radn = 0.0;
+        T wn[NB];
+        load(threadIdx.x, e4n, radn, wn);
         for (int i = threadIdx.x; i < v.n_size; i += blockDim.x) {
-            const T r = (T)(v.radius(lam, i) * rscale);
+            const double4 e4 = e4n;
+            const double rad = radn;
+            T wv[NB];
+#pragma unroll
+            for (int b = 0; b < NB; ++b) wv[b] = wn[b];
+            load(i + blockDim.x, e4n, radn, wn);
+            const T r = (T)(rad * rscale);
             const T A = (T)PI_D * r * r;
-            const T qext = (T)E[4 * i], qsca = (T)E[4 * i + 1], qb = (T)E[4 * i + 2], g = (T)E[4 * i + 3];
-            const T qabs = (T)(E[4 * i] - E[4 * i + 1]);
+            const T qext = (T)e4.x, qsca = (T)e4.y, qb = (T)e4.z, g = (T)e4.w;
+            const T qabs = (T)(e4.x - e4.y);
             const T as = A * qsca;
             const T f[9] = {A, qext * A, qsca * A, qabs * A, qb * A, g * as, qsca * A * as, qext * A * as, as};
 #pragma unroll
             for (int b = 0; b < NB; ++b) {
                 if (b < v.n_bin) {
-                    const size_t wi = v.wlam(lam) + (((size_t)rh * v.n_bin + b) * v.n_comp + comp) * v.n_size + i;
-                    const T w = sizeof(T) == 8 ? (T)v.W[wi] : (T)v.Wf[wi];
 #pragma unroll
-                    for (int j = 0; j < 9; ++j) acc[b][j].add(w * f[j]);
+                    for (int j = 0; j < 9; ++j) acc[b][j].add(wv[b] * f[j]);
                 }
             }
         }
