@@ -57,6 +57,7 @@ SIGNATURES = {
     "gbmie_table_run_graph": (ctypes.c_int, [_P, _P, _P]),
     "gbmie_table_plan_autotune": (ctypes.c_int, [_P, _P, _P]),
     "gbmie_table_plan_tuning": (ctypes.c_int, [_P, _P]),
+    "gbmie_table_plan_set_tuning": (ctypes.c_int, [_P, _P]),
     "gbmie_table_plan_set_wait_limit": (ctypes.c_int, [_P, _I64]),
     "gbmie_table_plan_set_dn_fp64": (ctypes.c_int, [_P, _I32]),
     "gbmie_gsf": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32, _P, _P, _I32]),

@@ -1186,6 +1186,7 @@ static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, co
 }
 
 int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *scr);
+int table_tc_win_max();
 
 // The plain angular kernel over one nmax bucket (sizes of every unit whose
 // nmax falls in it; bucket GBMIE_TUNE_BUCKETS = the whole grid), `chunk`
@@ -1518,6 +1519,30 @@ extern "C" int gbmie_table_plan_tuning(const gbmie_table_plan *p, int32_t *param
     params[0] = p->tuned;
     tune_save(p, params + 1);
     params[14] = params[15] = 0;
+    return GBMIE_OK;
+}
+
+// The inverse of gbmie_table_plan_tuning: launch parameters given by the
+// caller (those of an earlier autotuning, say), checked against the choices
+// the autotuner itself makes, which the plan's scratch is sized for.
+extern "C" int gbmie_table_plan_set_tuning(gbmie_table_plan *p, const int32_t *params)
+{
+    if (!p || !params) return GBMIE_ERR_INVALID;
+    const int32_t *q = params + 1;
+    bool ok = q[0] == 0 || q[0] == 1;
+    for (int b = 0; b <= GBMIE_TUNE_BUCKETS; ++b) {
+        const int c = q[1 + b], t = q[1 + GBMIE_TUNE_BUCKETS + 1 + b];
+        ok = ok && (c == 64 || c == 128 || c == 256 || c == 512) && t >= 32 && t <= 256 && t % 32 == 0;
+    }
+    ok = ok && (q[11] == 64 || q[11] == 128 || q[11] == 256) && q[12] >= 1 && q[12] <= table_tc_win_max();
+    if (!ok) return ctx_fail(p->ctx, GBMIE_ERR_INVALID, "gbmie_table_plan_set_tuning: parameters out of range");
+    if (p->gexec) {   // a captured graph holds the old launches; none of its replays may be in flight
+        GBMIE_TRY(ctx_cuda(p->ctx, cudaStreamSynchronize(p->ctx->stream), "set_tuning"));
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+    }
+    tune_load(p, q);
+    p->tuned = 1;
     return GBMIE_OK;
 }
 

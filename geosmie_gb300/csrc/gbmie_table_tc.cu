@@ -1475,6 +1475,7 @@ int launch_table_mixed(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, char *sc
 }
 
 size_t table_mixed_smem_bytes() { return TC_SMEM_BYTES(8); }
+int table_tc_win_max() { return TC_WIN_MAX; }
 
 // The B operands depend only on the angles and the largest nmax: built once
 // per plan into plan-owned memory (plan creation synchronises afterwards).

@@ -242,6 +242,19 @@ class TablePlan(object):
         return {"tuned": bool(q[0]), "plain_per_bucket": bool(q[1]), "plain_chunk": list(q[2:7]),
                 "plain_threads": list(q[7:12]), "coef_block": int(q[12]), "tc_window": int(q[13])}
 
+    def set_tuning(self, tun):
+        """Launch parameters in the form tuning() returns (those of an earlier
+        autotuning, say): a table's bits depend only on them, so saved
+        parameters reproduce a table exactly in another process."""
+        q = (ctypes.c_int32 * 16)()
+        q[1] = int(bool(tun["plain_per_bucket"]))
+        for b in range(5):
+            q[2 + b] = int(tun["plain_chunk"][b])
+            q[7 + b] = int(tun["plain_threads"][b])
+        q[12] = int(tun["coef_block"])
+        q[13] = int(tun["tc_window"])
+        self.ctx.check(self.ctx.lib.gbmie_table_plan_set_tuning(self.h, q), "gbmie_table_plan_set_tuning")
+
     def sync(self):
         """Wait for the plan's last run (on its stream) and raise on a device
         error flag."""

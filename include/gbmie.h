@@ -305,6 +305,15 @@ int gbmie_table_plan_set_dn_fp64(gbmie_table_plan *plan, int32_t enable);
  * buckets and of the whole-grid launch; [12] coefficient block size of the
  * mixed path; [13] its accumulation window. */
 int gbmie_table_plan_tuning(const gbmie_table_plan *plan, int32_t *params);
+/* Sets the launch parameters in the layout of gbmie_table_plan_tuning
+ * (params[0] is ignored): chunks of 64, 128, 256 or 512 sizes, 32 to 256
+ * angles per pass (multiples of 32), coefficient block 64, 128 or 256,
+ * accumulation window 1 to 4; else GBMIE_ERR_INVALID.  A table's bits
+ * depend on its launch layout only (repeated runs, graph replays and other
+ * plans with the same parameters give identical outputs), so parameters
+ * saved from one process reproduce its tables in another.  Drops a captured
+ * graph of the plan.  No counterpart in the reference. */
+int gbmie_table_plan_set_tuning(gbmie_table_plan *plan, const int32_t *params);
 
 /* ---- GSF expansion ------------------------------------------------------ */
 /* Expansion coefficients of ntab scattering matrices given on one angle grid:

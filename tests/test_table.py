@@ -375,6 +375,47 @@ def test_table_bits_reproducible_gpu(precision):
 
 
 @pytest.mark.gpu
+def test_set_tuning_gpu():
+    """gbmie_table_plan_set_tuning: launch parameters given by the caller.
+    The plain path's per-bucket layout (each nmax bucket its own launch, its
+    chunks in consecutive partial-sum slots) equals the whole-grid layout to
+    1e-12 of P11 (other partial sums); two plans with the same parameters
+    give identical bits; the mixed path with window 2 or 4 stays within 1e-6
+    of the FP64 table; out-of-range parameters are refused."""
+    from geosmie_gb300.table import TablePlan
+    spec = synthetic_spec(nl=2, nrh=2, ns=700, nbin=3)
+    split = {"plain_per_bucket": True, "plain_chunk": [64, 128, 64, 256, 128],
+             "plain_threads": [64, 128, 192, 256, 192], "coef_block": 128, "tc_window": 3}
+    whole = dict(split, plain_per_bucket=False)
+    res = {}
+    for name, tun in (("split", split), ("split2", split), ("whole", whole)):
+        plan = TablePlan(spec, precision=0)
+        plan.set_tuning(tun)
+        got = plan.tuning()
+        assert got["tuned"] and all(got[k] == tun[k] for k in tun), got
+        plan.run()
+        res[name] = plan.results()
+        plan.close()
+    p11 = np.abs(res["whole"]["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(res["split"][k] - res["whole"][k]) / p11) < 1e-12, k
+    for k in res["split"]:
+        assert np.array_equal(res["split"][k], res["split2"][k]), k
+    for win in (2, 4):
+        plan = TablePlan(spec, precision=1)
+        plan.set_tuning(dict(whole, tc_window=win))
+        plan.run()
+        m = plan.results()
+        for k in SCAT:
+            assert np.max(np.abs(m[k] - res["whole"][k]) / p11) < 1e-6, (win, k)
+        with pytest.raises(ValueError, match="out of range"):
+            plan.set_tuning(dict(whole, plain_chunk=[100, 128, 64, 256, 128]))
+        with pytest.raises(ValueError, match="out of range"):
+            plan.set_tuning(dict(whole, tc_window=9))
+        plan.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 1])
 def test_autotune_gpu(precision):
     """gbmie_table_plan_autotune: the tuned table equals the default one
