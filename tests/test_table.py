@@ -124,7 +124,7 @@ def synthetic_spec(nl=3, nrh=4, ns=300, nbin=3, nang=181, seed=20261203):
     m = np.empty((nl, nrh, 1), np.complex128)
     for i in range(nl):
         m[i, :, 0] = nw + (ndry - nw) / gf ** 3 * (1 + 0.01 * rng.random())
-    rg = 0.0695e-6 * np.array([0.5, 1.0, 2.0, 4.0, 0.25])[:nbin]
+    rg = 0.0695e-6 * np.array([0.5, 1.0, 2.0, 4.0, 0.25, 0.125, 8.0, 1.5])[:nbin]
     return {
         "lambda": lam, "grid": r, "dgrid": np.gradient(r), "grid_kind": 1, "m": m,
         "psd_kind": 0, "psd_param": np.array([[[g_, 0.0, 1e30, 2.03]] for g_ in rg]), "gf_psd": gf,
@@ -372,6 +372,32 @@ def test_table_bits_reproducible_gpu(precision):
         for b in outs[1:]:
             for k in a:
                 assert np.array_equal(b[k], a[k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nbin,nang", [(8, 181), (7, 300), (6, 512)])
+def test_many_bins_and_angle_blocks_gpu(nbin, nang):
+    """Tables of 6-8 bins (the contraction's largest sets of sums, its shared
+    memory closest to the limit) and of 300 or 512 angles (three or four
+    128-angle blocks: the resident angle chunk is reloaded per (unit,
+    block)): the FP64 table against the oracle, the mixed table against the
+    FP64 one at 1e-6 (phase elements of P11, scalars relative)."""
+    from geosmie_gb300.table import TablePlan
+    from oracle import integration
+    spec = synthetic_spec(nl=2, nrh=2, ns=300, nbin=nbin, nang=nang)
+    res = []
+    for prec in (0, 1):
+        plan = TablePlan(spec, precision=prec)
+        plan.run()
+        res.append(plan.results())
+        plan.close()
+    a, b = res
+    _check_table(a, integration.run_spec(spec))
+    p11 = np.abs(a["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, k
+    for k in TIGHT:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, k
 
 
 @pytest.mark.gpu
