@@ -401,6 +401,49 @@ def test_many_bins_and_angle_blocks_gpu(nbin, nang):
 
 
 @pytest.mark.gpu
+def test_ragged_and_refused_tables_gpu():
+    """Size counts that leave partial tiles: 2 and 20 sizes (one partial half
+    tile), 33 (a full half tile and one size), 65 (one tile and one size), in
+    both precisions against the oracle and each other; and tables the plan
+    refuses (one size, one angle, nine bins) raise ValueError before any
+    device work.  With this few sizes the phase function keeps the deep
+    interference minima of single large spheres (x up to 157), where the
+    mixed path's error relative to P11 at the same angle is ill-conditioned
+    (6e-6 at two sizes): here it is bounded by 1e-6 of the entry's largest
+    P11."""
+    from geosmie_gb300.table import TablePlan
+    from oracle import integration
+    for ns in (2, 20, 33, 65):
+        spec = synthetic_spec(nl=2, nrh=2, ns=ns, nbin=2)
+        res = []
+        for prec in (0, 1):
+            plan = TablePlan(spec, precision=prec)
+            plan.run()
+            res.append(plan.results())
+            plan.close()
+        a, b = res
+        _check_table(a, integration.run_spec(spec))
+        p11max = np.max(np.abs(a["p11"]), axis=-1, keepdims=True)
+        for k in SCAT:
+            assert np.max(np.abs(b[k] - a[k]) / p11max) < 1e-6, (ns, k)
+        for k in TIGHT:
+            assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, (ns, k)
+    one_size = synthetic_spec(nl=1, nrh=1, ns=2, nbin=2)
+    one_size["grid"], one_size["dgrid"] = one_size["grid"][:1], one_size["dgrid"][:1]
+    for spec in (one_size, synthetic_spec(nl=1, nrh=1, nbin=2, nang=1)):
+        with pytest.raises(ValueError, match="bad sizes"):
+            TablePlan(spec, precision=1)
+    spec = synthetic_spec(nl=1, nrh=1, nbin=8)
+    for k in ("frac", "rhop"):
+        spec[k] = np.concatenate([spec[k], spec[k][:1]], axis=0)
+    for k in ("rhop0", "rlow", "rup"):
+        spec[k] = np.concatenate([spec[k], spec[k][:1]])
+    spec["psd_param"] = np.concatenate([spec["psd_param"], spec["psd_param"][:1]], axis=0)
+    with pytest.raises(ValueError, match="n_bin"):
+        TablePlan(spec, precision=1)
+
+
+@pytest.mark.gpu
 def test_set_tuning_gpu():
     """gbmie_table_plan_set_tuning: launch parameters given by the caller.
     The plain path's per-bucket layout (each nmax bucket its own launch, its
