@@ -294,8 +294,10 @@ int gbmie_ctx_synchronize(gbmie_ctx *ctx)
 // CSR layout: offsets[i+1] - offsets[i] = nmax(size[i]) + add_per_row.
 // Three passes: per-block scan, scan of block totals, add block bases.
 // ---------------------------------------------------------------------------
-#define SCAN_THREADS 1024
-#define SCAN_ITEMS 4
+// one row per thread in 256-thread blocks: the rows' nmax (an FP64 pow each)
+// spread over every SM (120,000 rows: 469 blocks rather than 30)
+#define SCAN_THREADS 256
+#define SCAN_ITEMS 1
 
 __device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t *total)
 {
