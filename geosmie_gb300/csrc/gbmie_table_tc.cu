@@ -701,6 +701,13 @@ static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
      TC_SUM_FLOATS(NB) * 4 + TC_CTRL_BYTES)
 #define TC_NO_EX (-0x40000000)                         // no size: its weights are dropped
 #define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
+// back-off of the epilogue warps' waits (their lane 0 polls the weight slot
+// and the accumulator set): a polling warp takes issue slots from the
+// single-thread roles on its sub-partition.  Sulfate-like table, contraction
+// 3.04 ms without back-off, 2.98 / 2.97 / 2.97 ms with 32 / 128 / 512 ns; a
+// try_wait suspend-time hint of 1 us instead: 3.13 ms; back-off in the
+// issuers' waits as well: 2.99-3.01 ms
+#define TC_EPI_SLEEP_NS 128
 
 static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
 static_assert(8 * (2 * TC_NS + 2 + 2 * TC_NSETS + 1 + 2 * TC_NW) + 4 + 8 + 4 * TC_NS <= TC_CTRL_BYTES, "control block");
@@ -1183,7 +1190,8 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             const uint32_t wsl = ie % TC_NW;
             {
                 int go = 1;
-                if (lane == 0) go = mbar_wait_or_abort(w_full + wsl, (ie / TC_NW) & 1u, s_abort, 0, g.wait_limit) ? 1 : 0;
+                if (lane == 0)
+                    go = mbar_wait_or_abort(w_full + wsl, (ie / TC_NW) & 1u, s_abort, TC_EPI_SLEEP_NS, g.wait_limit) ? 1 : 0;
                 go = __shfl_sync(0xffffffffu, go, 0);
                 if (!go) {
                     ok = false;
@@ -1203,7 +1211,8 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 const uint32_t wi = ip ? wce[1] : wce[0];
                 const uint32_t set = 2 * ip + (wi & 1u), use = wi >> 1;
                 int go = 1;
-                if (lane == 0) go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort, 0, g.wait_limit) ? 1 : 0;
+                if (lane == 0)
+                    go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort, TC_EPI_SLEEP_NS, g.wait_limit) ? 1 : 0;
                 go = __shfl_sync(0xffffffffu, go, 0);
                 if (!go) {
                     ok = false;
