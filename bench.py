@@ -268,7 +268,9 @@ def executed_flop(counts):
     same steps: 15 per warm-up D_n step, 32 per order.  Tensor cores: 6 MMAs
     (M 128 angles x N 64 (32 sizes, Re/Im) x K 16) per 16-order chunk of a
     half tile of 32 sizes, per 128-angle block (3 split products x 2 GEMMs,
-    padded)."""
+    padded); a whole-tile item runs both halves as N = 128, the same flop,
+    except that a last tile of 32 sizes or fewer taken whole also runs its
+    empty half (not counted)."""
     nang, nbin, inst = counts["nang"], counts["nbin"], counts["instances"]
     return {"k_tab_s12_plain": (8.0 * counts["sum_nmax"] + (14.0 + 8.0 * nbin) * inst) * nang,
             "k_tab_coeffs": 12.0 * counts["sum_nmx"] + 89.0 * counts["sum_nmax"],

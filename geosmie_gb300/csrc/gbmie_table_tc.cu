@@ -33,7 +33,12 @@
 #define TC_HALF 32                      // sizes per half tile (MMA N = 64: Re, Im)
 #define TC_ABLK 128                     // angles per block (MMA M)
 #define TC_MAT_A (16 * TC_ABLK * 2)     // one angle-function matrix of a 16-order chunk: 4 KB
-#define TC_MAT_B (16 * 2 * TC_HALF * 2) // one coefficient matrix of a half-tile chunk: 2 KB
+// one coefficient matrix of a tile's chunk: 128 rows (64 sizes x Re, Im) x
+// 16 orders, FP16, K-major core matrices [kg = order / 8 % 2][row / 8][row %
+// 8][8 orders]: 4 KB.  A whole-tile MMA reads it with N = 128, a half-tile
+// MMA its rows 64 h .. 64 h + 63 (1 KB further on per h) with N = 64; both
+// step 2 KB between the two 8-order groups
+#define TC_MAT_B (16 * 2 * TC_INST * 2)
 #define SHIFT_BITS 13
 
 // ---------------------------------------------------------------------------
@@ -289,9 +294,10 @@ struct EmitCf {
 // Coefficient operand of the contraction (MMA B), written once per (unit,
 // 64-size tile, 16-order chunk) as a 16 KB block in the no-swizzle K-major
 // shared-memory layout
-//   [half h][matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
-// (rows 2 i', 2 i' + 1 = Re, Im of size 32 h + i'), so that the contraction
-// loads a half tile with one 8 KB bulk copy.  split_rows writes the rows of
+//   [matrix C_hi C_lo D_hi D_lo][kg = order / 8 % 2][row / 8][row % 8][8 orders]
+// (rows 2 i, 2 i + 1 = Re, Im of size i of the tile), so that the contraction
+// loads a tile's chunk with one 16 KB bulk copy and multiplies the whole tile
+// or either half of it.  split_rows writes the rows of
 // one instance (size i of its unit): FP32 (c, d) orders 1..nmax -> FP16
 // hi/lo scaled by 2^(13 - e_i), in every chunk of the instance's tile, zero
 // past nmax.  The coefficient kernels call it
@@ -323,7 +329,7 @@ __device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int 
     const int nc = si.cb1 - si.cb0;
     uint8_t *dst = asplit + (size_t)(si.ucb + si.cb0) * 16384;
     const float sc = ldexpf(1.0f, max(-126, min(126, SHIFT_BITS - ex)));
-    const int hh = ia >> 5, r0 = 2 * (ia & 31);
+    const int r0 = 2 * ia;
     for (int j = 0; j < nc; ++j)
 #pragma unroll
         for (int kg = 0; kg < 2; ++kg) {
@@ -340,29 +346,27 @@ __device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int 
             }
             // rows r0 (Re) and r1 = r0 + 1 (Im) of a matrix are 32 contiguous,
             // 32-byte aligned bytes (r0 even): one 256-bit store each
-            const uint32_t o0 = hh * 8192 + kg * 1024 + (r0 >> 3) * 128 + (r0 & 7) * 16;
+            const uint32_t o0 = kg * 2048 + (r0 >> 3) * 128 + (r0 & 7) * 16;
             uint8_t *blk = dst + (size_t)j * 16384;
-            st_global_32b(blk + 0 * 2048 + o0, *(uint4 *)ch[0], *(uint4 *)ch[1]);
-            st_global_32b(blk + 1 * 2048 + o0, *(uint4 *)cl[0], *(uint4 *)cl[1]);
-            st_global_32b(blk + 2 * 2048 + o0, *(uint4 *)ch[2], *(uint4 *)ch[3]);
-            st_global_32b(blk + 3 * 2048 + o0, *(uint4 *)cl[2], *(uint4 *)cl[3]);
+            st_global_32b(blk + 0 * TC_MAT_B + o0, *(uint4 *)ch[0], *(uint4 *)ch[1]);
+            st_global_32b(blk + 1 * TC_MAT_B + o0, *(uint4 *)cl[0], *(uint4 *)cl[1]);
+            st_global_32b(blk + 2 * TC_MAT_B + o0, *(uint4 *)ch[2], *(uint4 *)ch[3]);
+            st_global_32b(blk + 3 * TC_MAT_B + o0, *(uint4 *)cl[2], *(uint4 *)cl[3]);
         }
     // the last size of a partial tile also zeroes the rows of the sizes the
-    // tile lacks (their PSD weights are zero, but 0 x NaN would not be); a
-    // half tile without sizes is never read
+    // tile lacks (their PSD weights are zero, but 0 x NaN would not be): a
+    // whole-tile MMA reads all 128 rows
     const int ntile = min(64, v.n_size - 64 * tile);
     if (ia == ntile - 1 && ntile < 64) {
         const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-        const int rend = ntile <= 32 ? 64 : 128;
         for (int j = 0; j < nc; ++j)
-            for (int r = 2 * ntile; r < rend; ++r)
+            for (int r = 2 * ntile; r < 128; ++r)
 #pragma unroll
                 for (int kg = 0; kg < 2; ++kg) {
-                    const int rr = r & 63;
-                    const uint32_t o = (r >> 6) * 8192 + kg * 1024 + (rr >> 3) * 128 + (rr & 7) * 16;
+                    const uint32_t o = kg * 2048 + (r >> 3) * 128 + (r & 7) * 16;
                     uint8_t *blk = dst + (size_t)j * 16384;
 #pragma unroll
-                    for (int mtx = 0; mtx < 4; ++mtx) *(uint4 *)(blk + mtx * 2048 + o) = z;
+                    for (int mtx = 0; mtx < 4; ++mtx) *(uint4 *)(blk + mtx * TC_MAT_B + o) = z;
                 }
     }
 }
@@ -619,34 +623,41 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 // bulk P11 error at x = 628 near 2.6e-7 this way.
 //
 // Orientation: angles are the MMA's M (128 per block, TMEM lanes), the
-// (size, Re/Im) rows of half a tile its N (64 columns = 32 sizes).  Each
-// epilogue thread owns one angle and 16 sizes, so the Mueller elements and
-// their PSD-weighted sums over sizes stay in its registers: no shared-memory
-// staging, no shuffles and no barrier among the epilogue warps.
+// (size, Re/Im) rows of a 64-size tile its N (128 columns), or of half a
+// tile (64 columns) when the tile's orders span several accumulation
+// windows.  Each epilogue thread owns one angle and 16 sizes of each half
+// tile, so the Mueller elements and their PSD-weighted sums over sizes stay
+// in its registers: no shared-memory staging, no shuffles and no barrier
+// among the epilogue warps.
 //
 // Pipeline (one CTA per SM, persistent, 12 warps):
 //   warps 0-7   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
-//               angles) and columns of sizes 16 (w / 4) .. + 15 of the half
+//               angles) and columns of sizes 16 (w / 4) .. + 15 of each half
 //               tile; window sums -> Mueller -> PSD-weighted sums
 //   warps 8, 10 MMA issue (one thread each; items alternate between them)
-//   warp 9      producer (one thread): bulk copies of the coefficient half
-//               tiles (split_rows) and of the angle functions of orders > 16
-//               into a TC_NS-stage shared-memory ring
-//   warp 11     weights: per item the chunk count, the unit's constants and
+//   warp 9      producer (one thread): bulk copies of the coefficient chunks
+//               of a tile (split_rows) and of the angle functions of orders
+//               > 16 into a TC_NS-stage shared-memory ring
+//   warp 11     weights: per tile the chunk count, the unit's constants and
 //               the PSD weights, scaled and paired for the epilogue's packed
 //               FMAs, into a TC_NW-slot shared-memory ring (the epilogue
 //               warps make no global loads)
-// Work items are (unit, angle block, 64-size tile, half tile); a half tile
-// without sizes (the last tile of a grid) is skipped by every role.  TMEM
-// holds TC_NSETS accumulator sets (S+ 64 columns | S- 64 columns), so the
-// MMAs run up to four windows ahead of the epilogue.  The angle-function
-// chunk of orders 1..16 stays resident for up to TC_B0_SLOTS angle blocks
-// (loaded once: it is the same for every unit; 84% of the sulfate-like
-// table's tiles need no other order); with more blocks one slot is reloaded
-// at every (unit, block) change.  mbarriers: stage full/empty, resident
-// full/empty, accumulator-set full/empty.  Every wait is bounded and also
-// ends when another role has raised the block's abort flag; the epilogue
-// warps decide per warp (lane 0 waits, the warp follows its answer).
+// Work items are (unit, angle block, 64-size tile) when the tile's orders
+// fit one accumulation window (S+ and S- of its 64 sizes fill both of an
+// issuer's accumulator sets), else (unit, angle block, tile, half tile) with
+// one set per window; a half tile without sizes (the last tile of a grid) is
+// skipped by every role.  Whole-tile items halve the windows, MMA
+// instructions and hand-offs per size, which is what the contraction's time
+// follows.  TMEM holds TC_NSETS accumulator sets of 128 columns, so the MMAs
+// run up to two whole-tile or four half-tile windows ahead of the epilogue.
+// The angle-function chunk of orders 1..16 stays resident for up to
+// TC_B0_SLOTS angle blocks (loaded once: it is the same for every unit; 84%
+// of the sulfate-like table's tiles need no other order); with more blocks
+// one slot is reloaded at every (unit, block) change.  mbarriers: stage
+// full/empty, resident full/empty, accumulator-set full/empty, weight slot
+// full/empty.  Every wait is bounded and also ends when another role has
+// raised the block's abort flag; the epilogue warps decide per warp (lane 0
+// waits, the warp follows its answer).
 // ---------------------------------------------------------------------------
 struct TcArgs {
     TabView v;
@@ -666,10 +677,10 @@ struct TcArgs {
     int *flags;
 };
 
-// ring stages: the copies of a stage's next chunk wait for its MMAs, so the
-// ring's depth bounds the chunks in flight (sulfate-like table: 4 stages
-// 3.15 ms, 5 stages 3.04, 6 stages 3.03)
-#define TC_NS 6
+// ring stages of a tile's chunk (coefficients of 64 sizes, angle functions
+// of orders > 16): the copies of a stage's next chunk wait for its MMAs, so
+// the ring's depth bounds the chunks in flight
+#define TC_NS 4
 // longest accumulation window (chunks): the windows the accuracy of the FP32
 // accumulation was checked with (2-4 keep it near 2e-7); a window's chunks
 // sit in the ring together
@@ -680,8 +691,8 @@ static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
 // angles reload one slot per (unit, block))
 #define TC_B0_SLOTS(NB) 2
 #define TC_A_BYTES (4 * TC_MAT_A)                      // P_hi P_lo Q_hi Q_lo of a chunk: 16 KB
-#define TC_B_BYTES (4 * TC_MAT_B)                      // C_hi C_lo D_hi D_lo of a half chunk: 8 KB
-#define TC_STAGE_BYTES (TC_B_BYTES + TC_A_BYTES)       // 24 KB
+#define TC_B_BYTES (4 * TC_MAT_B)                      // C_hi C_lo D_hi D_lo of a tile's chunk: 16 KB
+#define TC_STAGE_BYTES (TC_B_BYTES + TC_A_BYTES)       // 32 KB
 #define TC_EPI_WARPS 8
 #define TC_EPI_THREADS (32 * TC_EPI_WARPS)
 #define TC_THREADS (TC_EPI_THREADS + 128)              // + two MMA warps, the producer and the weights warp
@@ -694,10 +705,11 @@ static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
 // mbarriers (2 TC_NS + 2 + 2 TC_NSETS + 1 + 2 TC_NW), the TMEM address, the
 // abort flag and the stages' chunk tags
 #define TC_CTRL_BYTES 512
-#define TC_WSLOT_FLOATS (16 + 32 * 16)                 // header + 32 sizes x 8 bins x (w, w)
+#define TC_NP(NB) (((NB) + 1) / 2)                     // float4 weight entries per size: two bins each
+#define TC_WSLOT_FLOATS(NB) (16 + TC_INST * 4 * TC_NP(NB))   // header + 64 sizes x bin pairs x (w, w, w', w')
 #define TC_SUM_FLOATS(NB) (4 * (NB) * TC_EPI_THREADS)  // running sums [bin][thread] of (E0 pair, E1 pair)
 #define TC_SMEM_BYTES(NB)                                                                                  \
-    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS * TC_STAGE_BYTES + TC_NW * TC_WSLOT_FLOATS * 4 +                     \
+    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS * TC_STAGE_BYTES + TC_NW * TC_WSLOT_FLOATS(NB) * 4 +                 \
      TC_SUM_FLOATS(NB) * 4 + TC_CTRL_BYTES)
 #define TC_NO_EX (-0x40000000)                         // no size: its weights are dropped
 #define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
@@ -756,9 +768,9 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sB0 = smem;                                            // resident angle chunks, orders 1..16
-    uint8_t *sStage = sB0 + TC_B0_SLOTS(NB) * TC_A_BYTES;           // TC_NS x (coeff 8 KB | angles 16 KB)
-    float *sW = (float *)(sStage + TC_NS * TC_STAGE_BYTES);         // weight ring [TC_NW][TC_WSLOT_FLOATS]
-    float *sSum = sW + TC_NW * TC_WSLOT_FLOATS;                     // per-(unit, block) running sums
+    uint8_t *sStage = sB0 + TC_B0_SLOTS(NB) * TC_A_BYTES;           // TC_NS x (coeff 16 KB | angles 16 KB)
+    float *sW = (float *)(sStage + TC_NS * TC_STAGE_BYTES);         // weight ring [TC_NW][TC_WSLOT_FLOATS(NB)]
+    float *sSum = sW + TC_NW * TC_WSLOT_FLOATS(NB);                 // per-(unit, block) running sums
     uint64_t *bars = (uint64_t *)(sSum + TC_SUM_FLOATS(NB));
     uint64_t *full = bars, *empty = bars + TC_NS;
     uint64_t *b0_full = bars + 2 * TC_NS, *b0_empty = b0_full + 1;
@@ -817,11 +829,12 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         // the tensor core's time for it.
         const uint32_t p = warp == 10 ? 1u : 0u;
         if (lane == 0) {
-            const uint32_t idesc = idesc_f16_f32(TC_ABLK, 2 * TC_HALF);
+            // whole-tile items N = 128 (64 sizes x Re, Im), half-tile items N = 64
+            const uint32_t idesc_t = idesc_f16_f32(TC_ABLK, 2 * TC_INST), idesc_h = idesc_f16_f32(TC_ABLK, 2 * TC_HALF);
             // no-swizzle K-major descriptors without the start address: A (angles)
-            // LBO = 16 core matrices (K step of 8 orders), B (coefficients) 8; SBO 128 B
+            // LBO = 16 core matrices (K step of 8 orders), B (coefficients) 16; SBO 128 B
             constexpr uint64_t DESC_A = ((uint64_t)((16 * 128) >> 4) << 16) | ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
-            constexpr uint64_t DESC_B = ((uint64_t)((8 * 128) >> 4) << 16) | ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
+            constexpr uint64_t DESC_B = ((uint64_t)((16 * 128) >> 4) << 16) | ((uint64_t)(128 >> 4) << 32) | (1ull << 46);
             const uint32_t sStage0 = smem_u32(sStage);
             uint32_t it = 0, ii = 0, wc = 0, b0_loads = 0;   // chunks, items, own windows
             bool ok = true, have_b0 = false;
@@ -858,18 +871,33 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                             o0 = ldg_pin_s64(off + last_of(tile + 1) - 1);
                         }
                         const int nc = (kt + TC_KC16 - 1) / TC_KC16;
-                        for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h, ++ii) {
+                        // a tile whose chunks fit one window is one item (N = 128,
+                        // its S+ and S- in both of the issuer's accumulator sets);
+                        // otherwise each half tile with sizes is one (N = 64, one
+                        // set per window)
+                        const bool whole = nc <= g.win;
+                        const int nitem = whole ? 1 : (ntile > TC_HALF ? 2 : 1);
+                        for (int h = 0; h < nitem && ok; ++h, ++ii) {
                             if ((ii & 1u) != p) {   // the other issuer's item
                                 it += nc;
                                 continue;
                             }
+                            const uint32_t bh = whole ? 0u : (uint32_t)h * (1024 >> 4);   // half tile: rows 64 h..
+                            const uint32_t idesc = whole ? idesc_t : idesc_h;
                             for (int w0 = 0; w0 < nc && ok; w0 += g.win) {
                                 const int nj = min(g.win, nc - w0);
-                                const uint32_t set = 2 * p + (wc & 1u), use = wc >> 1;
-                                if (use > 0 && !mbar_wait_or_abort(acc_empty + set, (use - 1) & 1u, s_abort, 0, g.wait_limit)) {
-                                    ok = false;
-                                    break;
+                                // accumulator sets: one per window, both for a whole tile
+                                const int nset = whole ? 2 : 1;
+                                uint32_t set[2];
+                                for (int q = 0; q < nset && ok; ++q) {
+                                    const uint32_t x = wc + q;
+                                    set[q] = 2 * p + (x & 1u);
+                                    const uint32_t use = x >> 1;
+                                    if (use > 0 &&
+                                        !mbar_wait_or_abort(acc_empty + set[q], (use - 1) & 1u, s_abort, 0, g.wait_limit))
+                                        ok = false;
                                 }
+                                if (!ok) break;
                                 for (int j = 0; j < nj && ok; ++j) {
                                     const uint32_t c = it + j, st = c % TC_NS, par = (c / TC_NS) & 1u;
                                     ok = false;
@@ -887,7 +915,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 }
                                 if (!ok) break;
                                 tc_fence_after();
-                                const uint32_t d = tmem + set * 128;   // S+ at d, S- at d + 64
+                                // S+ and S- columns: a half-tile window's set holds S+ at
+                                // 0 and S- at 64; a whole tile's S+ fills one set, S- the other
+                                const uint32_t dp = tmem + set[0] * 128;
+                                const uint32_t dm = whole ? tmem + set[1] * 128 : dp + 64;
                                 for (int pass = 0; pass < 2; ++pass) {
                                     for (int j = 0; j < nj; ++j) {
                                         const uint32_t c = it + j;
@@ -895,23 +926,23 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                         const uint32_t sA = (w0 + j) == 0 ? aB0 : sB + TC_B_BYTES;
                                         // descriptors: constant LBO/SBO fields + start address / 16;
                                         // matrix m of an operand starts m x its matrix size later
-                                        const uint64_t a0 = DESC_A | (sA >> 4), b0 = DESC_B | (sB >> 4);
+                                        const uint64_t a0 = DESC_A | (sA >> 4), b0 = (DESC_B | (sB >> 4)) + bh;
                                         constexpr uint64_t MA = TC_MAT_A >> 4, MB = TC_MAT_B >> 4;
                                         if (pass == 0) {   // cross products: small accumulator
-                                            mma_f16(d, a0, b0 + MB, idesc, j == 0 ? 0u : 1u);
-                                            mma_f16(d, a0 + MA, b0, idesc, 1u);
-                                            mma_f16(d + 64, a0 + 2 * MA, b0 + 3 * MB, idesc, j == 0 ? 0u : 1u);
-                                            mma_f16(d + 64, a0 + 3 * MA, b0 + 2 * MB, idesc, 1u);
+                                            mma_f16(dp, a0, b0 + MB, idesc, j == 0 ? 0u : 1u);
+                                            mma_f16(dp, a0 + MA, b0, idesc, 1u);
+                                            mma_f16(dm, a0 + 2 * MA, b0 + 3 * MB, idesc, j == 0 ? 0u : 1u);
+                                            mma_f16(dm, a0 + 3 * MA, b0 + 2 * MB, idesc, 1u);
                                         } else {
-                                            mma_f16(d, a0, b0, idesc, 1u);
-                                            mma_f16(d + 64, a0 + 2 * MA, b0 + 2 * MB, idesc, 1u);
+                                            mma_f16(dp, a0, b0, idesc, 1u);
+                                            mma_f16(dm, a0 + 2 * MA, b0 + 2 * MB, idesc, 1u);
                                             mma_commit(empty + c % TC_NS);   // stage free when its MMAs are done
                                         }
                                     }
                                 }
                                 it += nj;
-                                mma_commit(acc_full + set);
-                                ++wc;
+                                for (int q = 0; q < nset; ++q) mma_commit(acc_full + set[q]);
+                                wc += nset;
                             }
                         }
                     }
@@ -949,7 +980,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 const int64_t unit = wk.unit;
                 const int lam = (int)(unit / ((int64_t)v.n_rh * v.n_comp));
                 const int *tcb = g.tile_cbase + (size_t)v.le(lam) * (ntl + 1);
-                const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * (2 * TC_B_BYTES);
+                const uint8_t *ua = g.asplit + (size_t)g.unit_cbase[unit] * TC_B_BYTES;
                 const int comp = (int)(unit % v.n_comp), rhi = (int)((unit / v.n_comp) % v.n_rh);
                 const float *uW = v.Wf + v.wlam(lam) + ((size_t)rhi * v.n_bin * v.n_comp + comp) * v.n_size;
                 const int *uex = g.eexp + (size_t)unit * v.n_size;
@@ -982,7 +1013,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                         // weights warp reads them a few items ahead; they were
                         // evicted by the coefficient operand)
                         if (tile + 1 < wk.t1)
-                            bulk_prefetch_l2(ua + (size_t)cb0 * (2 * TC_B_BYTES), (uint32_t)(cb1 - cb0) * (2 * TC_B_BYTES));
+                            bulk_prefetch_l2(ua + (size_t)cb0 * TC_B_BYTES, (uint32_t)(cb1 - cb0) * TC_B_BYTES);
                         if (tile + 2 < wk.t1) {
                             const int tp = tile + 2;
                             const int t0 = tp * TC_INST, nt = min(TC_INST, v.n_size - t0);
@@ -994,7 +1025,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                             for (int b = 0; b < v.n_bin && b < NB; ++b)
                                 pf(uW + (size_t)b * v.n_comp * v.n_size + t0, sizeof(float) * nt);
                         }
-                        for (int h = 0; h < 2 && TC_HALF * h < ntile && ok; ++h) {
+                        // the tile's items (one, or one per half tile with sizes:
+                        // the issuers' rule), each reading every chunk of the tile
+                        const int nitem = nc <= g.win ? 1 : (ntile > TC_HALF ? 2 : 1);
+                        for (int h = 0; h < nitem && ok; ++h) {
                             for (int j = 0; j < nc; ++j) {
                                 const uint32_t c = it++;
                                 const int st = (int)(c % TC_NS);
@@ -1006,7 +1040,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 }
                                 s_chunk[st] = (int)c;
                                 mbar_arrive_expect_tx(full + st, TC_B_BYTES + (j > 0 ? TC_A_BYTES : 0));
-                                bulk_g2s(sS, ua + ((size_t)(base + j) * 2 + h) * TC_B_BYTES, TC_B_BYTES, full + st);
+                                bulk_g2s(sS, ua + (size_t)(base + j) * TC_B_BYTES, TC_B_BYTES, full + st);
                                 if (j > 0) bulk_g2s(sS + TC_B_BYTES, gA + (size_t)j * TC_A_BYTES, TC_A_BYTES, full + st);
                                 tx_used |= 1u << (TC_NS + st);
                                 st_phase = (st_phase & ~(1u << st)) | (((c / TC_NS) & 1u) << st);
@@ -1034,13 +1068,16 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
     } else if (warp == 11) {
         // ================= item info and PSD weights (one warp) =================
         // Item i (the epilogue's order) gets weight-ring slot i % TC_NW: a
-        // header (the tile's accumulation-window count, the unit's largest exponent
-        // E, its (wavelength, RH) index and component) and, per size s of the
-        // half tile (lane s), the bins' weights as pairs (w_b 2^(2 (e_s - E)),
+        // header (the item's accumulation-window count, the unit's largest
+        // exponent E, its (wavelength, RH) index and component; whether the
+        // item is a whole tile, else which half) and, per size s of the tile
+        // (lanes s and s - 32), the bins' weights as pairs (w_b 2^(2 (e_s - E)),
         // the same): the scaled, duplicated form the epilogue's packed FMAs read
         // (E is the unit's largest exponent, so the power is <= 1; below 2^-126
-        // the weight is dropped).  The loads of item i + 1 are issued before the
-        // wait for item i's slot, so their latency overlaps it.
+        // the weight is dropped).  The warp steps over tiles: the loads of tile
+        // t + 1 are issued before the waits for tile t's slots (one, or one per
+        // half tile), so their latency overlaps them, and no load waits for
+        // another's value.
         struct UnitW {
             bool valid;
             int comp, lr, E, t0, t1;
@@ -1066,72 +1103,91 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             u.tcb = g.tile_cbase + (size_t)v.le(lam) * (ntl + 1);
             return u;
         };
-        struct WItem {
-            int cb0, cb1, ex;   // chunk bases of the tile; this lane's size exponent (TC_NO_EX: none)
-            float w[NB];
+        struct WTile {
+            int cb0, cb1, ex[2];   // chunk bases of the tile; sizes lane, 32 + lane: exponents (TC_NO_EX: none)
+            float w[2][NB];
         };
-        auto load_item = [&](const UnitW &u, int tile, int h, WItem &it) {
+        auto load_tile = [&](const UnitW &u, int tile, WTile &it) {
             it.cb0 = ldg_pin_s32(u.tcb + tile);
             it.cb1 = ldg_pin_s32(u.tcb + tile + 1);
-            const int si = tile * TC_INST + TC_HALF * h + lane;
-            it.ex = TC_NO_EX;
 #pragma unroll
-            for (int b = 0; b < NB; ++b) it.w[b] = 0.f;
-            if (si < v.n_size) {
-                it.ex = ldg_pin_s32(u.ex + si);
+            for (int hh = 0; hh < 2; ++hh) {
+                const int si = tile * TC_INST + TC_HALF * hh + lane;
+                it.ex[hh] = TC_NO_EX;
 #pragma unroll
-                for (int b = 0; b < NB; ++b)
-                    if (b < v.n_bin) it.w[b] = ldg_pin_f32(u.Wb + (size_t)b * v.n_comp * v.n_size + si);
+                for (int b = 0; b < NB; ++b) it.w[hh][b] = 0.f;
+                if (si < v.n_size) {
+                    it.ex[hh] = ldg_pin_s32(u.ex + si);
+#pragma unroll
+                    for (int b = 0; b < NB; ++b)
+                        if (b < v.n_bin) it.w[hh][b] = ldg_pin_f32(u.Wb + (size_t)b * v.n_comp * v.n_size + si);
+                }
             }
         };
         bool ok = true;
         uint32_t iw = 0;
-        int kq = 0, h = 0;
+        int kq = 0;
         UnitW u = unit_w(0);
         int tile = u.valid ? u.t0 : 0;
-        // One step: issue the loads of the next item into nxt, wait for the
-        // current item's slot, store it from cur.  Steps alternate the roles
-        // of the two buffers (no register copies: a copy would wait for the
-        // loads it copies).
-        auto step = [&](const WItem &cur, WItem &nxt) {
-            const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
-            int nk = kq, nt = tile, nh = h + 1;
-            if (nh == 2 || TC_HALF * nh >= ntile) {
-                nh = 0;
-                if (++nt == u.t1) ++nk;   // the next work item
-            }
+        // One step: issue the loads of the next tile into nxt, then for each
+        // item of the current tile wait for its slot and store it from cur.
+        // Steps alternate the roles of the two buffers (no register copies: a
+        // copy would wait for the loads it copies).
+        auto step = [&](const WTile &cur, WTile &nxt) {
+            int nk = kq, nt = tile + 1;
+            if (nt == u.t1) ++nk;   // the next work item
             const UnitW un = nk == kq ? u : unit_w(nk);
             if (nk != kq && un.valid) nt = un.t0;
-            if (un.valid) load_item(un, nt, nh, nxt);
-            const uint32_t slot = iw % TC_NW;
-            int go = 1;
-            if (lane == 0 && iw >= TC_NW)
-                go = mbar_wait_or_abort(w_empty + slot, (iw / TC_NW - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit) ? 1 : 0;
-            go = __shfl_sync(0xffffffffu, go, 0);
-            if (!go) {
-                ok = false;
-                return;
+            if (un.valid) load_tile(un, nt, nxt);
+            // the tile's items: the issuers' rule
+            const int nc = cur.cb1 - cur.cb0;
+            const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
+            const bool whole = nc <= g.win;
+            const int nitem = whole ? 1 : (ntile > TC_HALF ? 2 : 1);
+            float4 wq[2][TC_NP(NB)];
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int e = cur.ex[hh] == TC_NO_EX ? -100000 : 2 * (cur.ex[hh] - u.E);
+                const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
+#pragma unroll
+                for (int pp = 0; pp < TC_NP(NB); ++pp) {
+                    const float w0 = 2 * pp < NB ? cur.w[hh][2 * pp] * p2 : 0.f;
+                    const float w1 = 2 * pp + 1 < NB ? cur.w[hh][2 * pp + 1] * p2 : 0.f;
+                    wq[hh][pp] = make_float4(w0, w0, w1, w1);
+                }
             }
-            float *ws = sW + slot * TC_WSLOT_FLOATS;
-            const int e = cur.ex == TC_NO_EX ? -100000 : 2 * (cur.ex - u.E);
-            const float p2 = e < -126 ? 0.f : __int_as_float((e + 127) << 23);
-            float w8[8];
+            for (int hi = 0; hi < nitem; ++hi) {
+                const uint32_t slot = iw % TC_NW;
+                int go = 1;
+                if (lane == 0 && iw >= TC_NW)
+                    go = mbar_wait_or_abort(w_empty + slot, (iw / TC_NW - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit) ? 1
+                                                                                                                      : 0;
+                go = __shfl_sync(0xffffffffu, go, 0);
+                if (!go) {
+                    ok = false;
+                    return;
+                }
+                float *ws = sW + slot * TC_WSLOT_FLOATS(NB);
 #pragma unroll
-            for (int b = 0; b < 8; ++b) w8[b] = b < NB ? cur.w[b] * p2 : 0.f;
-            float4 *dst = (float4 *)(ws + 16 + 16 * lane);
+                for (int hh = 0; hh < 2; ++hh) {
+                    float4 *dst = (float4 *)(ws + 16 + 4 * TC_NP(NB) * (TC_HALF * hh + lane));
 #pragma unroll
-            for (int b = 0; b < 8; b += 2) dst[b / 2] = make_float4(w8[b], w8[b], w8[b + 1], w8[b + 1]);
-            if (lane == 0) *(int4 *)ws = make_int4((cur.cb1 - cur.cb0 + g.win - 1) / g.win, u.E, u.lr, u.comp);
-            __syncwarp();
-            if (lane == 0) mbar_arrive(w_full + slot);
-            ++iw;
+                    for (int pp = 0; pp < TC_NP(NB); ++pp) dst[pp] = wq[hh][pp];
+                }
+                if (lane == 0) {
+                    *(int4 *)ws = make_int4(whole ? 1 : (nc + g.win - 1) / g.win, u.E, u.lr, u.comp);
+                    *(int4 *)(ws + 4) = make_int4(whole ? 1 : 0, hi, 0, 0);
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(w_full + slot);
+                ++iw;
+            }
             u = un;
             kq = nk;
             tile = nt;
-            h = nh;
         };
-        WItem ia, ib;
-        if (u.valid) load_item(u, u.t0, 0, ia);
+        WTile ia, ib;
+        if (u.valid) load_tile(u, u.t0, ia);
         while (ok && u.valid) {
             step(ia, ib);
             if (!ok || !u.valid) break;
@@ -1152,10 +1208,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         //   s33 = (|S+|^2 - |S-|^2)/4, s34 = -Im(S- S+*)/2
         // are applied to the unit's sums.
         const int q = warp & 3, wh = warp >> 2;
-        constexpr int NP = (NB + 1) / 2;   // 16-byte weight loads per size: two bins each
+        constexpr int NP = TC_NP(NB);   // 16-byte weight loads per size: two bins each
         bool ok = true;
-        uint32_t wce[2] = {0u, 0u}, ie = 0;   // windows read per issuer; items
-        int kq = 0, h = 0;
+        uint32_t wce[2] = {0u, 0u}, ie = 0;   // accumulator sets read per issuer; items
+        int kq = 0;
         TcWork cw = tc_work(g, 0, cta, G, nblocks, ntl, n_units);
         int tile = cw.t0;
         // Sums over sizes: acc[e][b] (registers) collects a tile's w_b E_e
@@ -1164,7 +1220,9 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         // access) takes H + acc by an exact two-sum whose rounding error
         // stays in acc as the next tile's start (block-wise compensated
         // summation), so the per-(unit, block) sum H + acc keeps FP32
-        // relative precision whatever the size count.
+        // relative precision whatever the size count.  A thread's sizes are
+        // 16 wh .. 16 wh + 15 of each half tile, in half-tile order, whether
+        // the tile comes as one item or as two.
         f32x2 acc[2][NB];
         ulonglong2 *sh = (ulonglong2 *)sSum + tid;
 #pragma unroll
@@ -1172,111 +1230,150 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             acc[0][b] = acc[1][b] = 0ull;
             sh[b * TC_EPI_THREADS] = make_ulonglong2(0ull, 0ull);
         }
+        // lane 0 waits, the warp follows its answer
+        auto warp_wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+            int go = 1;
+            if (lane == 0) go = mbar_wait_or_abort(bar, parity, s_abort, TC_EPI_SLEEP_NS, g.wait_limit) ? 1 : 0;
+            return __shfl_sync(0xffffffffu, go, 0) != 0;
+        };
         while (ok && cw.valid) {
             const int ntile = min(TC_INST, v.n_size - tile * TC_INST);
             const int ab = cw.ab;
             const bool active = TC_ABLK * ab + 32 * q < v.n_ang;   // this warp has angles in the block
-            // the next item; wend: this item ends the work item
-            int nk = kq, nt = tile, nh = h + 1;
-            bool wend = false;
-            if (nh == 2 || TC_HALF * nh >= ntile) {
-                nh = 0;
-                if (++nt == cw.t1) {
-                    wend = true;
-                    ++nk;
-                }
-            }
             // the item's slot of the weight ring
             const uint32_t wsl = ie % TC_NW;
-            {
-                int go = 1;
-                if (lane == 0)
-                    go = mbar_wait_or_abort(w_full + wsl, (ie / TC_NW) & 1u, s_abort, TC_EPI_SLEEP_NS, g.wait_limit) ? 1 : 0;
-                go = __shfl_sync(0xffffffffu, go, 0);
-                if (!go) {
-                    ok = false;
-                    break;
-                }
+            if (!warp_wait(w_full + wsl, (ie / TC_NW) & 1u)) {
+                ok = false;
+                break;
             }
-            const float *ws = sW + wsl * TC_WSLOT_FLOATS;
-            const int4 hdr = *(const int4 *)ws;   // windows, E, (wavelength, RH) index, component
-            const int nwin = hdr.x;
-            const float *wb = ws + 16 + 16 * 16 * wh;   // this warp's 16 sizes
-            // window sums of S+ and S- (this lane's angle, 16 sizes x Re/Im);
-            // later windows are added in pieces of 4 sizes (fewer live
-            // registers)
-            float rp[32], rm[32];
+            const float *ws = sW + wsl * TC_WSLOT_FLOATS(NB);
+            const int4 hdr = *(const int4 *)ws;         // windows, E, (wavelength, RH) index, component
+            const int4 hd2 = *(const int4 *)(ws + 4);   // whole tile, else the half
+            const bool whole = hd2.x != 0;
+            const int hcur = hd2.y;
+            // the next item; tend: this item ends its tile, wend: the work item
+            int nk = kq, nt = tile;
+            const bool tend = whole || hcur == 1 || TC_HALF * (hcur + 1) >= ntile;
+            bool wend = false;
+            if (tend && ++nt == cw.t1) {
+                wend = true;
+                ++nk;
+            }
             const uint32_t ip = ie & 1u;   // the item's issuer
-            for (int w = 0; w < nwin; ++w) {
-                const uint32_t wi = ip ? wce[1] : wce[0];
-                const uint32_t set = 2 * ip + (wi & 1u), use = wi >> 1;
-                int go = 1;
-                if (lane == 0)
-                    go = mbar_wait_or_abort(acc_full + set, use & 1u, s_abort, TC_EPI_SLEEP_NS, g.wait_limit) ? 1 : 0;
-                go = __shfl_sync(0xffffffffu, go, 0);
-                if (!go) {
-                    ok = false;
-                    break;
+            const uint32_t lanes = tmem + ((uint32_t)(32 * q) << 16);
+            // passes of 16 sizes: a whole tile's two halves (one window: S+ of the
+            // 64 sizes in one accumulator set, S- in the issuer's other), or the
+            // half tile's windows
+            const uint32_t wi0 = ip ? wce[1] : wce[0];
+            const uint32_t sp = 2 * ip + (wi0 & 1u), sm = 2 * ip + ((wi0 + 1) & 1u);
+            const int npass = whole ? 2 : 1;
+#pragma unroll 1
+            for (int hh = 0; hh < npass; ++hh) {
+                float rp[32], rm[32];
+                bool use;
+                int half;
+                if (whole) {
+                    if (hh == 0) {
+                        if (!warp_wait(acc_full + sp, (wi0 >> 1) & 1u) ||
+                            !warp_wait(acc_full + sm, ((wi0 + 1) >> 1) & 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                    }
+                    half = hh;
+                    use = active && TC_HALF * hh < ntile;
+                    if (use) {
+                        const uint32_t col = 64 * hh + 32 * wh;
+                        tmem_ld32x2(lanes + sp * 128 + col, lanes + sm * 128 + col, rp, rm);
+                    }
+                    if (hh == 1) {   // both sets read
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) {
+                            mbar_arrive(acc_empty + sp);
+                            mbar_arrive(acc_empty + sm);
+                        }
+                        if (ip) wce[1] += 2;
+                        else wce[0] += 2;
+                    }
+                } else {
+                    // window sums of S+ and S- (this lane's angle, 16 sizes x
+                    // Re/Im); later windows are added in pieces of 4 sizes (fewer
+                    // live registers)
+                    const int nwin = hdr.x;
+                    for (int w = 0; w < nwin; ++w) {
+                        const uint32_t wi = ip ? wce[1] : wce[0];
+                        const uint32_t set = 2 * ip + (wi & 1u), su = wi >> 1;
+                        if (!warp_wait(acc_full + set, su & 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        if (active) {
+                            const uint32_t ta = lanes + set * 128 + 32 * wh;
+                            if (w == 0) {
+                                tmem_ld32x2(ta, ta + 64, rp, rm);
+                            } else {
+#pragma unroll
+                                for (int hf = 0; hf < 4; ++hf) {
+                                    float t[8], u[8];
+                                    tmem_ld8x2(ta + 8 * hf, ta + 64 + 8 * hf, t, u);
+#pragma unroll
+                                    for (int i = 0; i < 8; ++i) {
+                                        rp[8 * hf + i] += t[i];
+                                        rm[8 * hf + i] += u[i];
+                                    }
+                                }
+                            }
+                        }
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(acc_empty + set);
+                        if (ip) ++wce[1];
+                        else ++wce[0];
+                    }
+                    half = hcur;
+                    use = active && nwin > 0;
                 }
-                tc_fence_after();
-                if (active) {
-                    const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + set * 128 + 32 * wh;
-                    if (w == 0) {
-                        tmem_ld32x2(ta, ta + 64, rp, rm);
-                    } else {
+                if (!ok) break;
+                if (use) {
+                    const float *wb = ws + 16 + 4 * NP * (TC_HALF * half + 16 * wh);   // this thread's 16 sizes
+                    // per group of 8 sizes: the pairs first (independent work for the
+                    // scheduler), then the weighted sums; rp/rm die as E0/E1 are formed
 #pragma unroll
-                        for (int hf = 0; hf < 4; ++hf) {
-                            float t[8], u[8];
-                            tmem_ld8x2(ta + 8 * hf, ta + 64 + 8 * hf, t, u);
+                    for (int sg = 0; sg < 16; sg += 8) {
+                        f32x2 E0[8], E1[8];
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) {
-                                rp[8 * hf + i] += t[i];
-                                rm[8 * hf + i] += u[i];
+                        for (int s = 0; s < 8; ++s) {
+                            const float pr = rp[2 * (sg + s)], pi = rp[2 * (sg + s) + 1], mr = rm[2 * (sg + s)],
+                                        mi = rm[2 * (sg + s) + 1];
+                            E0[s] = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
+                            E1[s] = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
+                        }
+#pragma unroll
+                        for (int s = 0; s < 8; ++s) {
+                            const f32x2 e0 = E0[s], e1 = E1[s];
+                            const ulonglong2 *wp = (const ulonglong2 *)(wb + 4 * NP * (sg + s));
+#pragma unroll
+                            for (int p = 0; p < NP; ++p) {
+                                const ulonglong2 w2 = wp[p];   // (w_2p, w_2p), (w_2p+1, w_2p+1)
+                                acc[0][2 * p] = f2_fma(w2.x, e0, acc[0][2 * p]);
+                                acc[1][2 * p] = f2_fma(w2.x, e1, acc[1][2 * p]);
+                                if (2 * p + 1 < NB) {
+                                    acc[0][2 * p + 1] = f2_fma(w2.y, e0, acc[0][2 * p + 1]);
+                                    acc[1][2 * p + 1] = f2_fma(w2.y, e1, acc[1][2 * p + 1]);
+                                }
                             }
                         }
                     }
                 }
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(acc_empty + set);
-                if (ip) ++wce[1];
-                else ++wce[0];
             }
             if (!ok) break;
-            if (active) {
-                // per group of 8 sizes: the pairs first (independent work for the
-                // scheduler), then the weighted sums; rp/rm die as E0/E1 are formed
-#pragma unroll
-                for (int sg = 0; sg < 16; sg += 8) {
-                    f32x2 E0[8], E1[8];
-#pragma unroll
-                    for (int s = 0; s < 8; ++s) {
-                        const float pr = rp[2 * (sg + s)], pi = rp[2 * (sg + s) + 1], mr = rm[2 * (sg + s)],
-                                    mi = rm[2 * (sg + s) + 1];
-                        E0[s] = f2_pack(fmaf(pr, pr, pi * pi), fmaf(mr, mr, mi * mi));
-                        E1[s] = f2_pack(fmaf(pr, mr, pi * mi), fmaf(mr, pi, -(mi * pr)));
-                    }
-#pragma unroll
-                    for (int s = 0; s < 8; ++s) {
-                        const f32x2 e0 = E0[s], e1 = E1[s];
-                        const ulonglong2 *wp = (const ulonglong2 *)(wb + 16 * (sg + s));
-#pragma unroll
-                        for (int p = 0; p < NP; ++p) {
-                            const ulonglong2 w2 = wp[p];   // (w_2p, w_2p), (w_2p+1, w_2p+1)
-                            acc[0][2 * p] = f2_fma(w2.x, e0, acc[0][2 * p]);
-                            acc[1][2 * p] = f2_fma(w2.x, e1, acc[1][2 * p]);
-                            if (2 * p + 1 < NB) {
-                                acc[0][2 * p + 1] = f2_fma(w2.y, e0, acc[0][2 * p + 1]);
-                                acc[1][2 * p + 1] = f2_fma(w2.y, e1, acc[1][2 * p + 1]);
-                            }
-                        }
-                    }
-                }
-            }
             // the slot is read (every warp, active or not, waited for it first)
             __syncwarp();
             if (lane == 0) mbar_arrive(w_empty + wsl);
-            if (nh == 0) {
+            if (tend) {
                 // end of a tile: H += acc exactly rounded, the error stays in acc
                 auto two_sum = [](f32x2 &hi, f32x2 &a) {
                     const f32x2 sum = f2_add(hi, a);
@@ -1354,7 +1451,6 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 nt = cw.t0;
             }
             tile = nt;
-            h = nh;
             ++ie;
         }
         if (!ok && lane == 0) {

@@ -200,7 +200,7 @@ def work_counts(spec):
     # tensor-core tiles: 64 sizes, orders in chunks of 16 up to the tile's
     # largest nmax, per unit
     sum_kc16 = 0
-    sum_kc16_half = 0   # the same per half tile of 32 sizes (the contraction's MMA N = 64)
+    sum_kc16_half = 0   # the same per half tile of 32 sizes (MMA N = 64; a whole tile runs both halves)
     tsize = np.minimum(64, grid.size - np.arange(0, grid.size, 64))
     halves = np.where(tsize > 32, 2, 1)
     for li in range(nl):
