@@ -637,7 +637,7 @@ __global__ void k_tab_bt_f16(int nang, int n_pad, int k_pad, int nmax, const dou
 //   warps 8, 10 MMA issue (one thread each; items alternate between them)
 //   warp 9      producer (one thread): bulk copies of the coefficient chunks
 //               of a tile (split_rows) and of the angle functions of orders
-//               > 16 into a TC_NS-stage shared-memory ring
+//               > 16 into a TC_NS(NB)-stage shared-memory ring
 //   warp 11     weights: per tile the chunk count, the unit's constants and
 //               the PSD weights, scaled and paired for the epilogue's packed
 //               FMAs, into a TC_NW-slot shared-memory ring (the epilogue
@@ -679,13 +679,17 @@ struct TcArgs {
 
 // ring stages of a tile's chunk (coefficients of 64 sizes, angle functions
 // of orders > 16): the copies of a stage's next chunk wait for its MMAs, so
-// the ring's depth bounds the chunks in flight
-#define TC_NS 4
+// the ring's depth bounds the chunks in flight.  Sulfate-like table (5
+// bins): 4 stages 2.79 ms; 5 stages (225 KB of shared memory per block,
+// room for up to 5 bins) 2.73 ms, but the pipelined tables of the batch API
+// then took 6.85 instead of 4.72 ms each: the next plan's setup kernels no
+// longer ran beside the contraction.  Kept at 4 for every bin count.
+#define TC_NS(NB) 4
 // longest accumulation window (chunks): the windows the accuracy of the FP32
 // accumulation was checked with (2-4 keep it near 2e-7); a window's chunks
 // sit in the ring together
 #define TC_WIN_MAX 4
-static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
+static_assert(TC_WIN_MAX <= TC_NS(8), "a window's chunks must fit the ring");
 #define TC_NSETS 4                                     // TMEM accumulator sets of 128 columns
 // resident angle-function chunks (angle blocks; tables of more than 256
 // angles reload one slot per (unit, block))
@@ -699,9 +703,10 @@ static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
 // register bound of 12 warps: three warps on an SM sub-partition fit its
 // 16K registers at 168 each
 #define TC_REG_BOUND_THREADS 384
-// weight-ring slots (items); measured on the sulfate-like table with 2, 4,
-// 6, 8 and 10 slots: 3.23, 3.10, 3.03, 3.06, 3.09 ms
-#define TC_NW 6
+// weight-ring slots (items); with half-tile items only, measured on the
+// sulfate-like table with 2, 4, 6, 8 and 10 slots: 3.23, 3.10, 3.03, 3.06,
+// 3.09 ms; with whole-tile items 4 and 6 slots measure the same (2.86 ms)
+#define TC_NW 4
 // mbarriers (2 TC_NS + 2 + 2 TC_NSETS + 1 + 2 TC_NW), the TMEM address, the
 // abort flag and the stages' chunk tags
 #define TC_CTRL_BYTES 512
@@ -709,7 +714,7 @@ static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
 #define TC_WSLOT_FLOATS(NB) (16 + TC_INST * 4 * TC_NP(NB))   // header + 64 sizes x bin pairs x (w, w, w', w')
 #define TC_SUM_FLOATS(NB) (4 * (NB) * TC_EPI_THREADS)  // running sums [bin][thread] of (E0 pair, E1 pair)
 #define TC_SMEM_BYTES(NB)                                                                                  \
-    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS * TC_STAGE_BYTES + TC_NW * TC_WSLOT_FLOATS(NB) * 4 +                 \
+    (TC_B0_SLOTS(NB) * TC_A_BYTES + TC_NS(NB) * TC_STAGE_BYTES + TC_NW * TC_WSLOT_FLOATS(NB) * 4 +             \
      TC_SUM_FLOATS(NB) * 4 + TC_CTRL_BYTES)
 #define TC_NO_EX (-0x40000000)                         // no size: its weights are dropped
 #define TC_SLEEP_NS 32                                 // back-off of the MMA and producer waits
@@ -722,8 +727,11 @@ static_assert(TC_WIN_MAX <= TC_NS, "a window's chunks must fit the ring");
 #define TC_EPI_SLEEP_NS 128
 
 static_assert(TC_NSETS * 128 <= 512, "TMEM columns");
-static_assert(8 * (2 * TC_NS + 2 + 2 * TC_NSETS + 1 + 2 * TC_NW) + 4 + 8 + 4 * TC_NS <= TC_CTRL_BYTES, "control block");
-static_assert(TC_SMEM_BYTES(5) <= 227 * 1024 && TC_SMEM_BYTES(8) <= 227 * 1024, "shared memory");
+static_assert(8 * (2 * TC_NS(1) + 2 + 2 * TC_NSETS + 1 + 2 * TC_NW) + 4 + 8 + 4 * TC_NS(1) <= TC_CTRL_BYTES, "control block");
+static_assert(TC_SMEM_BYTES(1) <= 227 * 1024 && TC_SMEM_BYTES(2) <= 227 * 1024 && TC_SMEM_BYTES(3) <= 227 * 1024 &&
+                  TC_SMEM_BYTES(4) <= 227 * 1024 && TC_SMEM_BYTES(5) <= 227 * 1024 && TC_SMEM_BYTES(6) <= 227 * 1024 &&
+                  TC_SMEM_BYTES(7) <= 227 * 1024 && TC_SMEM_BYTES(8) <= 227 * 1024,
+              "shared memory");
 
 // k-th unit of CTA `cta` among G CTAs: units in decreasing-work order,
 // dealt in a snake (c, then G-1-c) so that every CTA gets a similar mix.
@@ -767,13 +775,14 @@ template <int NB>
 __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
+    constexpr int NS = TC_NS(NB);                                   // ring stages
     uint8_t *sB0 = smem;                                            // resident angle chunks, orders 1..16
-    uint8_t *sStage = sB0 + TC_B0_SLOTS(NB) * TC_A_BYTES;           // TC_NS x (coeff 16 KB | angles 16 KB)
-    float *sW = (float *)(sStage + TC_NS * TC_STAGE_BYTES);         // weight ring [TC_NW][TC_WSLOT_FLOATS(NB)]
+    uint8_t *sStage = sB0 + TC_B0_SLOTS(NB) * TC_A_BYTES;           // NS x (coeff 16 KB | angles 16 KB)
+    float *sW = (float *)(sStage + NS * TC_STAGE_BYTES);         // weight ring [TC_NW][TC_WSLOT_FLOATS(NB)]
     float *sSum = sW + TC_NW * TC_WSLOT_FLOATS(NB);                 // per-(unit, block) running sums
     uint64_t *bars = (uint64_t *)(sSum + TC_SUM_FLOATS(NB));
-    uint64_t *full = bars, *empty = bars + TC_NS;
-    uint64_t *b0_full = bars + 2 * TC_NS, *b0_empty = b0_full + 1;
+    uint64_t *full = bars, *empty = bars + NS;
+    uint64_t *b0_full = bars + 2 * NS, *b0_empty = b0_full + 1;
     uint64_t *acc_full = b0_full + 2, *acc_empty = acc_full + TC_NSETS, *drain = acc_empty + TC_NSETS;
     uint64_t *w_full = drain + 1, *w_empty = w_full + TC_NW;
     uint32_t *s_tmem = (uint32_t *)(w_empty + TC_NW);
@@ -794,7 +803,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
     const bool reload = nblocks > TC_B0_SLOTS(NB);   // one resident slot, reloaded per (unit, block)
     if (warp == 0) tmem_alloc(s_tmem, 512);
     if (tid == 0) {
-        for (int i = 0; i < TC_NS; ++i) {
+        for (int i = 0; i < NS; ++i) {
             mbar_init(full + i, 1);    // the producer's arrival with the copies' bytes
             mbar_init(empty + i, 1);   // tcgen05.commit
         }
@@ -811,7 +820,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         }
         fence_mbar_init();
         *s_abort = 0;
-        for (int i = 0; i < TC_NS; ++i) s_chunk[i] = -1;
+        for (int i = 0; i < NS; ++i) s_chunk[i] = -1;
     }
     tc_fence_before();
     __syncthreads();
@@ -899,7 +908,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 }
                                 if (!ok) break;
                                 for (int j = 0; j < nj && ok; ++j) {
-                                    const uint32_t c = it + j, st = c % TC_NS, par = (c / TC_NS) & 1u;
+                                    const uint32_t c = it + j, st = c % NS, par = (c / NS) & 1u;
                                     ok = false;
                                     for (uint32_t tr = 0; tr < g.wait_limit; ++tr) {
                                         if (s_chunk[st] == (int)c) {
@@ -922,7 +931,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 for (int pass = 0; pass < 2; ++pass) {
                                     for (int j = 0; j < nj; ++j) {
                                         const uint32_t c = it + j;
-                                        const uint32_t sB = sStage0 + (c % TC_NS) * TC_STAGE_BYTES;
+                                        const uint32_t sB = sStage0 + (c % NS) * TC_STAGE_BYTES;
                                         const uint32_t sA = (w0 + j) == 0 ? aB0 : sB + TC_B_BYTES;
                                         // descriptors: constant LBO/SBO fields + start address / 16;
                                         // matrix m of an operand starts m x its matrix size later
@@ -936,7 +945,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                         } else {
                                             mma_f16(dp, a0, b0, idesc, 1u);
                                             mma_f16(dm, a0 + 2 * MA, b0 + 2 * MB, idesc, 1u);
-                                            mma_commit(empty + c % TC_NS);   // stage free when its MMAs are done
+                                            mma_commit(empty + c % NS);   // stage free when its MMAs are done
                                         }
                                     }
                                 }
@@ -962,7 +971,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
         if (lane == 0) {
             uint32_t it = 0, b0_loads = 0;
             // the phase of the latest bulk copy into each ring stage (bit
-            // TC_NS + st: stage st has one) and into the resident slot, so
+            // NS + st: stage st has one) and into the resident slot, so
             // that an abort can wait for every copy still in flight
             uint32_t st_phase = 0, tx_used = 0, b0_phase = 0;
             bool ok = true;
@@ -971,7 +980,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                 for (int b = 0; b < nblocks; ++b)
                     bulk_g2s(sB0 + b * TC_A_BYTES, (const uint8_t *)g.bt + (size_t)b * nkc * TC_A_BYTES, TC_A_BYTES,
                              b0_full);
-                tx_used |= 1u << (2 * TC_NS);
+                tx_used |= 1u << (2 * NS);
                 b0_phase = 0;
             }
             for (int k = 0; ok; ++k) {
@@ -995,7 +1004,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                         }
                         mbar_arrive_expect_tx(b0_full, TC_A_BYTES);
                         bulk_g2s(sB0, gA, TC_A_BYTES, b0_full);
-                        tx_used |= 1u << (2 * TC_NS);
+                        tx_used |= 1u << (2 * NS);
                         b0_phase = b0_loads & 1u;
                         ++b0_loads;
                     }
@@ -1031,10 +1040,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                         for (int h = 0; h < nitem && ok; ++h) {
                             for (int j = 0; j < nc; ++j) {
                                 const uint32_t c = it++;
-                                const int st = (int)(c % TC_NS);
+                                const int st = (int)(c % NS);
                                 uint8_t *sS = sStage + st * TC_STAGE_BYTES;
-                                if (c >= TC_NS &&
-                                    !mbar_wait_or_abort(empty + st, (c / TC_NS - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit)) {
+                                if (c >= NS &&
+                                    !mbar_wait_or_abort(empty + st, (c / NS - 1) & 1u, s_abort, TC_SLEEP_NS, g.wait_limit)) {
                                     ok = false;
                                     break;
                                 }
@@ -1042,8 +1051,8 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                                 mbar_arrive_expect_tx(full + st, TC_B_BYTES + (j > 0 ? TC_A_BYTES : 0));
                                 bulk_g2s(sS, ua + (size_t)(base + j) * TC_B_BYTES, TC_B_BYTES, full + st);
                                 if (j > 0) bulk_g2s(sS + TC_B_BYTES, gA + (size_t)j * TC_A_BYTES, TC_A_BYTES, full + st);
-                                tx_used |= 1u << (TC_NS + st);
-                                st_phase = (st_phase & ~(1u << st)) | (((c / TC_NS) & 1u) << st);
+                                tx_used |= 1u << (NS + st);
+                                st_phase = (st_phase & ~(1u << st)) | (((c / NS) & 1u) << st);
                             }
                         }
                     }
@@ -1058,10 +1067,10 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
             // the latest phase of every stage that received one (an earlier
             // phase of a stage completed before its next copy was issued); in
             // a run without timeouts these have all completed already
-            for (int st = 0; st < TC_NS; ++st)
-                if ((tx_used >> (TC_NS + st)) & 1u && !mbar_wait(full + st, (st_phase >> st) & 1u, 1u << 20))
+            for (int st = 0; st < NS; ++st)
+                if ((tx_used >> (NS + st)) & 1u && !mbar_wait(full + st, (st_phase >> st) & 1u, 1u << 20))
                     atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
-            if ((tx_used >> (2 * TC_NS)) & 1u && !mbar_wait(b0_full, b0_phase, 1u << 20))
+            if ((tx_used >> (2 * NS)) & 1u && !mbar_wait(b0_full, b0_phase, 1u << 20))
                 atomicOr(g.flags, GBMIE_FLAG_TIMEOUT);
         }
         __syncwarp();
@@ -1270,7 +1279,7 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
 #pragma unroll 1
             for (int hh = 0; hh < npass; ++hh) {
                 float rp[32], rm[32];
-                bool use;
+                bool use, pend = false, rel = false;
                 int half;
                 if (whole) {
                     if (hh == 0) {
@@ -1284,19 +1293,28 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     half = hh;
                     use = active && TC_HALF * hh < ntile;
                     if (use) {
+                        // sizes 0-7 of the pass now, 8-15 in flight while 0-7 are summed
                         const uint32_t col = 64 * hh + 32 * wh;
-                        tmem_ld32x2(lanes + sp * 128 + col, lanes + sm * 128 + col, rp, rm);
+                        tmem_ld8x2(lanes + sp * 128 + col, lanes + sm * 128 + col, rp, rm);
+                        tmem_ld8x2(lanes + sp * 128 + col + 8, lanes + sm * 128 + col + 8, rp + 8, rm + 8);
+                        tmem_ld16x2_nowait(lanes + sp * 128 + col + 16, lanes + sm * 128 + col + 16, rp + 16, rm + 16);
+                        pend = true;
                     }
-                    if (hh == 1) {   // both sets read
+                    if (hh == 1 && !use) {   // both sets read
                         tc_fence_before();
                         __syncwarp();
                         if (lane == 0) {
                             mbar_arrive(acc_empty + sp);
                             mbar_arrive(acc_empty + sm);
                         }
+                    }
+                    if (hh == 1) {
                         if (ip) wce[1] += 2;
                         else wce[0] += 2;
                     }
+                    // a whole tile's sets are released once the last pass's
+                    // in-flight half has landed (in the sums below)
+                    rel = hh == 1 && use;
                 } else {
                     // window sums of S+ and S- (this lane's angle, 16 sizes x
                     // Re/Im); later windows are added in pieces of 4 sizes (fewer
@@ -1343,6 +1361,17 @@ __global__ void __launch_bounds__(TC_REG_BOUND_THREADS, 1) k_tab_s12_tc(TcArgs g
                     // scheduler), then the weighted sums; rp/rm die as E0/E1 are formed
 #pragma unroll
                     for (int sg = 0; sg < 16; sg += 8) {
+                        if (sg == 8 && pend) {
+                            tmem_wait_tie(rp + 16, rm + 16);
+                            if (rel) {   // both sets read
+                                tc_fence_before();
+                                __syncwarp();
+                                if (lane == 0) {
+                                    mbar_arrive(acc_empty + sp);
+                                    mbar_arrive(acc_empty + sm);
+                                }
+                            }
+                        }
                         f32x2 E0[8], E1[8];
 #pragma unroll
                         for (int s = 0; s < 8; ++s) {
