@@ -353,21 +353,24 @@ __device__ __forceinline__ void split_rows(const TabView &v, int i, int ex, int 
             st_global_32b(blk + 2 * TC_MAT_B + o0, *(uint4 *)ch[2], *(uint4 *)ch[3]);
             st_global_32b(blk + 3 * TC_MAT_B + o0, *(uint4 *)cl[2], *(uint4 *)cl[3]);
         }
-    // the last size of a partial tile also zeroes the rows of the sizes the
-    // tile lacks (their PSD weights are zero, but 0 x NaN would not be): a
-    // whole-tile MMA reads all 128 rows
+    // the sizes of a partial tile also zero the rows of the sizes the tile
+    // lacks (their PSD weights are zero, but 0 x NaN would not be): a
+    // whole-tile MMA reads all 128 rows.  Size ia takes the absent sizes ia +
+    // ntile, ia + 2 ntile, ... (one 32-byte store per row pair, as above)
     const int ntile = min(64, v.n_size - 64 * tile);
-    if (ia == ntile - 1 && ntile < 64) {
+    if (ntile < 64) {
         const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-        for (int j = 0; j < nc; ++j)
-            for (int r = 2 * ntile; r < 128; ++r)
+        for (int a = ia + ntile; a < 64; a += ntile) {
+            const int r = 2 * a;
+            for (int j = 0; j < nc; ++j)
 #pragma unroll
                 for (int kg = 0; kg < 2; ++kg) {
                     const uint32_t o = kg * 2048 + (r >> 3) * 128 + (r & 7) * 16;
                     uint8_t *blk = dst + (size_t)j * 16384;
 #pragma unroll
-                    for (int mtx = 0; mtx < 4; ++mtx) *(uint4 *)(blk + mtx * TC_MAT_B + o) = z;
+                    for (int mtx = 0; mtx < 4; ++mtx) st_global_32b(blk + mtx * TC_MAT_B + o, z, z);
                 }
+        }
     }
 }
 
