@@ -488,7 +488,11 @@ __global__ void k_tab_trapz(int nang, const double *__restrict__ theta, double *
 // Phase normalisation and the per-entry outputs (dointegration.py:950-1001).
 // The entry's Mueller sums are first formed from the angular kernels'
 // partial sums: over components c, then slots s < used, in that order (a
-// fixed order, so that repeated runs give the same bits), into pacc.
+// fixed order, so that repeated runs give the same bits).  APT > 0: up to
+// APT angles per thread (n_ang <= 64 APT), the sums in registers with every
+// slot's loads of the thread issued together; APT = 0: any angle count, the
+// sums through pacc.
+template <int APT>
 __global__ void __launch_bounds__(64) k_tab_finalize(TabView v, gbmie_table_out out, int used)
 {
     const int blk = blockIdx.x;   // (lam * n_rh + rh) * n_bin + bin
@@ -502,24 +506,64 @@ __global__ void __launch_bounds__(64) k_tab_finalize(TabView v, gbmie_table_out 
     // trapz(p11 sin(theta), theta) with the precomputed weights
     double tr[1] = {0.0};
     const int nsrc = v.n_comp * v.n_slots;
-    for (int a = threadIdx.x; a < nang; a += blockDim.x) {
-        for (int k = 0; k < 4; ++k) {
-            const double *q = src + k * nang + a;
-            double sum = 0.0;
+    double R[APT > 0 ? APT : 1][4];   // APT > 0: the sums of angle threadIdx.x + 64 i
+    if (APT > 0) {
+#pragma unroll
+        for (int i = 0; i < (APT > 0 ? APT : 1); ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) R[i][k] = 0.0;
 #pragma unroll 1
-            for (int c = 0; c < nsrc; c += v.n_slots)
+        for (int c = 0; c < nsrc; c += v.n_slots)
+#pragma unroll 1
+            for (int sl = 0; sl < used; ++sl) {
+                const double *__restrict__ q = src + (size_t)(c + sl) * plane + threadIdx.x;
+#pragma unroll
+                for (int i = 0; i < (APT > 0 ? APT : 1); ++i)
+                    if (threadIdx.x + 64 * i < nang)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) R[i][k] += __ldg(q + k * nang + 64 * i);
+            }
+#pragma unroll
+        for (int i = 0; i < (APT > 0 ? APT : 1); ++i)
+            if (threadIdx.x + 64 * i < nang) tr[0] += R[i][0] * v.tw[threadIdx.x + 64 * i];
+    } else {
+        for (int a = threadIdx.x; a < nang; a += blockDim.x) {
+            for (int k = 0; k < 4; ++k) {
+                const double *q = src + k * nang + a;
+                double sum = 0.0;
+#pragma unroll 1
+                for (int c = 0; c < nsrc; c += v.n_slots)
 #pragma unroll 8
-                for (int sl = 0; sl < used; ++sl) sum += q[(size_t)(c + sl) * plane];   // loads issued ahead, adds in order
-            P[k * nang + a] = sum;   // read back below by this thread only
+                    for (int sl = 0; sl < used; ++sl) sum += q[(size_t)(c + sl) * plane];   // loads issued ahead, adds in order
+                P[k * nang + a] = sum;   // read back below by this thread only
+            }
+            tr[0] += P[a] * v.tw[a];
         }
-        tr[0] += P[a] * v.tw[a];
     }
     block_sum<1>(tr);
     const double scale = 2.0 / tr[0];   // p11n / p11, the same at every angle
     const size_t e = ((size_t)bin * v.n_lambda + lam) * v.n_rh + rh;   // output entry
     double *ph = out.phase + e * 6 * nang;
-    for (int a = threadIdx.x; a < nang; a += blockDim.x) {
-        const double p11 = P[a], p12 = P[nang + a], p33 = P[2 * nang + a], p34 = P[3 * nang + a];
+    for (int a = threadIdx.x, i = 0; a < nang; a += blockDim.x, ++i) {
+        double p11, p12, p33, p34;
+        if (APT > 0) {
+            // i < APT here (n_ang <= 64 APT); the index is a compile-time one
+            // after unrolling the selection
+            p11 = p12 = p33 = p34 = 0.0;
+#pragma unroll
+            for (int j = 0; j < (APT > 0 ? APT : 1); ++j)
+                if (j == i) {
+                    p11 = R[j][0];
+                    p12 = R[j][1];
+                    p33 = R[j][2];
+                    p34 = R[j][3];
+                }
+        } else {
+            p11 = P[a];
+            p12 = P[nang + a];
+            p33 = P[2 * nang + a];
+            p34 = P[3 * nang + a];
+        }
         const double p11n = p11 * scale;
         const double p12n = p12 * scale, p22n = p11n;
         const double p33n = p33 * scale, p34n = p34 * scale;
@@ -1175,7 +1219,12 @@ static int launch_table_tail(gbmie_ctx *ctx, gbmie_table_plan *p, TabView &v, co
     k_tab_trapz<<<1, 256, 0, st>>>(d.n_ang, d.theta, v.tw);
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_trapz"));
     ctx_pre_launch(ctx);
-    k_tab_finalize<<<(unsigned)p->n_entries, 64, 0, st>>>(v, *out, p->slots_used);   // 2-3 angles per thread
+    {
+        const int apt = (d.n_ang + 63) / 64;   // angles per thread of 64-thread blocks
+        auto fin = apt <= 1 ? k_tab_finalize<1> : apt == 2 ? k_tab_finalize<2> : apt == 3 ? k_tab_finalize<3>
+                 : apt == 4 ? k_tab_finalize<4> : k_tab_finalize<0>;
+        fin<<<(unsigned)p->n_entries, 64, 0, st>>>(v, *out, p->slots_used);
+    }
     GBMIE_TRY(ctx_check_launch(ctx, "k_tab_finalize"));
     if (p->has_gsf) {
         GsfMap map = {{0, 2, 3, 5, 1, 4}, {0, 4, 2, 5, 1, 3}};
