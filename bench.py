@@ -53,7 +53,7 @@ REF_RH = [0, 7, 14, 21, 28, 35]
 # profiles/k_tab_coeffs_mixed_sulfate12.md), scaled to a run by its units
 # (sulfate table only)
 NCU_BYTES_PER_UNIT = {"k_tab_coeffs_mixed": (34.952192e6 + 371.037952e6) / 432,
-                      "k_tab_s12_tc": (323.385344e6 + 16.973056e6) / 432}
+                      "k_tab_s12_tc": (323.177472e6 + 16.813312e6) / 432}
 SCAT = ["p11", "p12", "p22", "p33", "p34", "p44"]
 SCALARS = ["qext", "qsca", "qb", "g", "csca", "cext", "ssa", "bsca", "bext", "bbck", "refreal", "refimag",
            "lidar_ratio"]

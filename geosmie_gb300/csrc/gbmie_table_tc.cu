@@ -683,11 +683,11 @@ struct TcArgs {
 // ring stages of a tile's chunk (coefficients of 64 sizes, angle functions
 // of orders > 16): the copies of a stage's next chunk wait for its MMAs, so
 // the ring's depth bounds the chunks in flight.  Sulfate-like table (5
-// bins): 4 stages 2.79 ms; 5 stages (225 KB of shared memory per block,
-// room for up to 5 bins) 2.73 ms, but the pipelined tables of the batch API
-// then took 6.85 instead of 4.72 ms each: the next plan's setup kernels no
-// longer ran beside the contraction.  Kept at 4 for every bin count.
-#define TC_NS(NB) 4
+// bins), the same GB300 in one run: 4 stages 2.79-2.80 ms (table 4.43 ms,
+// e2e 905-916M instance-evals/s), 5 stages 2.73 ms (table 4.36 ms, e2e 926M);
+// tables of more bins keep 4 (their running sums and weights leave no room
+// for a fifth)
+#define TC_NS(NB) ((NB) <= 5 ? 5 : 4)
 // longest accumulation window (chunks): the windows the accuracy of the FP32
 // accumulation was checked with (2-4 keep it near 2e-7); a window's chunks
 // sit in the ring together
