@@ -401,6 +401,33 @@ def test_many_bins_and_angle_blocks_gpu(nbin, nang):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("nbin,nang", [(5, 129), (2, 256), (3, 160)])
+def test_second_angle_block_edges_gpu(nbin, nang):
+    """The contraction's second 128-angle block with one angle (129), full
+    (256) and half full (160: its active epilogue warps end inside a lane
+    quadrant), whole-tile and half-tile items alike: the mixed table against
+    the FP64 one at 1e-6 (phase elements of P11, scalars relative), the FP64
+    table against the oracle."""
+    from geosmie_gb300.table import TablePlan
+    from oracle import integration
+    spec = synthetic_spec(nl=2, nrh=2, ns=300, nbin=nbin, nang=nang)
+    res = []
+    for prec in (0, 1):
+        plan = TablePlan(spec, precision=prec)
+        plan.run()
+        res.append(plan.results())
+        plan.close()
+    a, b = res
+    _check_table(a, integration.run_spec(spec))
+    p11 = np.abs(a["p11"])
+    for k in SCAT:
+        assert np.max(np.abs(b[k] - a[k]) / p11) < 1e-6, k
+    assert np.max(np.abs(b["pback"] - a["pback"]) / np.abs(a["pback"][..., :1])) < 1e-6
+    for k in TIGHT:
+        assert np.max(np.abs(b[k] - a[k]) / np.abs(a[k])) < 1e-6, k
+
+
+@pytest.mark.gpu
 def test_ragged_and_refused_tables_gpu():
     """Size counts that leave partial tiles: 2 and 20 sizes (one partial half
     tile), 33 (a full half tile and one size), 65 (one tile and one size), in
