@@ -198,8 +198,11 @@ __global__ void k_gsf_tc_zero(size_t n, uint4 *__restrict__ p)
 // stage s done), accf[b] (window in TMEM buffer b complete), acce[b] (buffer
 // b read back by the four epilogue warps).  Chunk kc uses stage kc % GT_NS
 // (phase kc / GT_NS); window w uses buffer w & 1 (phase w >> 1).  Every wait
-// is bounded and also ends when another role raised s_abort.
-__global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, int ntn, int nkc,
+// is bounded and also ends when another role raised s_abort.  nsplit > 1:
+// the K chunks of an output tile are split over nsplit blocks (tables with
+// fewer tiles than SMs), each adding its exact int64 sums into the zeroed
+// output with integer atomics, so the result does not depend on the split.
+__global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, int ntn, int nkc, int nsplit,
                                                                const __half *__restrict__ bt, GsfTcBuf buf,
                                                                int *flags)
 {
@@ -208,8 +211,9 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, 
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort_i;
     volatile int *s_abort = &s_abort_i;
-    // block -> (table, M tile, N tile)
-    int blk = blockIdx.x, t = 0, nmt = 0;
+    // block -> (table, M tile, N tile, K split)
+    const int split = blockIdx.x % nsplit;
+    int blk = blockIdx.x / nsplit, t = 0, nmt = 0;
     for (t = 0; t < 4; ++t) {
         nmt = (ntab * c_gt_rows_per_entry[t] + GT_MT - 1) / GT_MT;
         if (blk < nmt * ntn) break;
@@ -218,10 +222,13 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, 
     if (t == 4) return;
     const int mt = blk / ntn, nt = blk % ntn;
     const int rows = ntab * c_gt_rows_per_entry[t];
-    const uint8_t *ga = buf.a + buf.a_off[t] + (size_t)mt * nkc * GT_A_CHUNK;
-    const uint8_t *gb = (const uint8_t *)bt + (size_t)(t * ntn + nt) * nkc * GT_B_CHUNK;
+    // this block's chunks: [k_lo, k_lo + nk) of the tile's nkc
+    const int cps = (nkc + nsplit - 1) / nsplit;
+    const int k_lo = min(nkc, split * cps), nk = min(nkc, k_lo + cps) - k_lo;
+    const uint8_t *ga = buf.a + buf.a_off[t] + ((size_t)mt * nkc + k_lo) * GT_A_CHUNK;
+    const uint8_t *gb = (const uint8_t *)bt + ((size_t)(t * ntn + nt) * nkc + k_lo) * GT_B_CHUNK;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nwin = (nkc + GT_WIN - 1) / GT_WIN;
+    const int nwin = (nk + GT_WIN - 1) / GT_WIN;
     if (warp == 0) tmem_alloc(&s_tmem, GT_TMEM_COLS);
     if (tid == 0) {
         for (int i = 0; i < GT_NS; ++i) {
@@ -252,7 +259,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, 
                 bulk_g2s(st + GT_A_CHUNK, gb + (size_t)kc * GT_B_CHUNK, GT_B_CHUNK, full + kc % GT_NS);
                 last_ld = kc;
             };
-            for (int kc = 0; kc < nkc && kc < GT_NS; ++kc) load(kc);
+            for (int kc = 0; kc < nk && kc < GT_NS; ++kc) load(kc);
             bool ok = true;
             for (int w = 0; w < nwin && ok; ++w) {
                 const int b = w & 1;
@@ -261,7 +268,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, 
                     break;
                 }
                 tc_fence_after();
-                const int k0 = w * GT_WIN, k1 = min(nkc, k0 + GT_WIN);
+                const int k0 = w * GT_WIN, k1 = min(nk, k0 + GT_WIN);
                 for (int kc = k0; kc < k1; ++kc) {
                     if (!mbar_wait_or_abort(full + kc % GT_NS, (kc / GT_NS) & 1u, s_abort)) {
                         ok = false;
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, 
                     mma_commit(empty + kc % GT_NS);
                     // refill the stage of the previous chunk (its MMAs were issued one step ago)
                     const int kp = kc - 1;
-                    if (kp >= 0 && kp + GT_NS < nkc) {
+                    if (kp >= 0 && kp + GT_NS < nk) {
                         if (!mbar_wait_or_abort(empty + kp % GT_NS, (kp / GT_NS) & 1u, s_abort)) {
                             ok = false;
                             break;
@@ -333,10 +340,17 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gsf_tc_gemm(int ntab, int L, 
         __syncwarp();
         const int row = mt * GT_MT + 32 * warp + lane;
         if (!*s_abort && row < rows) {
-            double *c = buf.c + ((size_t)t * buf.rows_cap + row) * buf.lpad + nt * GT_NT;
+            long long *c = buf.c + ((size_t)t * buf.rows_cap + row) * buf.lpad + nt * GT_NT;
+            if (nsplit == 1) {
 #pragma unroll
-            for (int j = 0; j < GT_NT; ++j)
-                if (nt * GT_NT + j < L) c[j] = (double)sum[j];
+                for (int j = 0; j < GT_NT; ++j)
+                    if (nt * GT_NT + j < L) c[j] = sum[j];
+            } else {   // exact: two's complement sums in any order
+#pragma unroll
+                for (int j = 0; j < GT_NT; ++j)
+                    if (nt * GT_NT + j < L && nk > 0)
+                        atomicAdd((unsigned long long *)(c + j), (unsigned long long)sum[j]);
+            }
         }
     }
     tc_fence_before();
@@ -364,7 +378,7 @@ __global__ void k_gsf_tc_finish(int ntab, int L, GsfTcBuf buf, GsfMap map, doubl
                 const int64_t row = (int64_t)e * c_gt_rows_per_entry[t] + sub_of[c];
                 const int ex = buf.rexp[(size_t)t * buf.rows_cap + row];
                 if (ex > -1100)
-                    al[c] = ldexp(buf.c[((size_t)t * buf.rows_cap + row) * buf.lpad + l], ex - 13 - GT_SHIFT);
+                    al[c] = ldexp((double)buf.c[((size_t)t * buf.rows_cap + row) * buf.lpad + l], ex - 13 - GT_SHIFT);
             }
         const double cl = (double)l + 0.5;
         const double a2 = al[2] * cl * 0.5, a3 = al[3] * cl * 0.5;
@@ -404,7 +418,7 @@ int gsf_tc_prepare(gbmie_ctx *ctx, GsfTables *t, int ntab_max)
         a_bytes += (size_t)nmt * nkc * GT_A_CHUNK;
     }
     const size_t bt_bytes = (size_t)4 * ntn * nkc * GT_B_CHUNK;
-    const size_t c_bytes = sizeof(double) * 4 * (size_t)b.rows_cap * b.lpad;
+    const size_t c_bytes = sizeof(long long) * 4 * (size_t)b.rows_cap * b.lpad;
     const size_t e_bytes = sizeof(int) * 4 * (size_t)b.rows_cap;
     const size_t total = align_up(bt_bytes, 256) + align_up(a_bytes, 256) + align_up(c_bytes, 256) + e_bytes;
     GBMIE_TRY(ctx_cuda(ctx, cudaMallocAsync(&t->tc.mem, total, ctx->stream), "gsf tensor-core buffers"));
@@ -413,7 +427,7 @@ int gsf_tc_prepare(gbmie_ctx *ctx, GsfTables *t, int ntab_max)
     p += align_up(bt_bytes, 256);
     b.a = (uint8_t *)p;
     p += align_up(a_bytes, 256);
-    b.c = (double *)p;
+    b.c = (long long *)p;
     p += align_up(c_bytes, 256);
     b.rexp = (int *)p;
     if (nkc > (1 << 16)) return ctx_fail(ctx, GBMIE_ERR_INVALID, "gsf: more than 2^20 Gauss nodes");
@@ -446,8 +460,18 @@ int launch_gsf_expand_tc(gbmie_ctx *ctx, const GsfTables *t, int ntab, const dou
     const size_t smem = GT_SMEM;
     cudaError_t e = cudaFuncSetAttribute(k_gsf_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     GBMIE_TRY(ctx_cuda(ctx, e, "k_gsf_tc_gemm smem attribute"));
+    // K split: tables with fewer output tiles than SMs (one block per SM)
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    int nsplit = nblk > 0 && nblk < nsm ? nsm / nblk : 1;
+    nsplit = max(1, min(nsplit, nkc / 4));   // at least 4 chunks per split
+    if (nsplit > 1) {
+        const size_t c_bytes = sizeof(long long) * 4 * (size_t)t->tc.buf.rows_cap * t->tc.buf.lpad;
+        GBMIE_TRY(ctx_cuda(ctx, cudaMemsetAsync(t->tc.buf.c, 0, c_bytes, st), "gsf split sums"));
+    }
     ctx_pre_launch(ctx);
-    k_gsf_tc_gemm<<<nblk, GT_THREADS, smem, st>>>(ntab, t->L, ntn, nkc, t->tc.bt, t->tc.buf, ctx->d_flags);
+    k_gsf_tc_gemm<<<nblk * nsplit, GT_THREADS, smem, st>>>(ntab, t->L, ntn, nkc, nsplit, t->tc.bt, t->tc.buf,
+                                                          ctx->d_flags);
     GBMIE_TRY(ctx_check_launch(ctx, "k_gsf_tc_gemm"));
     const int thr = t->L >= 256 ? 256 : ((t->L + 31) / 32) * 32;
     ctx_pre_launch(ctx);

@@ -9,7 +9,7 @@
 struct GsfTcBuf {
     uint8_t *a;
     size_t a_off[4];
-    double *c;        // [4][rows_cap][lpad]
+    long long *c;     // [4][rows_cap][lpad] exact integer sums of the digit products
     int *rexp;        // [4][rows_cap]
     int64_t rows_cap;
     int lpad;
